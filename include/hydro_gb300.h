@@ -1,0 +1,129 @@
+/*
+ * hydro_gb300.h -- C ABI of the GB300-native MaHyCo hydro hot path.
+ *
+ * Plain C types only (no C++ or torch types cross this boundary).  Every
+ * call returns an int status: 0 = OK, < 0 = error; hydro_last_error() gives
+ * the message of the last failure on the calling thread.
+ *
+ * What each entry point replaces in the reference (file:line within the
+ * MaHyCo project):
+ *   hydro_spec_default     option structs' defaults: includes/Options.h:9-21,
+ *                          includes/GestionTemps.h:9-18, includes/Limiteurs.h
+ *                          :10-25, includes/Eos.h:10-17, includes/CstMesh.h
+ *   hydro_spec_parse_deck  LectureDonneesClass::LectureDonnees
+ *                          (lecture_donnees/LectureDonnees.cc:12-226)
+ *   hydro_run_create       scheme construction + set-up in main.cc:42-62 and
+ *                          Vnr::simulate (vnr_remap/VnrRemap.cc:289-342) /
+ *                          Eucclhyd::simulate (eucclhyd_remap/EucclhydRemap.cc
+ *                          :233-286): mesh, initial state, dt_init
+ *   hydro_run_step         Vnr::executeTimeLoopN (vnr_remap/VnrRemap.cc
+ *                          :127-253) / Eucclhyd::executeTimeLoopN
+ *                          (eucclhyd_remap/EucclhydRemap.cc:83-195), a bounded
+ *                          number of cycles per call
+ *   hydro_run_fetch        the arrays Vnr::dumpVariables /
+ *                          Eucclhyd::dumpVariables hand to
+ *                          PvdFileWriter2D::writeFile (VnrRemap.cc:255-287,
+ *                          EucclhydRemap.cc:24-64), plus full state fields
+ *   hydro_run_time         GestTemps t_n / deltat_n and the cycle counter n
+ *   hydro_run_error        replaces the exit(1) aborts of the reference
+ *                          (vnr_remap/PhaseRemapFinal.cc:174-196,
+ *                          vnr_remap/PhaseLagrange.cc:358-369,
+ *                          eucclhyd_remap/EucclhydRemap.cc:215-220)
+ */
+#ifndef HYDRO_GB300_H
+#define HYDRO_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Scheme ids (includes/SchemaLagrange.h:10-15). */
+#define HYDRO_SCHEME_EUCCLHYD 2000
+#define HYDRO_SCHEME_VNR 2001
+
+/* Limiter ids (includes/Limiteurs.h:10-25). */
+#define HYDRO_LIM_MINMOD 300
+#define HYDRO_LIM_SUPERBEE 301
+#define HYDRO_LIM_VANLEER 302
+#define HYDRO_LIM_MINMODG 1300
+#define HYDRO_LIM_SUPERBEEG 1301
+#define HYDRO_LIM_VANLEERG 1302
+#define HYDRO_LIM_ARITHMETICG 1303
+#define HYDRO_LIM_ULTRABEEG 1304
+
+/* EOS ids (includes/Eos.h:10-14). */
+#define HYDRO_EOS_VOID 100
+#define HYDRO_EOS_PERFECT_GAS 101
+
+/* Device error word bits (sticky per run). */
+#define HYDRO_ERR_NAN 0x1u          /* NaN density/energy after remap       */
+#define HYDRO_ERR_ENERGY 0x2u       /* |e_mat| > 5 in the VNR energy update */
+#define HYDRO_ERR_DT_MIN 0x4u       /* dt < deltat_min (Eucclhyd)           */
+#define HYDRO_ERR_NEGATIVE 0x8u     /* negative mass/energy zeroed (info)   */
+
+/* Options of one hydro run.  Field meaning mirrors the reference's option
+ * structs; hydro_spec_default() fills the reference defaults. */
+typedef struct hydro_spec {
+  int scheme;            /* HYDRO_SCHEME_*                                  */
+  int test_case;         /* CasTest id (includes/CasTest.h:10-32)           */
+  int nx, ny;            /* cells in x / y                                  */
+  double dx, dy;         /* cell sizes (X_EDGE_LENGTH / Y_EDGE_LENGTH)      */
+  int nbmat;             /* 1..3                                            */
+  int eos[3];            /* HYDRO_EOS_* per material                        */
+  double gamma[3];       /* Eos::gammap                                     */
+  double gamma_scalar;   /* Eos::gamma (VNR pseudo-viscosity, init)         */
+  double final_time;
+  double output_time;
+  double dt_init;        /* deck value; VNR with Lagrange recomputes it     */
+  double dt_min;
+  double cfl;            /* GestTemps::cfl (Eucclhyd; VNR hard-codes its own)*/
+  long max_cycles;       /* stop after this many cycles; 0 = no cap         */
+  int space_order;
+  int projection;        /* AvecProjection                                  */
+  int projection_conservative;
+  int projection_order;  /* 1, 2 or 3                                       */
+  double threshold;
+  int limiter;           /* projectionLimiterId                             */
+  int pb;                /* projectionAvecPlateauPente                      */
+  int pb_mixte;          /* projectionLimiteurMixte                         */
+  int limiter_pure;      /* projectionLimiterIdPure                         */
+  int pb_complet;        /* projectionPlateauPenteComplet                   */
+  int pseudo_centree;
+  int dual_mass_flux;    /* methode_flux_masse: 0 A1, 1 A2, 2 PB            */
+  int sans_lagrange;     /* advection cases: no Lagrange phase              */
+  int init_variant;      /* 0 reference init; 1 bi-material Sod with a 50/50
+                            mixed cell row/column at the interface          */
+  double energy_limit;   /* VNR aborts when |e_mat| exceeds it (5 in the
+                            reference, vnr_remap/PhaseLagrange.cc:358);
+                            <= 0 disables the check                         */
+} hydro_spec;
+
+typedef struct hydro_ctx hydro_ctx;  /* device, streams, arena            */
+typedef struct hydro_run hydro_run;  /* one mesh instance resident in HBM  */
+
+const char* hydro_last_error(void);
+
+int hydro_spec_default(hydro_spec* spec);
+int hydro_spec_parse_deck(const char* path, hydro_spec* spec);
+
+int hydro_ctx_create(int device, size_t hbm_budget_bytes, hydro_ctx** out);
+void hydro_ctx_destroy(hydro_ctx* ctx);
+
+int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out);
+/* Advance at most ncycles cycles (stops early at final_time / max_cycles);
+ * *done is set to 1 once the reference loop condition ends the run. */
+int hydro_run_step(hydro_run* run, int ncycles, int* done);
+/* Copy a named field (see hydro_run_field_size) into host memory. */
+int hydro_run_fetch(hydro_run* run, const char* field, double* host_dst,
+                    size_t n);
+size_t hydro_run_field_size(hydro_run* run, const char* field);
+int hydro_run_time(hydro_run* run, double* t, double* dt, long* cycle);
+int hydro_run_error(hydro_run* run, unsigned* code, long* cell);
+int hydro_run_destroy(hydro_run* run);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYDRO_GB300_H */

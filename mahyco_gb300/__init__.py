@@ -1,0 +1,228 @@
+"""GB300-native implementation of MaHyCo's per-cycle hydro hot path.
+
+Python mirror of the reference's entry points, bound to the C ABI of
+include/hydro_gb300.h (libmahyco_gb300.so, built in-tree by
+mahyco_gb300.build):
+
+  parse_deck(path)          LectureDonnees (lecture_donnees/LectureDonnees.cc)
+  Run(spec).simulate()      Vnr::simulate (vnr_remap/VnrRemap.cc:289-346)
+  Run.step(n)               cycles of Vnr::executeTimeLoopN (VnrRemap.cc:127)
+  Run.fetch(name)           the arrays dumpVariables writes (VnrRemap.cc:255)
+
+There is no CPU fallback: every call runs the CUDA kernels, and importing
+this module without the built library, or calling it without a GPU, raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libmahyco_gb300.so"
+
+SCHEME_EUCCLHYD = 2000
+SCHEME_VNR = 2001
+LIMITERS = {"minmod": 300, "superBee": 301, "vanLeer": 302, "minmodG": 1300,
+            "superBeeG": 1301, "vanLeerG": 1302, "arithmeticG": 1303,
+            "ultrabeeG": 1304}
+ERR_NAN, ERR_ENERGY, ERR_DT_MIN, ERR_NEGATIVE = 1, 2, 4, 8
+
+
+class HydroSpec(C.Structure):
+    """ctypes mirror of struct hydro_spec (include/hydro_gb300.h)."""
+
+    _fields_ = [
+        ("scheme", C.c_int), ("test_case", C.c_int), ("nx", C.c_int),
+        ("ny", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
+        ("nbmat", C.c_int), ("eos", C.c_int * 3), ("gamma", C.c_double * 3),
+        ("gamma_scalar", C.c_double), ("final_time", C.c_double),
+        ("output_time", C.c_double), ("dt_init", C.c_double),
+        ("dt_min", C.c_double), ("cfl", C.c_double), ("max_cycles", C.c_long),
+        ("space_order", C.c_int), ("projection", C.c_int),
+        ("projection_conservative", C.c_int), ("projection_order", C.c_int),
+        ("threshold", C.c_double), ("limiter", C.c_int), ("pb", C.c_int),
+        ("pb_mixte", C.c_int), ("limiter_pure", C.c_int),
+        ("pb_complet", C.c_int), ("pseudo_centree", C.c_int),
+        ("dual_mass_flux", C.c_int), ("sans_lagrange", C.c_int),
+        ("init_variant", C.c_int), ("energy_limit", C.c_double),
+    ]
+
+    def copy(self) -> "HydroSpec":
+        s = HydroSpec()
+        C.pointer(s)[0] = self
+        return s
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            val = getattr(self, name)
+            out[name] = list(val) if hasattr(val, "__len__") else val
+        return out
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libmahyco_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: run `python -m mahyco_gb300.build` "
+                "(the CUDA path has no CPU fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        vp, i, sz = C.c_void_p, C.c_int, C.c_size_t
+        L.hydro_last_error.restype = C.c_char_p
+        L.hydro_spec_default.argtypes = [C.POINTER(HydroSpec)]
+        L.hydro_spec_parse_deck.argtypes = [C.c_char_p, C.POINTER(HydroSpec)]
+        L.hydro_ctx_create.argtypes = [i, sz, C.POINTER(vp)]
+        L.hydro_ctx_destroy.argtypes = [vp]
+        L.hydro_ctx_destroy.restype = None
+        L.hydro_ctx_stream.argtypes = [vp]
+        L.hydro_ctx_stream.restype = vp
+        L.hydro_run_create.argtypes = [vp, C.POINTER(HydroSpec), C.POINTER(vp)]
+        L.hydro_run_step.argtypes = [vp, i, C.POINTER(i)]
+        L.hydro_run_enqueue.argtypes = [vp, i]
+        L.hydro_run_sync.argtypes = [vp, C.POINTER(i)]
+        L.hydro_run_fetch.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), sz]
+        L.hydro_run_field_size.argtypes = [vp, C.c_char_p]
+        L.hydro_run_field_size.restype = sz
+        L.hydro_run_time.argtypes = [vp, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_long)]
+        L.hydro_run_error.argtypes = [vp, C.POINTER(C.c_uint), C.POINTER(C.c_long)]
+        L.hydro_run_destroy.argtypes = [vp]
+        L.hydro_run_kernel_launches.argtypes = [vp]
+        L.hydro_run_kernel_launches.restype = C.c_longlong
+        L.hydro_run_device_bytes.argtypes = [vp]
+        L.hydro_run_device_bytes.restype = sz
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = lib().hydro_last_error().decode(errors="replace")
+        raise RuntimeError(f"{what} failed ({rc}): {msg}")
+
+
+def default_spec() -> HydroSpec:
+    s = HydroSpec()
+    _check(lib().hydro_spec_default(C.byref(s)), "hydro_spec_default")
+    return s
+
+
+def parse_deck(path: str | os.PathLike) -> HydroSpec:
+    """Reads a MaHyCo input deck (donnees.txt) into a HydroSpec."""
+    s = HydroSpec()
+    _check(lib().hydro_spec_parse_deck(str(path).encode(), C.byref(s)),
+           "hydro_spec_parse_deck")
+    return s
+
+
+class Context:
+    """One GPU, one CUDA stream, an optional HBM budget."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self.h = C.c_void_p()
+        _check(lib().hydro_ctx_create(device, hbm_budget, C.byref(self.h)),
+               "hydro_ctx_create")
+
+    def close(self):
+        if self.h:
+            lib().hydro_ctx_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return lib().hydro_ctx_stream(self.h) or 0
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class Run:
+    """One hydro run resident in HBM (a Vnr scheme instance)."""
+
+    def __init__(self, spec: HydroSpec, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.spec = spec
+        self.h = C.c_void_p()
+        _check(lib().hydro_run_create(self.ctx.h, C.byref(spec), C.byref(self.h)),
+               "hydro_run_create")
+
+    def close(self):
+        if self.h:
+            lib().hydro_run_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, ncycles: int = 1) -> bool:
+        """Runs up to ncycles cycles; returns True once the run has ended."""
+        done = C.c_int(0)
+        _check(lib().hydro_run_step(self.h, ncycles, C.byref(done)), "hydro_run_step")
+        return bool(done.value)
+
+    def enqueue(self, ncycles: int) -> None:
+        _check(lib().hydro_run_enqueue(self.h, ncycles), "hydro_run_enqueue")
+
+    def sync(self) -> bool:
+        done = C.c_int(0)
+        _check(lib().hydro_run_sync(self.h, C.byref(done)), "hydro_run_sync")
+        return bool(done.value)
+
+    def simulate(self, chunk: int = 64) -> None:
+        """Runs to the end (final time or cycle cap)."""
+        while not self.step(chunk):
+            pass
+
+    def fetch(self, name: str) -> np.ndarray:
+        n = lib().hydro_run_field_size(self.h, name.encode())
+        if n == 0:
+            raise KeyError(name)
+        out = np.empty(n, dtype=np.float64)
+        _check(lib().hydro_run_fetch(self.h, name.encode(),
+                                     out.ctypes.data_as(C.POINTER(C.c_double)), n),
+               "hydro_run_fetch")
+        return out
+
+    def time(self):
+        t, dt, n = C.c_double(), C.c_double(), C.c_long()
+        _check(lib().hydro_run_time(self.h, C.byref(t), C.byref(dt), C.byref(n)),
+               "hydro_run_time")
+        return t.value, dt.value, n.value
+
+    def error(self):
+        code, cell = C.c_uint(), C.c_long()
+        _check(lib().hydro_run_error(self.h, C.byref(code), C.byref(cell)),
+               "hydro_run_error")
+        return code.value, cell.value
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().hydro_run_kernel_launches(self.h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().hydro_run_device_bytes(self.h))

@@ -1,0 +1,540 @@
+// Host runtime of the GB300 hydro path: context, per-run HBM arena, cycle
+// loop (CUDA-graph replay), field fetch and the public C ABI of
+// include/hydro_gb300.h.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../internal.h"
+#include "init.h"
+
+namespace hydro {
+
+static thread_local std::string g_last_error;
+
+int fail(int rc, const std::string& msg) {
+  g_last_error = msg;
+  return rc;
+}
+
+void launch_prologue(const RunView& v, cudaStream_t s);
+int launch_cycle(const RunView& v, cudaStream_t s);
+
+#define CUDA_TRY(expr)                                                     \
+  do {                                                                     \
+    cudaError_t e_ = (expr);                                               \
+    if (e_ != cudaSuccess)                                                 \
+      return fail(-100, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+}  // namespace hydro
+
+using namespace hydro;
+
+struct hydro_ctx {
+  int device = 0;
+  size_t budget = 0;
+  size_t used = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+};
+
+struct hydro_run {
+  hydro_ctx* ctx = nullptr;
+  hydro_spec spec{};
+  RunView v{};
+  HostInit init;     // kept for the Euler geometry / sizes
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  Ctrl* d_ctrl = nullptr;
+  Ctrl h_ctrl{};
+  cudaGraphExec_t graph = nullptr;
+  int graph_cycles = 0;
+  int kernels_per_cycle = 0;
+  long long kernels_launched = 0;
+};
+
+namespace {
+
+long long round_up(long long n, long long a) { return (n + a - 1) / a * a; }
+
+// Bump allocator over one device allocation.
+struct Carve {
+  char* base;
+  size_t off = 0;
+  template <class T>
+  T* take(long long count) {
+    size_t bytes = (size_t)count * sizeof(T);
+    size_t at = (off + 255) & ~(size_t)255;
+    off = at + bytes;
+    return base ? reinterpret_cast<T*>(base + at) : nullptr;
+  }
+};
+
+// Lays out every device array of a run; with base == nullptr it only sizes.
+size_t layout(RunView& v, char* base) {
+  Carve a{base};
+  const long long P = v.pitch, NP = v.npitch, FP = v.fpitch;
+  const int nb = v.nbmat, nc = v.ncomp;
+  v.rho = a.take<double>(P);
+  v.p = a.take<double>(P);
+  v.c = a.take<double>(P);
+  v.e = a.take<double>(P);
+  v.q = a.take<double>(P);
+  v.divu = a.take<double>(P);
+  v.cell_mass = a.take<double>(P);
+  v.rhom = a.take<double>(nb * P);
+  v.pm = a.take<double>(nb * P);
+  v.cm = a.take<double>(nb * P);
+  v.em = a.take<double>(nb * P);
+  v.qm = a.take<double>(nb * P);
+  v.fm = a.take<double>(nb * P);
+  v.mfm = a.take<double>(nb * P);
+  v.cmassm = a.take<double>(nb * P);
+  v.mixte = a.take<int>(P);
+  v.pure = a.take<int>(P);
+  v.u = a.take<double>(2 * NP);
+  v.node_mass = a.take<double>(NP);
+  v.speed = a.take<double>(NP);
+  v.XL = a.take<double>(2 * NP);
+  v.vL = a.take<double>(P);
+  v.rL = a.take<double>(P);
+  v.XcL = a.take<double>(2 * P);
+  v.Hx = a.take<double>(P);
+  v.Hy = a.take<double>(P);
+  v.UL = a.take<double>(nc * P);
+  v.Phi = a.take<double>(nc * P);
+  v.U1 = a.take<double>(nc * P);
+  v.gP = a.take<double>(nc * P);
+  v.dPAv = a.take<double>(nc * P);
+  v.dPAr = a.take<double>(nc * P);
+  v.DPF = a.take<double>(nb * P);
+  v.phiF = a.take<double>(nc * FP);
+  v.FFd = a.take<double>(2 * nb * P);
+  v.DPv = a.take<double>(2 * NP);
+  v.gD = a.take<double>(2 * NP);
+  v.UD1 = a.take<double>(3 * NP);
+  v.xs = a.take<double>(v.nx + 1);
+  v.ys = a.take<double>(v.ny + 1);
+  v.cqs = a.take<double>(8 * P);
+  v.cflsq = a.take<double>(P);
+  v.s0 = a.take<double>(P);
+  v.sqs0 = a.take<double>(P);
+  v.nout = a.take<double>(4 * P);
+  v.flv = a.take<double>(v.ny);
+  v.flh = a.take<double>(v.nx);
+  v.rho0_left = a.take<double>(v.ny);
+  v.ctrl = a.take<Ctrl>(1);
+  return a.off + 256;
+}
+
+// Copies nplanes host planes of n values (host stride hs) into device planes
+// of stride ds.
+int upload(double* dst, long long ds, const std::vector<double>& src,
+           long long hs, int nplanes, long long n, cudaStream_t s) {
+  for (int k = 0; k < nplanes; ++k)
+    CUDA_TRY(cudaMemcpyAsync(dst + k * ds, src.data() + k * hs,
+                             (size_t)n * sizeof(double),
+                             cudaMemcpyHostToDevice, s));
+  return 0;
+}
+
+int validate(const hydro_spec& s) {
+  if (s.scheme != HYDRO_SCHEME_VNR)
+    return fail(-20, "the GPU path currently implements the VNR scheme");
+  if (s.projection != 1)
+    return fail(-21, "the GPU path requires the remap (AvecProjection = oui)");
+  if (s.nbmat < 1 || s.nbmat > 3) return fail(-22, "nbmat must be 1..3");
+  if (s.projection_order < 1 || s.projection_order > 3)
+    return fail(-23, "projection order must be 1, 2 or 3");
+  if (s.nx < 2 || s.ny < 2) return fail(-24, "nx and ny must be >= 2");
+  for (int m = 0; m < s.nbmat; ++m)
+    if (s.eos[m] != HYDRO_EOS_PERFECT_GAS && s.eos[m] != HYDRO_EOS_VOID)
+      return fail(-25, "only PerfectGas and Void equations of state exist in "
+                       "the reference (others only print)");
+  if (s.dual_mass_flux < 0 || s.dual_mass_flux > 2)
+    return fail(-26, "dual mass-flux method must be A1, A2 or PB");
+  if (s.dual_mass_flux == 2 && !(s.pb == 1 && s.projection_order > 1))
+    return fail(-27, "the PB dual mass flux needs PenteBorne and order > 1");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hydro_last_error(void) { return g_last_error.c_str(); }
+
+int hydro_ctx_create(int device, size_t budget, hydro_ctx** out) {
+  if (!out) return fail(-1, "hydro_ctx_create: null out");
+  int n = 0;
+  CUDA_TRY(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n)
+    return fail(-2, "hydro_ctx_create: no CUDA device " + std::to_string(device));
+  CUDA_TRY(cudaSetDevice(device));
+  auto* c = new hydro_ctx();
+  c->device = device;
+  c->budget = budget;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(-3, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+  }
+  *out = c;
+  return 0;
+}
+
+void hydro_ctx_destroy(hydro_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out) {
+  if (!ctx || !spec || !out) return fail(-1, "hydro_run_create: null argument");
+  if (int rc = validate(*spec)) return rc;
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  auto* r = new hydro_run();
+  r->ctx = ctx;
+  r->spec = *spec;
+  if (int rc = build_initial_state(*spec, r->init)) {
+    delete r;
+    return rc;
+  }
+  const HostInit& h = r->init;
+  RunView& v = r->v;
+  v.nx = spec->nx;
+  v.ny = spec->ny;
+  v.nc = h.nc;
+  v.nn = h.nn;
+  v.pitch = round_up(h.nc, 32);
+  v.npitch = round_up(h.nn, 32);
+  v.fpitch = round_up(std::max((long long)(spec->nx + 1) * spec->ny,
+                               (long long)spec->nx * (spec->ny + 1)),
+                      32);
+  v.nbmat = spec->nbmat;
+  v.ncomp = 3 * spec->nbmat + 1;
+  for (int k = 0; k < kMaxComp; ++k) v.comp_ref[k] = -1;
+  for (int k = 0; k < 3 * spec->nbmat; ++k) v.comp_ref[k] = k;
+  v.comp_ref[3 * spec->nbmat] = 3 * spec->nbmat + 3;
+  v.scheme = spec->scheme;
+  v.order = spec->projection_order;
+  v.pb = spec->pb;
+  v.pb_mixte = spec->pb_mixte;
+  v.pb_complet = spec->pb_complet;
+  v.limiter = spec->limiter;
+  v.limiter_pure = spec->limiter_pure;
+  v.dual_method = spec->dual_mass_flux;
+  v.pseudo_centree = spec->pseudo_centree;
+  v.sans_lagrange = spec->sans_lagrange;
+  v.projection = spec->projection;
+  v.conservative = spec->projection_conservative;
+  for (int m = 0; m < 3; ++m) {
+    v.eos[m] = spec->eos[m];
+    v.gamma[m] = spec->gamma[m];
+  }
+  v.threshold = spec->threshold;
+  v.gamma_scalar = spec->gamma_scalar;
+  v.energy_limit = spec->energy_limit;
+  v.dx = spec->dx;
+  v.dy = spec->dy;
+  v.euler_volume = spec->dx * spec->dy;
+  v.dt_min = spec->dt_min;
+  v.final_time = spec->final_time;
+  v.cfl = spec->cfl;
+  v.max_iter = spec->max_cycles > 0 ? spec->max_cycles + 1 : 500000000LL;
+  v.bc_left = h.bc_left;
+  v.bc_right = h.bc_right;
+  v.bc_bottom = h.bc_bottom;
+  v.bc_top = h.bc_top;
+  for (int d = 0; d < 2; ++d) {
+    v.v_left[d] = h.v_left[d];
+    v.v_right[d] = h.v_right[d];
+    v.v_bottom[d] = h.v_bottom[d];
+    v.v_top[d] = h.v_top[d];
+  }
+  v.periodic_x = h.periodic_x;
+
+  const size_t bytes = layout(v, nullptr);
+  if (ctx->budget && ctx->used + bytes > ctx->budget) {
+    delete r;
+    return fail(-30, "HBM budget exceeded");
+  }
+  cudaError_t e = cudaMalloc(&r->arena, bytes);
+  if (e != cudaSuccess) {
+    delete r;
+    return fail(-31, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  r->arena_bytes = bytes;
+  ctx->used += bytes;
+  layout(v, (char*)r->arena);
+  r->d_ctrl = v.ctrl;
+  cudaStream_t s = ctx->stream;
+  int rc = 0;
+  auto cp = [&](const double* dst, const std::vector<double>& src) {
+    if (rc) return;
+    cudaError_t ee = cudaMemcpyAsync((void*)dst, src.data(),
+                                     src.size() * sizeof(double),
+                                     cudaMemcpyHostToDevice, s);
+    if (ee != cudaSuccess) rc = fail(-32, cudaGetErrorString(ee));
+  };
+  CUDA_TRY(cudaMemsetAsync(r->arena, 0, bytes, s));
+  const long long nc = h.nc, nn = h.nn, P = v.pitch, NP = v.npitch;
+  const int nb = v.nbmat;
+  rc = rc ? rc : upload(v.rho, P, h.rho, nc, 1, nc, s);
+  rc = rc ? rc : upload(v.p, P, h.p, nc, 1, nc, s);
+  rc = rc ? rc : upload(v.c, P, h.c, nc, 1, nc, s);
+  rc = rc ? rc : upload(v.e, P, h.e, nc, 1, nc, s);
+  rc = rc ? rc : upload(v.q, P, h.q, nc, 1, nc, s);
+  rc = rc ? rc : upload(v.divu, P, h.divu, nc, 1, nc, s);
+  rc = rc ? rc : upload(v.cell_mass, P, h.cell_mass, nc, 1, nc, s);
+  rc = rc ? rc : upload(v.rhom, P, h.rhom, nc, nb, nc, s);
+  rc = rc ? rc : upload(v.pm, P, h.pm, nc, nb, nc, s);
+  rc = rc ? rc : upload(v.cm, P, h.cm, nc, nb, nc, s);
+  rc = rc ? rc : upload(v.em, P, h.em, nc, nb, nc, s);
+  rc = rc ? rc : upload(v.qm, P, h.qm, nc, nb, nc, s);
+  rc = rc ? rc : upload(v.fm, P, h.fm, nc, nb, nc, s);
+  rc = rc ? rc : upload(v.mfm, P, h.mfm, nc, nb, nc, s);
+  rc = rc ? rc : upload(v.cmassm, P, h.cmassm, nc, nb, nc, s);
+  rc = rc ? rc : upload(v.u, NP, h.u, nn, 2, nn, s);
+  rc = rc ? rc : upload(const_cast<double*>(v.cqs), P, h.cqs, nc, 8, nc, s);
+  rc = rc ? rc : upload(const_cast<double*>(v.nout), P, h.nout, nc, 4, nc, s);
+  cp(v.cflsq, h.cflsq);
+  cp(v.s0, h.s0);
+  cp(v.sqs0, h.sqs0);
+  cp(v.xs, h.xs);
+  cp(v.ys, h.ys);
+  cp(v.flv, h.flv);
+  cp(v.flh, h.flh);
+  cp(v.rho0_left, h.rho0_left);
+  cp(v.node_mass, h.node_mass);
+  if (!rc) {
+    CUDA_TRY(cudaMemcpyAsync(v.mixte, h.mixte.data(), nc * sizeof(int),
+                             cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(v.pure, h.pure.data(), nc * sizeof(int),
+                             cudaMemcpyHostToDevice, s));
+  }
+  Ctrl c0{};
+  c0.t_n = 0.0;
+  c0.dt_n = h.dt_init;
+  c0.n = 0;
+  c0.done = 0;
+  c0.active = 0;
+  c0.x_then_y = 1;
+  c0.err = 0;
+  c0.err_cell = LLONG_MAX;
+  c0.dt_min_bits = 0xFFEFFFFFFFFFFFFFull;  // ordered encoding of +DBL_MAX
+  c0.pmax_bits = 0x0010000000000000ull;    // ordered encoding of -DBL_MAX
+  r->h_ctrl = c0;
+  if (!rc)
+    rc = cudaMemcpyAsync(r->d_ctrl, &c0, sizeof(Ctrl), cudaMemcpyHostToDevice,
+                         s) == cudaSuccess
+             ? 0
+             : fail(-33, "ctrl upload");
+  if (!rc) launch_prologue(v, s);
+  if (!rc && cudaStreamSynchronize(s) != cudaSuccess)
+    rc = fail(-34, std::string("initial upload: ") +
+                       cudaGetErrorString(cudaGetLastError()));
+  if (rc) {
+    cudaFree(r->arena);
+    ctx->used -= bytes;
+    delete r;
+    return rc;
+  }
+  *out = r;
+  return 0;
+}
+
+int hydro_run_destroy(hydro_run* r) {
+  if (!r) return 0;
+  cudaSetDevice(r->ctx->device);
+  if (r->graph) cudaGraphExecDestroy(r->graph);
+  if (r->arena) cudaFree(r->arena);
+  r->ctx->used -= r->arena_bytes;
+  delete r;
+  return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Captures `cycles` consecutive cycles of one run into a CUDA graph.
+int build_graph(hydro_run* r, int cycles) {
+  cudaStream_t s = r->ctx->stream;
+  if (r->graph) {
+    cudaGraphExecDestroy(r->graph);
+    r->graph = nullptr;
+  }
+  cudaGraph_t g;
+  CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int nk = 0;
+  for (int k = 0; k < cycles; ++k) nk = launch_cycle(r->v, s);
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (e != cudaSuccess) return fail(-40, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&r->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(-41, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  r->graph_cycles = cycles;
+  r->kernels_per_cycle = nk;
+  return 0;
+}
+
+int sync_ctrl(hydro_run* r) {
+  cudaStream_t s = r->ctx->stream;
+  CUDA_TRY(cudaMemcpyAsync(&r->h_ctrl, r->d_ctrl, sizeof(Ctrl),
+                           cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Enqueues ncycles cycles without waiting (graph replays of 8 cycles plus
+// single-cycle launches for the remainder).
+int hydro_run_enqueue(hydro_run* r, int ncycles) {
+  if (!r) return fail(-1, "null run");
+  CUDA_TRY(cudaSetDevice(r->ctx->device));
+  const int G = 8;
+  if (!r->graph) {
+    if (int rc = build_graph(r, G)) return rc;
+  }
+  cudaStream_t s = r->ctx->stream;
+  int left = ncycles;
+  while (left >= r->graph_cycles) {
+    CUDA_TRY(cudaGraphLaunch(r->graph, s));
+    left -= r->graph_cycles;
+    r->kernels_launched += (long long)r->graph_cycles * r->kernels_per_cycle;
+  }
+  for (int k = 0; k < left; ++k) {
+    r->kernels_launched += launch_cycle(r->v, s);
+  }
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int hydro_run_step(hydro_run* r, int ncycles, int* done) {
+  if (!r) return fail(-1, "null run");
+  if (int rc = hydro_run_enqueue(r, ncycles)) return rc;
+  if (int rc = sync_ctrl(r)) return rc;
+  if (done) *done = r->h_ctrl.done;
+  return 0;
+}
+
+int hydro_run_sync(hydro_run* r, int* done) {
+  if (!r) return fail(-1, "null run");
+  if (int rc = sync_ctrl(r)) return rc;
+  if (done) *done = r->h_ctrl.done;
+  return 0;
+}
+
+int hydro_run_time(hydro_run* r, double* t, double* dt, long* cycle) {
+  if (!r) return fail(-1, "null run");
+  if (int rc = sync_ctrl(r)) return rc;
+  if (t) *t = r->h_ctrl.t_n;
+  if (dt) *dt = r->h_ctrl.dt_n;
+  if (cycle) *cycle = (long)r->h_ctrl.n;
+  return 0;
+}
+
+int hydro_run_error(hydro_run* r, unsigned* code, long* cell) {
+  if (!r) return fail(-1, "null run");
+  if (int rc = sync_ctrl(r)) return rc;
+  if (code) *code = r->h_ctrl.err;
+  if (cell) *cell = r->h_ctrl.err_cell == LLONG_MAX ? -1 : (long)r->h_ctrl.err_cell;
+  return 0;
+}
+
+long long hydro_run_kernel_launches(hydro_run* r) {
+  return r ? r->kernels_launched : 0;
+}
+
+size_t hydro_run_field_size(hydro_run* r, const char* f) {
+  if (!r || !f) return 0;
+  const size_t nc = (size_t)r->v.nc, nn = (size_t)r->v.nn;
+  static const char* cell1[] = {"density", "pressure", "energy", "sound_speed",
+                                "pseudo", "divu", "cell_mass"};
+  for (auto n : cell1)
+    if (!strcmp(f, n)) return nc;
+  static const char* cell3[] = {"density_env", "energy_env", "pressure_env",
+                                "fracvol_env", "mass_fraction_env"};
+  for (auto n : cell3)
+    if (!strcmp(f, n)) return 3 * nc;
+  if (!strcmp(f, "node_velocity")) return 2 * nn;
+  if (!strcmp(f, "node_mass")) return nn;
+  return 0;
+}
+
+// Copies a field to host memory.  Per-material fields use the reference's
+// layout (3 values per cell, zero for absent material slots); node_velocity
+// is (u, v) per node.
+int hydro_run_fetch(hydro_run* r, const char* f, double* dst, size_t n) {
+  if (!r || !f || !dst) return fail(-1, "hydro_run_fetch: null argument");
+  const size_t want = hydro_run_field_size(r, f);
+  if (!want) return fail(-2, std::string("unknown field ") + f);
+  if (n != want) return fail(-3, "hydro_run_fetch: wrong size for " + std::string(f));
+  CUDA_TRY(cudaSetDevice(r->ctx->device));
+  cudaStream_t s = r->ctx->stream;
+  const RunView& v = r->v;
+  const long long nc = v.nc, nn = v.nn;
+  auto get = [&](const double* src, long long cnt, std::vector<double>& out) {
+    out.resize(cnt);
+    return cudaMemcpyAsync(out.data(), src, cnt * sizeof(double),
+                           cudaMemcpyDeviceToHost, s);
+  };
+  std::vector<double> tmp;
+  const double* one = nullptr;
+  if (!strcmp(f, "density")) one = v.rho;
+  else if (!strcmp(f, "pressure")) one = v.p;
+  else if (!strcmp(f, "energy")) one = v.e;
+  else if (!strcmp(f, "sound_speed")) one = v.c;
+  else if (!strcmp(f, "pseudo")) one = v.q;
+  else if (!strcmp(f, "divu")) one = v.divu;
+  else if (!strcmp(f, "cell_mass")) one = v.cell_mass;
+  else if (!strcmp(f, "node_mass")) one = v.node_mass;
+  if (one) {
+    CUDA_TRY(cudaMemcpyAsync(dst, one, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return 0;
+  }
+  const double* planes = nullptr;
+  if (!strcmp(f, "density_env")) planes = v.rhom;
+  else if (!strcmp(f, "energy_env")) planes = v.em;
+  else if (!strcmp(f, "pressure_env")) planes = v.pm;
+  else if (!strcmp(f, "fracvol_env")) planes = v.fm;
+  else if (!strcmp(f, "mass_fraction_env")) planes = v.mfm;
+  if (planes) {
+    CUDA_TRY(get(planes, v.nbmat * v.pitch, tmp));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    for (long long c = 0; c < nc; ++c)
+      for (int m = 0; m < 3; ++m)
+        dst[3 * c + m] = m < v.nbmat ? tmp[m * v.pitch + c] : 0.0;
+    return 0;
+  }
+  if (!strcmp(f, "node_velocity")) {
+    CUDA_TRY(get(v.u, 2 * v.npitch, tmp));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    for (long long p = 0; p < nn; ++p) {
+      dst[2 * p] = tmp[p];
+      dst[2 * p + 1] = tmp[v.npitch + p];
+    }
+    return 0;
+  }
+  return fail(-2, std::string("unknown field ") + f);
+}
+
+// Stream of the context (for host code that records CUDA events around
+// enqueued cycles).
+void* hydro_ctx_stream(hydro_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+size_t hydro_run_device_bytes(hydro_run* r) { return r ? r->arena_bytes : 0; }
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+// Internal declarations shared by the host runtime (.cc) and the CUDA
+// kernels (.cu) of the GB300 hydro path.  Not part of the public ABI.
+#ifndef MAHYCO_GB300_INTERNAL_H
+#define MAHYCO_GB300_INTERNAL_H
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "hydro_gb300.h"
+
+namespace hydro {
+
+// Sets the thread's last-error message and returns rc.
+int fail(int rc, const std::string& msg);
+
+// includes/ConditionsLimites.h:14-17
+constexpr int kBcSym = 200;
+constexpr int kBcImposed = 201;
+constexpr int kBcPeriodic = 203;
+
+// Number of conserved components carried through the remap.  The reference
+// carries 13 (nbequamax, includes/Constantes.h:9-13); for nbmat materials
+// only 3*nbmat+4 are ever non-zero, and the VNR scheme leaves the three
+// velocity / kinetic-energy slots at zero too (vnr_remap/PrepareRemap.cc
+// :121-123), so VNR remaps 3*nbmat+1 "live" slots: volumes, masses,
+// energies, pseudo-viscosity.  Slot k of the device arrays maps to reference
+// slot ref_slot(k).
+constexpr int kMaxComp = 13;
+
+// Device-side view of one run: sizes, options and raw device pointers.
+// All cell arrays are SoA planes of `pitch` doubles (pitch >= nc, multiple
+// of 32); per-material and per-component arrays are consecutive planes.
+struct RunView {
+  // ---- sizes
+  int nx, ny;
+  long long nc, nn;
+  long long pitch;   // cell plane stride
+  long long npitch;  // node plane stride
+  long long fpitch;  // face-value plane stride
+  int nbmat;
+  int ncomp;         // live remap components
+  int comp_ref[kMaxComp];
+
+  // ---- options (reference option structs)
+  int scheme;
+  int order, pb, pb_mixte, pb_complet, limiter, limiter_pure, dual_method;
+  int pseudo_centree, sans_lagrange, projection, conservative;
+  int eos[3];
+  double threshold, gamma[3], gamma_scalar, energy_limit;
+  double dx, dy, euler_volume, dt_min, final_time, cfl;
+  long long max_iter;
+
+  // ---- boundary conditions (Cdl)
+  int bc_left, bc_right, bc_bottom, bc_top;
+  double v_left[2], v_right[2], v_bottom[2], v_top[2];
+  int periodic_x;
+
+  // ---- constant Euler geometry
+  const double* xs;      // nx+1 node abscissae (dx * j)
+  const double* ys;      // ny+1 node ordinates (dy * i)
+  const double* cqs;     // 8 planes: corner normals, [(k*2+d)]
+  const double* cflsq;   // cfl * sqrt(sum of initial sub-volumes)
+  const double* s0;      // sum of initial sub-volumes
+  const double* sqs0;    // sqrt(s0)
+  const double* nout;    // 4 planes: outer normal components (L.x,R.x,B.y,T.y)
+  const double* flv;     // ny   Euler lengths of vertical faces per row
+  const double* flh;     // nx   Euler lengths of horizontal faces per column
+
+  // ---- persistent state
+  double *rho, *p, *c, *e, *q, *divu, *cell_mass;
+  double *rhom, *pm, *cm, *em, *qm, *fm, *mfm, *cmassm;  // nbmat planes
+  int *mixte, *pure;
+  double* u;          // 2 node planes
+  double* node_mass;
+  double* speed;      // |u| per node (dt reduction)
+  const double* rho0_left;  // ny: initial density of column 0 (periodic)
+
+  // ---- Lagrange -> remap
+  double* XL;         // 2 node planes
+  double *vL, *rL, *XcL /*2 planes*/, *Hx, *Hy;
+  double* UL;         // ncomp planes (also receives the second sweep)
+  double* Phi;        // ncomp planes
+  double* U1;         // ncomp planes
+  double* gP;         // ncomp planes (limited gradients)
+  double *dPAv, *dPAr;  // ncomp planes (plateau-slope swept integrals)
+  double* DPF;        // nbmat planes (plateau-slope dual mass flux)
+  double* phiF;       // ncomp face planes
+  double* FFd;        // 2*nbmat planes: dual-method flux comps, minus / plus
+  double* DPv;        // 2 node planes: nodal velocity after sweep 1
+  double* gD;         // 2 node planes: limited nodal velocity gradient
+  double* UD1;        // 3 node planes: m*u, m*v, m after sweep 1
+
+  // ---- control block (device)
+  struct Ctrl* ctrl;
+};
+
+// Per-run device control block.
+struct Ctrl {
+  double t_n, dt_n, t_np1, dt_np1;
+  long long n;          // cycles done
+  int done;             // reference loop condition failed
+  int active;           // this cycle runs
+  int x_then_y;         // direction of the first sweep of this cycle
+  int pad;
+  unsigned long long dt_min_bits;  // ordered encoding of the dt partial min
+  unsigned long long pmax_bits;    // ordered encoding of max pressure
+  double pmax_prev;                // max pressure of the state at cycle start
+  unsigned err;
+  int pad2;
+  long long err_cell;
+};
+
+}  // namespace hydro
+
+#endif
