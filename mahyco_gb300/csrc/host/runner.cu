@@ -24,6 +24,7 @@ int fail(int rc, const std::string& msg) {
 
 void launch_prologue(const RunView& v, cudaStream_t s);
 int launch_cycle(const RunView& v, cudaStream_t s);
+void launch_node_mass(const RunView& v, cudaStream_t s);
 
 #define CUDA_TRY(expr)                                                     \
   do {                                                                     \
@@ -499,7 +500,10 @@ int hydro_run_fetch(hydro_run* r, const char* f, double* dst, size_t n) {
   else if (!strcmp(f, "pseudo")) one = v.q;
   else if (!strcmp(f, "divu")) one = v.divu;
   else if (!strcmp(f, "cell_mass")) one = v.cell_mass;
-  else if (!strcmp(f, "node_mass")) one = v.node_mass;
+  else if (!strcmp(f, "node_mass")) {
+    launch_node_mass(v, s);
+    one = v.node_mass;
+  }
   if (one) {
     CUDA_TRY(cudaMemcpyAsync(dst, one, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));

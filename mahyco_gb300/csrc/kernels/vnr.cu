@@ -1139,6 +1139,21 @@ __global__ void __launch_bounds__(kBX* kBY) k_init_reductions(RunView v) {
   block_reduce_minmax(dtb, pb, &C);
 }
 
+// Vnr::computeNodeMass (PhaseLagrange.cc:31-48) from the current cell
+// masses; the cycle recomputes it at its start, this refreshes it for a fetch.
+__global__ void k_node_mass(RunView v) {
+  const int j = blockIdx.x * kBX + threadIdx.x;
+  const int i = blockIdx.y * kBY + threadIdx.y;
+  if (i > v.ny || j > v.nx) return;
+  double r = 0.0;
+  int k = 0;
+  if (i < v.ny && j < v.nx) { r = r + v.cell_mass[(long long)i * v.nx + j]; ++k; }
+  if (i < v.ny && j > 0) { r = r + v.cell_mass[(long long)i * v.nx + j - 1]; ++k; }
+  if (i > 0 && j < v.nx) { r = r + v.cell_mass[(long long)(i - 1) * v.nx + j]; ++k; }
+  if (i > 0 && j > 0) { r = r + v.cell_mass[(long long)(i - 1) * v.nx + j - 1]; ++k; }
+  v.node_mass[(long long)i * (v.nx + 1) + j] = r / (double)k;
+}
+
 __global__ void k_node_speed(RunView v) {
   const int j = blockIdx.x * kBX + threadIdx.x;
   const int i = blockIdx.y * kBY + threadIdx.y;
@@ -1162,6 +1177,10 @@ static dim3 node_grid(const RunView& v) {
 void launch_prologue(const RunView& v, cudaStream_t s) {
   k_node_speed<<<node_grid(v), dim3(kBX, kBY), 0, s>>>(v);
   k_init_reductions<<<cell_grid(v), dim3(kBX, kBY), 0, s>>>(v);
+}
+
+void launch_node_mass(const RunView& v, cudaStream_t s) {
+  k_node_mass<<<node_grid(v), dim3(kBX, kBY), 0, s>>>(v);
 }
 
 // Enqueues one full cycle on stream s.  Returns the number of kernels.

@@ -1,0 +1,71 @@
+"""Shared fixtures.  GPU tests are marked `gpu`; everything else runs on CPU."""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+GOLDEN = ROOT / "tests" / "golden"
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+    config.addinivalue_line("markers", "slow: long-running CPU check")
+
+
+def load_golden(path: Path):
+    import mahyco_gb300 as M
+    z = np.load(path)
+    spec = M.HydroSpec()
+    for k, v in json.loads(str(z["spec"])).items():
+        if isinstance(v, list):
+            arr = getattr(spec, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(spec, k, v)
+    meta = json.loads(str(z["meta"]))
+    fields = {k: z[k] for k in z.files if k not in ("spec", "meta")}
+    return spec, meta, fields
+
+
+def golden_cases():
+    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+
+
+# fields compared per case; *_env fields keep only the nbmat live columns
+CELL_FIELDS = ["density", "pressure", "energy", "sound_speed", "pseudo", "divu",
+               "cell_mass", "density_env", "energy_env", "pressure_env",
+               "fracvol_env", "mass_fraction_env"]
+NODE_FIELDS = ["node_velocity"]
+
+
+def get_field(run, name, nbmat):
+    a = run.fetch(name)
+    if name.endswith("_env"):
+        a = a.reshape(-1, 3)[:, :nbmat]
+    return a
+
+
+def assert_bitwise(name, got, want):
+    got = np.asarray(got)
+    want = np.asarray(want)
+    assert got.shape == want.shape, (name, got.shape, want.shape)
+    if not np.array_equal(got, want, equal_nan=True):
+        d = np.abs(got - want)
+        i = int(np.nanargmax(d))
+        raise AssertionError(
+            f"{name}: {int(np.sum(got != want))} values differ, max |diff| "
+            f"{np.nanmax(d):.3e} at {i}: got {got.flat[i]!r} want {want.flat[i]!r}")
+
+
+@pytest.fixture(scope="session")
+def port_lib():
+    from oracle import port
+    port.build()
+    return port
