@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 hydro path: FP64 cell-updates/s.
+
+Default workload (the single large instance): bi-material Sod along Y on a
+2048x2048 mesh over [0,1]^2, a 50/50 mixed cell row at the interface, VNR
+Lagrange scheme, order-2 remap, Superbee limiter with PenteBorne (pure),
+A1 dual mass flux, 200 cycles, FP64.  One "step" is one full cycle
+(Lagrange + two directional remap sweeps + dual remap + remap final) over
+all 4,194,304 cells.  The state (~1.9 GB) is far larger than L2, so every
+cycle streams it from HBM.
+
+  value      device time (CUDA events on the run's stream) of K cycles,
+             state resident in HBM
+  e2e        the same work through the C ABI with host buffers: run
+             creation (host initial state, host->device upload), K cycles,
+             fetch of the final fields (device->host)
+  roofline   the dominant kernel's algorithmic bytes / measured launch time
+             against the measured HBM copy bandwidth, plus its FP64 rate
+             against the measured FP64 FMA throughput (the kernels are FP64
+             instruction bound on GB300)
+  cpu_baseline  the C restatement of the reference (oracle/port, OpenMP on
+             all host cores) on a bounded sample of the same workload
+
+  --impl reference   times the reference's CPU algorithm (the C restatement;
+                     the reference's own build cannot exist on this host) on
+                     the same workload, on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "FP64 cell-updates/s on 1 GB300 batched/served vs plain GPU vs CPU; p50/p99"
+UNIT = "cell-updates/s"
+
+
+def workload_spec(M, n: int = 2048, cycles: int = 200):
+    s = M.default_spec()
+    s.scheme, s.test_case, s.nbmat = M.SCHEME_VNR, 16, 2  # BiSodCaseY
+    s.nx = s.ny = n
+    s.dx = s.dy = 1.0 / n
+    s.final_time, s.output_time, s.dt_init, s.dt_min = 0.2, 1e-2, 1e-4, 1e-12
+    s.space_order, s.projection, s.projection_order = 2, 1, 2
+    s.limiter = M.LIMITERS["superBee"]
+    s.pb, s.pb_mixte = 1, 0
+    s.limiter_pure, s.pb_complet = M.LIMITERS["arithmeticG"], 0
+    s.pseudo_centree, s.dual_mass_flux = 0, 0
+    s.init_variant = 1
+    s.max_cycles = cycles
+    return s
+
+
+WORKLOAD = {
+    "workload": "bi-material Sod Y, 2048x2048 cells, 50/50 mixed interface row, "
+                "VNR + order-2 remap, superBee + PenteBorne pure, A1 dual flux, "
+                "200 cycles",
+    "mesh": [2048, 2048], "nbmat": 2, "cycles": 200, "scheme": "VNR",
+    "projection_order": 2, "limiter": "superBee", "pente_borne": "pure",
+    "dual_mass_flux": "A1", "state_bytes": None,
+    "l2": "state (~1.9 GB) >> L2 (129 MB): every cycle streams it from HBM",
+}
+
+
+# Algorithmic (compulsory) bytes per unit of each kernel: every input plane
+# read once, every output plane written once; units are cells or nodes.
+def algorithmic_bytes(kind: str, nb: int, pb: bool) -> int:
+    nc = 3 * nb + 1
+    d = 8
+    table = {
+        "k_lag_nodes": 18,                       # u, cell mass, p, q, cqs / u, XL, m
+        "k_lag_cells": (7 + 7 * nb) + (8 + nb + 2 * nc),
+        "k_sweep_grad": (nc + 3 + (4 if pb else 0)) + (2 * nc if pb else nc),
+        "k_sweep_face": (2 * nc if pb else 2 * nc + 2) + nc,
+        "k_sweep_update": (2 * nc + 5) + (nc + 2 * nb) + (nc + 1) // 2,
+        "k_dual_grad": 5,
+        "k_dual_update": (2 * nb + 2 + 8) + 5,
+        "k_final": (nc + 2) + (6 + 7 * nb + 1),
+    }
+    return table.get(kind, 0) * d
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+class Clocks:
+    """Samples nvidia-smi clocks / throttle reasons while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self) -> dict:
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, r in rows for k in range(4)
+                          if r[k].lower() in ("active", "1")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def barrier_max(value: float, world: int) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(spec_fn, budget_s: float = 25.0) -> dict:
+    """The C restatement on all host cores, a bounded sample of the workload:
+    the full 2048^2 mesh, whole cycles until ~budget_s of CPU time."""
+    from oracle import port
+    cores = port.num_threads()
+    spec = spec_fn()
+    run = port.PortRun(spec)
+    run.step(1)  # warm: first touch of every array
+    n, t0 = 0, time.perf_counter()
+    while True:
+        run.step(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or n >= 50:
+            break
+    cells = spec.nx * spec.ny
+    run.close()
+    return {"value": cells * n / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} cycles of the 2048x2048 workload (cycles 2..{n + 1}) "
+                      f"on {cores} OpenMP threads, {el:.1f} s"}
+
+
+def run_reference(args) -> None:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    import mahyco_gb300 as M
+    from oracle import port
+    spec = workload_spec(M, 2048, 200)
+    cores = port.num_threads()
+    run = port.PortRun(spec)
+    for _ in range(min(args.warmup, 1)):
+        run.step(1)
+    budget = 150.0
+    n, t0 = 0, time.perf_counter()
+    while n < args.steps:
+        run.step(1)
+        n += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    val = spec.nx * spec.ny * n / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": n, "warmup": min(args.warmup, 1),
+        "ms_per_step": 1e3 * el / n, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(WORKLOAD, form="cpu"),
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{n} cycles of the 2048x2048 workload on "
+                                   f"{cores} OpenMP threads (time-capped at "
+                                   f"{budget:.0f} s)"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args) -> None:
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    import mahyco_gb300 as M
+    ctx = M.Context(local)
+    W, K = args.warmup, args.steps
+    n = args.mesh
+    spec = workload_spec(M, n, K + 16)
+    cells = n * n
+    # warm-up: graph instantiation, first launches, clocks up
+    w = M.Run(workload_spec(M, n, W + 1), ctx)
+    w.timed(W)
+    w.close()
+    run = M.Run(spec, ctx)
+    state_bytes = run.device_bytes
+    launches0 = run.kernel_launches
+    barrier_max(0.0, world)
+    with Clocks(local) as clk:
+        ms = run.timed(K)
+    clocks = clk.summary()
+    launches = run.kernel_launches - launches0
+    ms = barrier_max(ms, world)
+    value = cells * K * world / (ms * 1e-3)
+    # per-kernel profile over 8 further cycles of the same run
+    prof = run.profile(8)
+    run.close()
+    # dominant kernel and its roofline
+    kinds = {k: v for k, v in prof.items() if v[1] > 0}
+    dom = max(kinds, key=lambda k: kinds[k][0])
+    dom_ms, dom_n = kinds[dom]
+    per_launch_ms = dom_ms / dom_n
+    node_kernel = dom in ("k_lag_nodes", "k_dual_grad", "k_dual_update")
+    units = (n + 1) * (n + 1) if node_kernel else cells
+    alg = algorithmic_bytes(dom, spec.nbmat, bool(spec.pb)) * units
+    achieved = alg / (per_launch_ms * 1e-3) / 1e9
+    peaks = load_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    prof_file = ROOT / "profiles" / "kernel_counters_bisod_vnr.json"
+    traffic = None
+    fp64 = None
+    fp64_peak = M.fp64_peak_tflops(local)
+    if prof_file.exists():
+        pj = json.loads(prof_file.read_text())
+        kp = pj.get("kernels", {}).get(dom, {})
+        if "dram_bytes_per_unit" in kp:
+            traffic = kp["dram_bytes_per_unit"] * units
+        if "fp64_flops_per_unit" in kp:
+            fl = kp["fp64_flops_per_unit"] * units
+            ach = fl / (per_launch_ms * 1e-3) / 1e12
+            fp64 = {"achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                    "frac": ach / fp64_peak, "flops_per_launch": fl,
+                    "peak_source": "measured DFMA chain (hydro_fp64_peak)"}
+    if fp64 is None:
+        fp64 = {"achieved": None, "peak": fp64_peak, "unit": "TFLOP/s",
+                "peak_source": "measured DFMA chain (hydro_fp64_peak)"}
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg,
+                "launch_ms": per_launch_ms,
+                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"
+                if not peaks.get("fallback") else "of fallback",
+                "fp64": fp64}
+    # end to end through the C ABI with host buffers
+    t0 = time.perf_counter()
+    e = M.Run(workload_spec(M, n, K), ctx)
+    e.step(K)
+    outs = [e.fetch(f) for f in ("density", "pressure", "energy", "fracvol_env",
+                                 "node_velocity")]
+    e2e_s = time.perf_counter() - t0
+    h2d = e.device_bytes  # upper bound: the whole arena is written from host
+    d2h = sum(o.nbytes for o in outs)
+    e.close()
+    e2e = {"value": cells * K / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
+           "includes": "host initial state + upload, K cycles, fetch of 5 fields"}
+    if rank != 0:
+        return
+    cpu = None if args.no_cpu else cpu_baseline(lambda: workload_spec(M, n, 200))
+    cfg = dict(WORKLOAD, form="plain", state_bytes=state_bytes)
+    if n != 2048:
+        cfg["mesh"] = [n, n]
+        cfg["workload"] = cfg["workload"].replace("2048x2048", f"{n}x{n}")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (analytic initial state)", "config": cfg,
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+        "gpu_launches": launches,
+        "kernel_ms": {k: [round(v[0], 4), v[1]] for k, v in kinds.items()},
+    }
+    print(json.dumps(line))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mesh", type=int, default=2048)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

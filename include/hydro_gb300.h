@@ -123,6 +123,22 @@ int hydro_run_time(hydro_run* run, double* t, double* dt, long* cycle);
 int hydro_run_error(hydro_run* run, unsigned* code, long* cell);
 int hydro_run_destroy(hydro_run* run);
 
+/* Asynchronous form of hydro_run_step: enqueue cycles on the context's
+ * stream; hydro_run_sync waits and reports whether the run has ended. */
+int hydro_run_enqueue(hydro_run* run, int ncycles);
+int hydro_run_sync(hydro_run* run, int* done);
+long long hydro_run_kernel_launches(hydro_run* run);
+size_t hydro_run_device_bytes(hydro_run* run);
+void* hydro_ctx_stream(hydro_ctx* ctx);
+
+/* Measurement helpers (no counterpart in the reference). */
+int hydro_run_timed(hydro_run* run, int ncycles, float* ms);
+int hydro_run_profile(hydro_run* run, int ncycles, double* ms,
+                      long long* launches, int nkinds);
+const char* hydro_kernel_name(int kind);
+int hydro_kernel_kinds(void);
+int hydro_fp64_peak(int device, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

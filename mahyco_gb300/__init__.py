@@ -99,6 +99,13 @@ def lib() -> C.CDLL:
         L.hydro_run_kernel_launches.restype = C.c_longlong
         L.hydro_run_device_bytes.argtypes = [vp]
         L.hydro_run_device_bytes.restype = sz
+        L.hydro_run_timed.argtypes = [vp, i, C.POINTER(C.c_float)]
+        L.hydro_run_profile.argtypes = [vp, i, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_longlong), i]
+        L.hydro_kernel_name.argtypes = [i]
+        L.hydro_kernel_name.restype = C.c_char_p
+        L.hydro_kernel_kinds.restype = i
+        L.hydro_fp64_peak.argtypes = [i, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -107,6 +114,13 @@ def _check(rc: int, what: str) -> None:
     if rc != 0:
         msg = lib().hydro_last_error().decode(errors="replace")
         raise RuntimeError(f"{what} failed ({rc}): {msg}")
+
+
+def fp64_peak_tflops(device: int = 0) -> float:
+    """Measured FP64 FMA throughput of the device (TFLOP/s)."""
+    t = C.c_double()
+    _check(lib().hydro_fp64_peak(device, C.byref(t)), "hydro_fp64_peak")
+    return t.value
 
 
 def default_spec() -> HydroSpec:
@@ -218,6 +232,20 @@ class Run:
         _check(lib().hydro_run_error(self.h, C.byref(code), C.byref(cell)),
                "hydro_run_error")
         return code.value, cell.value
+
+    def timed(self, ncycles: int) -> float:
+        """Device time (ms, CUDA events on the run's stream) of ncycles."""
+        ms = C.c_float()
+        _check(lib().hydro_run_timed(self.h, ncycles, C.byref(ms)), "hydro_run_timed")
+        return ms.value
+
+    def profile(self, ncycles: int) -> dict:
+        """Per-kernel device time over ncycles launched one by one."""
+        nk = lib().hydro_kernel_kinds()
+        ms = (C.c_double * nk)()
+        cnt = (C.c_longlong * nk)()
+        _check(lib().hydro_run_profile(self.h, ncycles, ms, cnt, nk), "hydro_run_profile")
+        return {lib().hydro_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(nk)}
 
     @property
     def kernel_launches(self) -> int:

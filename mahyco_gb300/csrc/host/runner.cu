@@ -23,8 +23,9 @@ int fail(int rc, const std::string& msg) {
 }
 
 void launch_prologue(const RunView& v, cudaStream_t s);
-int launch_cycle(const RunView& v, cudaStream_t s);
+int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook);
 void launch_node_mass(const RunView& v, cudaStream_t s);
+int measure_fp64_peak(int device, double* tflops);
 
 #define CUDA_TRY(expr)                                                     \
   do {                                                                     \
@@ -376,7 +377,7 @@ int build_graph(hydro_run* r, int cycles) {
   cudaGraph_t g;
   CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   int nk = 0;
-  for (int k = 0; k < cycles; ++k) nk = launch_cycle(r->v, s);
+  for (int k = 0; k < cycles; ++k) nk = launch_cycle(r->v, s, nullptr);
   cudaError_t e = cudaStreamEndCapture(s, &g);
   if (e != cudaSuccess) return fail(-40, std::string("graph capture: ") + cudaGetErrorString(e));
   e = cudaGraphInstantiate(&r->graph, g, 0);
@@ -416,7 +417,7 @@ int hydro_run_enqueue(hydro_run* r, int ncycles) {
     r->kernels_launched += (long long)r->graph_cycles * r->kernels_per_cycle;
   }
   for (int k = 0; k < left; ++k) {
-    r->kernels_launched += launch_cycle(r->v, s);
+    r->kernels_launched += launch_cycle(r->v, s, nullptr);
   }
   CUDA_TRY(cudaGetLastError());
   return 0;
@@ -533,6 +534,80 @@ int hydro_run_fetch(hydro_run* r, const char* f, double* dst, size_t n) {
     return 0;
   }
   return fail(-2, std::string("unknown field ") + f);
+}
+
+// Times ncycles cycles (graph replays) between two CUDA events recorded on
+// the run's stream; *ms is the device time.  Benchmark helper, no
+// counterpart in the reference.
+int hydro_run_timed(hydro_run* r, int ncycles, float* ms) {
+  if (!r || !ms) return fail(-1, "hydro_run_timed: null argument");
+  CUDA_TRY(cudaSetDevice(r->ctx->device));
+  cudaStream_t s = r->ctx->stream;
+  if (!r->graph)
+    if (int rc = build_graph(r, 8)) return rc;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  CUDA_TRY(cudaEventRecord(e0, s));
+  if (int rc = hydro_run_enqueue(r, ncycles)) return rc;
+  CUDA_TRY(cudaEventRecord(e1, s));
+  CUDA_TRY(cudaEventSynchronize(e1));
+  CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return sync_ctrl(r);
+}
+
+// Runs ncycles cycles kernel by kernel with CUDA events between launches and
+// accumulates per kernel kind: ms[kind] (device time) and launches[kind].
+// Benchmark helper, no counterpart in the reference.
+int hydro_run_profile(hydro_run* r, int ncycles, double* ms, long long* launches,
+                      int nkinds) {
+  if (!r || !ms || !launches || nkinds < kNumKernelKinds)
+    return fail(-1, "hydro_run_profile: bad arguments");
+  CUDA_TRY(cudaSetDevice(r->ctx->device));
+  cudaStream_t s = r->ctx->stream;
+  for (int k = 0; k < nkinds; ++k) {
+    ms[k] = 0.0;
+    launches[k] = 0;
+  }
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kinds;
+  for (int c = 0; c < ncycles; ++c) {
+    ev.clear();
+    kinds.clear();
+    LaunchHook hook = [&](int kind) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      cudaEventRecord(e, s);
+      ev.push_back(e);
+      kinds.push_back(kind);
+    };
+    launch_cycle(r->v, s, &hook);
+    CUDA_TRY(cudaStreamSynchronize(s));
+    for (size_t i = 0; i + 1 < ev.size(); ++i) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+      ms[kinds[i]] += t;
+      launches[kinds[i]] += 1;
+    }
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+  r->kernels_launched += 0;
+  CUDA_TRY(cudaGetLastError());
+  return sync_ctrl(r);
+}
+
+const char* hydro_kernel_name(int kind) {
+  return (kind >= 0 && kind < kNumKernelKinds) ? kKernelNames[kind] : "";
+}
+
+int hydro_kernel_kinds(void) { return kNumKernelKinds; }
+
+int hydro_fp64_peak(int device, double* tflops) {
+  if (!tflops) return fail(-1, "hydro_fp64_peak: null argument");
+  return measure_fp64_peak(device, tflops);
 }
 
 // Stream of the context (for host code that records CUDA events around

@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <string>
 
 #include "hydro_gb300.h"
@@ -110,6 +111,11 @@ struct Ctrl {
   int pad2;
   long long err_cell;
 };
+
+// Per-kernel timing hook for launch_cycle.
+using LaunchHook = std::function<void(int)>;
+constexpr int kNumKernelKinds = 11;
+extern const char* const kKernelNames[kNumKernelKinds];
 
 }  // namespace hydro
 

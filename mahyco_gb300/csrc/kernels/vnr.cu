@@ -1183,25 +1183,37 @@ void launch_node_mass(const RunView& v, cudaStream_t s) {
   k_node_mass<<<node_grid(v), dim3(kBX, kBY), 0, s>>>(v);
 }
 
-// Enqueues one full cycle on stream s.  Returns the number of kernels.
-int launch_cycle(const RunView& v, cudaStream_t s) {
+// Kernel kinds of one cycle (for per-kernel timing).
+const char* const kKernelNames[kNumKernelKinds] = {
+    "k_begin",      "k_reset_reductions", "k_lag_nodes", "k_lag_cells",
+    "k_sweep_grad", "k_sweep_face",       "k_sweep_update", "k_dual_grad",
+    "k_dual_update", "k_final",           "k_end"};
+
+// Enqueues one full cycle on stream s; hook(kind) is called before each
+// launch (and with kind = -1 after the last) when given.  Returns the number
+// of kernels.
+int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook) {
   const dim3 blk(kBX, kBY);
   const dim3 cg = cell_grid(v), ng = node_grid(v);
-  dim3 fg = dim3((v.nx + 1 + kBX - 1) / kBX, (v.ny + 1 + kBY - 1) / kBY);
+  const dim3 fg = ng;
   int nk = 0;
-  k_begin<<<1, 1, 0, s>>>(v); ++nk;
-  k_reset_reductions<<<1, 1, 0, s>>>(v); ++nk;
-  k_lag_nodes<<<ng, blk, 0, s>>>(v); ++nk;
-  k_lag_cells<<<cg, blk, 0, s>>>(v); ++nk;
+  auto H = [&](int kind) {
+    if (hook) (*hook)(kind);
+  };
+  H(0); k_begin<<<1, 1, 0, s>>>(v); ++nk;
+  H(1); k_reset_reductions<<<1, 1, 0, s>>>(v); ++nk;
+  H(2); k_lag_nodes<<<ng, blk, 0, s>>>(v); ++nk;
+  H(3); k_lag_cells<<<cg, blk, 0, s>>>(v); ++nk;
   for (int sweep = 1; sweep <= 2; ++sweep) {
-    if (v.order > 1) { k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk; }
-    k_sweep_face<<<fg, blk, 0, s>>>(v, sweep); ++nk;
-    k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
-    k_dual_grad<<<ng, blk, 0, s>>>(v, sweep); ++nk;
-    k_dual_update<<<ng, blk, 0, s>>>(v, sweep); ++nk;
+    if (v.order > 1) { H(4); k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk; }
+    H(5); k_sweep_face<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+    H(6); k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
+    H(7); k_dual_grad<<<ng, blk, 0, s>>>(v, sweep); ++nk;
+    H(8); k_dual_update<<<ng, blk, 0, s>>>(v, sweep); ++nk;
   }
-  k_final<<<cg, blk, 0, s>>>(v); ++nk;
-  k_end<<<1, 1, 0, s>>>(v); ++nk;
+  H(9); k_final<<<cg, blk, 0, s>>>(v); ++nk;
+  H(10); k_end<<<1, 1, 0, s>>>(v); ++nk;
+  H(-1);
   return nk;
 }
 
