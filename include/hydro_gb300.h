@@ -139,6 +139,21 @@ const char* hydro_kernel_name(int kind);
 int hydro_kernel_kinds(void);
 int hydro_fp64_peak(int device, double* tflops);
 
+/* CFL time step of a VNR state held in caller device memory, allocating
+ * nothing (no counterpart in the reference; it restates the reduction of
+ * Vnr::computeDeltaT with the remap on).  For callers that may not call
+ * cudaMalloc/cudaFree because their own pool owns the device memory.  Inputs:
+ * node velocity planes d_u, d_v ((nx+1)*(ny+1) each), cell sound speed d_c
+ * (nx*ny), the current dt_n; output: one double at d_dt_out.  Its scratch is
+ * a fixed 32 KiB device array inside the library, so at most 1,048,576 cells
+ * are accepted (larger meshes return an error).  The first call on a device
+ * looks up that array's address and should come before any stream capture.
+ * Calls that overlap on the GPU share the scratch and race. */
+int hydro_vnr_dt_noalloc(int nx, int ny, double dx, double dy,
+                         const double* d_u, const double* d_v,
+                         const double* d_c, double dt_n, double* d_dt_out,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif
