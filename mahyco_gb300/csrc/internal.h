@@ -114,7 +114,7 @@ struct Ctrl {
 
 // Per-kernel timing hook for launch_cycle.
 using LaunchHook = std::function<void(int)>;
-constexpr int kNumKernelKinds = 11;
+constexpr int kNumKernelKinds = 12;
 extern const char* const kKernelNames[kNumKernelKinds];
 
 }  // namespace hydro

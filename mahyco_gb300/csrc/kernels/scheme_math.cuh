@@ -28,6 +28,35 @@ HD double from_ord(unsigned long long o) {
   return __longlong_as_double((long long)b);
 }
 
+// IEEE division behind a call: the optimizer cannot if-convert a branch
+// around it into an unconditional division, so divisions on paths that are
+// rarely taken cost nothing when they are not taken.
+static __device__ __noinline__ double ddiv_call(double n, double d) { return n / d; }
+
+// n / d with the exact shortcuts decided on the integer pipe:
+//   n = +-0, d finite non-zero   -> zero with sign(n) xor sign(d)
+//   d = 1                        -> n
+//   n = d, finite non-zero       -> 1
+// (uniform and single-material cells produce many of these); otherwise the
+// IEEE division.  Bit-identical to n / d (NaN results stay NaN).
+HD double qdiv(double n, double d) {
+  const unsigned long long nb = (unsigned long long)__double_as_longlong(n);
+  const unsigned long long db = (unsigned long long)__double_as_longlong(d);
+  const bool dfin = ((db >> 52) & 0x7ffull) != 0x7ffull;
+  const bool dnz = (db << 1) != 0ull;
+  if ((nb << 1) == 0ull && dnz && dfin)
+    return __longlong_as_double((long long)((nb ^ db) & 0x8000000000000000ull));
+  if (db == 0x3ff0000000000000ull) return n;
+  if (nb == db && dnz && dfin) return 1.0;
+  return ddiv_call(n, d);
+}
+
+// x / k for k = 1, 2 or 4, as the exact multiplication by 1/k (division by
+// a power of two and multiplication by its reciprocal round identically).
+HD double div_pow2(double x, int k) {
+  return x * (k == 4 ? 0.25 : (k == 2 ? 0.5 : 1.0));
+}
+
 // Remap::fluxLimiter (remap/UtilesRemap.cc:9-23)
 HD double flux_limiter(int id, double r) {
   if (id == HYDRO_LIM_MINMOD) return smax(0.0, smin(1.0, r));
@@ -43,7 +72,7 @@ HD double flux_limiter(int id, double r) {
 // divideNoExcept (includes/Freefunctions.h:86-92)
 HD double divide_no_except(double a, double b) {
   if (fabs(b) < 1.0E-12) return 0.0;
-  return a / b;
+  return qdiv(a, b);
 }
 
 // Remap::fluxLimiterPP (remap/UtilesRemap.cc:25-72)
@@ -80,13 +109,60 @@ HD double flux_limiter_pp(int id, double gp, double gm, double yp, double ym,
 }
 
 // one component of Remap::computeAndLimitGradPhi (UtilesRemap-Impl.h:99-126)
+//
+// Classic limiters: res = (phi(r1)*gm + phi(r2)*gp) / 2 with
+// r1 = divideNoExcept(gp, gm), r2 = divideNoExcept(gm, gp).  For minmod and
+// superBee, phi(r) only depends on the exact value of r in some ranges, and
+// r1, r2 are reciprocal, so for finite gradients of the same sign one
+// division decides both: the other phi is a constant fixed by comparing
+// |gp| and |gm| (phi is continuous at its breakpoints, so ratios that round
+// onto a breakpoint give the same constant).  Opposite signs give phi = 0
+// for both.  Anything else (NaN, infinities, other limiters) takes the
+// reference's two divisions.  The result is bit-identical in every case.
 HD double limit_grad1(int id, double gp, double gm, double yp, double ym,
                       double h0, double hp, double hm) {
-  if (id < HYDRO_LIM_MINMODG)
-    return (flux_limiter(id, divide_no_except(gp, gm)) * gm +
-            flux_limiter(id, divide_no_except(gm, gp)) * gp) /
-           2.0;
-  return flux_limiter_pp(id, gp, gm, yp, ym, h0, hp, hm);
+  if (id >= HYDRO_LIM_MINMODG) return flux_limiter_pp(id, gp, gm, yp, ym, h0, hp, hm);
+  const double a = fabs(gp), b = fabs(gm);
+  if ((id == HYDRO_LIM_MINMOD || id == HYDRO_LIM_SUPERBEE) && isfinite(gp) &&
+      isfinite(gm)) {
+    double f1, f2;  // phi(r1), phi(r2)
+    if (b < 1.0E-12) {
+      f1 = 0.0;
+      f2 = flux_limiter(id, divide_no_except(gm, gp));
+    } else if (a < 1.0E-12) {
+      f2 = 0.0;
+      f1 = flux_limiter(id, qdiv(gp, gm));
+    } else if ((gp < 0.0) != (gm < 0.0)) {
+      f1 = 0.0;  // r1, r2 < 0 (or -0 after underflow)
+      f2 = 0.0;
+    } else if (id == HYDRO_LIM_MINMOD) {
+      if (a <= b) {
+        f1 = flux_limiter(id, qdiv(gp, gm));
+        f2 = 1.0;  // r2 >= 1
+      } else {
+        f1 = 1.0;  // r1 >= 1
+        f2 = flux_limiter(id, qdiv(gm, gp));
+      }
+    } else {  // superBee: 2r on [0,1/2], 1 on [1/2,1], r on [1,2], 2 above
+      if (a <= 0.5 * b) {
+        f1 = flux_limiter(id, qdiv(gp, gm));
+        f2 = 2.0;  // r2 >= 2
+      } else if (a <= b) {
+        f1 = 1.0;  // r1 in [1/2, 1]
+        f2 = flux_limiter(id, qdiv(gm, gp));
+      } else if (a <= 2.0 * b) {
+        f1 = flux_limiter(id, qdiv(gp, gm));
+        f2 = 1.0;  // r2 in [1/2, 1]
+      } else {
+        f1 = 2.0;  // r1 >= 2
+        f2 = flux_limiter(id, qdiv(gm, gp));
+      }
+    }
+    return (f1 * gm + f2 * gp) / 2.0;
+  }
+  return (flux_limiter(id, divide_no_except(gp, gm)) * gm +
+          flux_limiter(id, divide_no_except(gm, gp)) * gp) /
+         2.0;
 }
 
 // Remap::computeY0 (remap/UtilesRemap.cc:74-125): both thresholds at once.
@@ -123,12 +199,25 @@ HD void compute_y0(int id, double yp, double ym, double h0, double hp,
   }
 }
 
-// Remap::INT2Y (remap/UtilesRemap.cc:177-188)
+// Remap::INT2Y (remap/UtilesRemap.cc:177-188).  eta = min(max(0, n/d), 1)
+// is decided by comparison when the quotient is certainly <= 0 (eta = +0)
+// or >= 1 (eta = 1) for finite operands; the division is only performed for
+// points strictly inside the interval (or non-finite operands).  Same
+// result bit for bit.
 HD double int2y(double X, double x0, double y0, double x1, double y1) {
   double flux = 0.;
-  if (fabs(x1 - x0) > 1.e-14) {
-    double eta = smin(smax(0., (X - x0) / (x1 - x0)), 1.);
-    flux = (y0 + 0.5 * eta * (y1 - y0)) * (x1 - x0) * eta;
+  const double d = x1 - x0;
+  if (fabs(d) > 1.e-14) {
+    const double n = X - x0;
+    double eta;
+    const bool fin = isfinite(n) && isfinite(d);
+    if (fin && (d > 0. ? n <= 0. : n >= 0.))
+      eta = 0.;
+    else if (fin && (d > 0. ? n >= d : n <= d))
+      eta = 1.;
+    else
+      eta = smin(smax(0., ddiv_call(n, d)), 1.);
+    flux = (y0 + 0.5 * eta * (y1 - y0)) * d * eta;
   }
   return flux;
 }
@@ -143,8 +232,8 @@ HD PPShape pp_shape(int lim, double thr, double y0, double yp, double ym,
   double y0p, y0m;
   compute_y0(lim, yp, ym, h0, hp, hm, y0p, y0m);
   double xp = 1., xm = 1.;
-  if (fabs(y0p - yp) > thr) xp = (y0 - yp) / (y0p - yp) - 1. / 2.;
-  if (fabs(y0m - ym) > thr) xm = (y0 - ym) / (y0m - ym) - 1. / 2.;
+  if (fabs(y0p - yp) > thr) xp = qdiv(y0 - yp, y0p - yp) - 1. / 2.;
+  if (fabs(y0m - ym) > thr) xm = qdiv(y0 - ym, y0m - ym) - 1. / 2.;
   PPShape s;
   s.xd = +h0 * smin(smax(xp, -1. / 2.), 1. / 2.);
   s.xg = -h0 * smin(smax(xm, -1. / 2.), 1. / 2.);

@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) {
   if (i > 0 && j > 0) { cells[k] = (long long)(i - 1) * v.nx + j - 1; loc[k++] = 2; }
   double msum = 0.0;
   for (int t = 0; t < k; ++t) msum = msum + v.cell_mass[cells[t]];
-  const double m = msum / (double)k;
+  const double m = div_pow2(msum, k);  // msum / k, k in {1, 2, 4}
   v.node_mass[p] = m;
 
   double ux = v.u[p], uy = v.u[v.npitch + p];
@@ -390,13 +390,13 @@ __global__ void __launch_bounds__(kBX* kBY) k_lag_cells(RunView v) {
     double sv = 0.;
     for (int m = 0; m < nb; ++m) sv += U[m];
     for (int m = 0; m < nb; ++m) {
-      v.Phi[m * P + c] = U[m] / sv;
-      v.Phi[(nb + m) * P + c] = (U[m] != 0.) ? U[nb + m] / U[m] : 0.;
-      v.Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? U[2 * nb + m] / U[nb + m] : 0.;
+      v.Phi[m * P + c] = qdiv(U[m], sv);
+      v.Phi[(nb + m) * P + c] = (U[m] != 0.) ? qdiv(U[nb + m], U[m]) : 0.;
+      v.Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
     }
     v.Phi[3 * nb * P + c] = q_new;
   } else {
-    for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = U[k] / vol;
+    for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv(U[k], vol);
   }
   v.vL[c] = vol;
   v.rL[c] = rho_new;
@@ -443,6 +443,37 @@ HD double fnv_horizontal(const RunView& v, long long na, long long nb) {
 }
 
 // ----------------------------------------------------------- remap sweep
+// Face gradients of one sweep (Remap::computeGradPhiFace{1,2},
+// remap/PhaseRemap1.cc:22-55, PhaseRemap2.cc:21-55): one thread per inner
+// face perpendicular to the sweep, (Phi(front) - Phi(back)) / deltaxLagrange,
+// stored in the face-value planes (k_sweep_face overwrites them later).
+__global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) {
+  const Ctrl& C = *v.ctrl;
+  if (!C.active) return;
+  const int j = blockIdx.x * kBX + threadIdx.x;
+  const int i = blockIdx.y * kBY + threadIdx.y;
+  const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+  const long long P = v.pitch, FP = v.fpitch;
+  long long back, front, fidx;
+  int ax;
+  if (dirx) {
+    if (i >= v.ny || j < 1 || j >= v.nx) return;
+    front = (long long)i * v.nx + j;
+    back = front - 1;
+    fidx = (long long)i * (v.nx + 1) + j;
+    ax = 0;
+  } else {
+    if (j >= v.nx || i < 1 || i >= v.ny) return;
+    back = (long long)i * v.nx + j;
+    front = back - v.nx;
+    fidx = (long long)i * v.nx + j;
+    ax = 1;
+  }
+  const double dx = (v.XcL[ax * P + front] - v.XcL[ax * P + back]) + 0.0;
+  for (int k = 0; k < v.ncomp; ++k)
+    v.phiF[k * FP + fidx] = qdiv(v.Phi[k * P + front] - v.Phi[k * P + back], dx);
+}
+
 // Limited slopes and plateau-slope integrals of one sweep
 // (Remap::computeGradPhiFace{1,2} + computeGradPhi{1,2},
 // remap/PhaseRemap1.cc:22-323, remap/PhaseRemap2.cc:21-323).
@@ -459,32 +490,26 @@ __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) {
   // reference naming: cf = "front" (right / below), cb = "back" (left / above)
   long long cf, cb;
   bool has_gp, has_gm;       // gradient faces exist (inner)
-  long long gpn, gmn;        // neighbour used by each face gradient
   if (dirx) {
     cf = (j < v.nx - 1) ? c + 1 : c;
     cb = (j > 0) ? c - 1 : c;
     has_gp = (j < v.nx - 1);  // right face
     has_gm = (j > 0);         // left face
-    gpn = c + 1;
-    gmn = c - 1;
   } else {
     cf = (i > 0) ? c - v.nx : c;
     cb = (i < v.ny - 1) ? c + v.nx : c;
     has_gp = (i > 0);          // bottom face
     has_gm = (i < v.ny - 1);   // top face
-    gpn = c - v.nx;
-    gmn = c + v.nx;
   }
-  const int ax = dirx ? 0 : 1;
-  const double xc = v.XcL[ax * P + c];
-  // deltaxLagrange of the two faces (dot with the axis normal)
-  double dxp = 0., dxm = 0.;
+  // face gradients written by k_face_grad
+  const long long FP = v.fpitch;
+  long long fp_idx, fm_idx;
   if (dirx) {
-    if (has_gp) dxp = (v.XcL[gpn] - xc) + 0.0;
-    if (has_gm) dxm = (xc - v.XcL[gmn]) + 0.0;
+    fm_idx = (long long)i * (v.nx + 1) + j;  // left face
+    fp_idx = fm_idx + 1;                     // right face
   } else {
-    if (has_gp) dxp = (v.XcL[P + gpn] - xc) + 0.0;
-    if (has_gm) dxm = (xc - v.XcL[P + gmn]) + 0.0;
+    fp_idx = (long long)i * v.nx + j;        // bottom face
+    fm_idx = fp_idx + v.nx;                  // top face
   }
   const bool vp = (v.pb_mixte == 1) &&
                   (v.mixte[c] == 0 && v.mixte[cf] == 0 && v.mixte[cb] == 0 &&
@@ -499,15 +524,8 @@ __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) {
   for (int k = 0; k < ncomp; ++k) {
     const double y0 = v.Phi[k * P + c];
     const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
-    // face gradients: (Phi(front) - Phi(back)) / deltaxLagrange
-    double gp = 0., gm = 0.;
-    if (dirx) {
-      if (has_gp) gp = (yp - y0) / dxp;
-      if (has_gm) gm = (y0 - ym) / dxm;
-    } else {
-      if (has_gp) gp = (ym - y0) / dxp;
-      if (has_gm) gm = (y0 - yp) / dxm;
-    }
+    const double gp = has_gp ? v.phiF[k * FP + fp_idx] : 0.;
+    const double gm = has_gm ? v.phiF[k * FP + fm_idx] : 0.;
     grad[k] = limit_grad1(lim, gp, gm, yp, ym, h0, hp, hm);
     if (v.pb == 0) v.gP[k * P + c] = grad[k];
   }
@@ -545,13 +563,27 @@ __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) {
     for (int k = 0; k < nuse; ++k) {
       const double y0 = v.Phi[k * P + c];
       const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
-      const PPShape sh = pp_shape(plim, v.threshold, y0, yp, ym, hh, hp, hm, grad[k]);
-      if (k < nint) {
-        Fr[k] = pp_integral(sh, -hh / 2., -hh / 2. + ppa, hh, y0, yp, ym, ppa);
-        Fv[k] = pp_integral(sh, hh / 2. - ppb, hh / 2., hh, y0, yp, ym, ppb);
+      const bool dual_k = cfd && k >= nb && k < 2 * nb;
+      double fa_, fb_, fd_;
+      if (((yp - y0) * (ym - y0)) >= 0.) {
+        // "formule 16" (UtilesRemap-Impl.h:201-203): the reference replaces
+        // every integral of this component by y0 * swept length, so the
+        // reconstruction is not built
+        fa_ = y0 * ppa;
+        fb_ = y0 * ppb;
+        fd_ = y0 * ppd;
+      } else {
+        const PPShape sh = pp_shape(plim, v.threshold, y0, yp, ym, hh, hp, hm, grad[k]);
+        fa_ = (k < nint) ? pp_integral(sh, -hh / 2., -hh / 2. + ppa, hh, y0, yp, ym, ppa) : 0.;
+        fb_ = (k < nint) ? pp_integral(sh, hh / 2. - ppb, hh / 2., hh, y0, yp, ym, ppb) : 0.;
+        fd_ = dual_k ? pp_integral(sh, 0., ppd, hh, y0, yp, ym, ppd) : 0.;
       }
-      if (cfd && k >= nb && k < 2 * nb) {
-        double d = pp_integral(sh, 0., ppd, hh, y0, yp, ym, ppd);
+      if (k < nint) {
+        Fr[k] = fa_;
+        Fv[k] = fb_;
+      }
+      if (dual_k) {
+        double d = fd_;
         if (ppd == 0.) d = 0.;
         v.DPF[(k - nb) * P + c] = d * flen;
       }
@@ -748,16 +780,16 @@ __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep)
       for (int m = 0; m < nb; m++) sv += U[m];
       double sm = 0.;
       for (int m = 0; m < nb; m++) {
-        Phi[m * P + c] = U[m] / sv;
-        Phi[(nb + m) * P + c] = (U[m] != 0.) ? U[nb + m] / (U[m]) : 0.;
+        Phi[m * P + c] = qdiv(U[m], sv);
+        Phi[(nb + m) * P + c] = (U[m] != 0.) ? qdiv(U[nb + m], U[m]) : 0.;
         sm += U[nb + m];
       }
       for (int m = 0; m < nb; m++)
-        Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? U[2 * nb + m] / U[nb + m] : 0.;
+        Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
       (void)sm;
     } else {
       const double vl = v.vL[c];
-      for (int k = 0; k < ncomp; ++k) Phi[k * P + c] = U[k] / vl;
+      for (int k = 0; k < ncomp; ++k) Phi[k * P + c] = qdiv(U[k], vl);
     }
     int matcell = 0, imatpure = -1;
     for (int m = 0; m < nb; m++)
@@ -817,8 +849,8 @@ __global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) {
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const double dp = D[k * NP + p], dr = D[k * NP + R], dl = D[k * NP + L];
-        const double gr = (dr - dp) / (xr - xp);
-        const double gl = (dp - dl) / (xp - xl);
+        const double gr = qdiv(dr - dp, xr - xp);
+        const double gl = qdiv(dp - dl, xp - xl);
         g[k] = limit_grad1(v.limiter, gr, gl, dr, dl, h0, hp, hm);
       }
       g0 = g[0];
@@ -903,12 +935,12 @@ __global__ void __launch_bounds__(kBX* kBY) k_dual_update(RunView v, int sweep) 
     }
     if (v.dual_method == 2) {
       if (nface != 0) {
-        pp /= nface;
-        pm /= nface;
+        pp = div_pow2(pp, nface);
+        pm = div_pow2(pm, nface);
       }
     } else if (nface != 0) {
-      pp /= (2 * nface);
-      pm /= (2 * nface);
+      pp = div_pow2(pp, 2 * nface);
+      pm = div_pow2(pm, 2 * nface);
     }
     Fp += pp;
     Fm += pm;
@@ -1007,16 +1039,16 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   }
   double vnorm = 0.;
   for (int m = 0; m < nb; m++) {
-    vn[m] *= vol / volt;
+    vn[m] *= qdiv(vol, volt);
     vnorm += vn[m];
   }
   double f[3], mf[3], sf = 0.;
   for (int m = 0; m < nb; m++) {
-    f[m] = vn[m] / vnorm;
+    f[m] = qdiv(vn[m], vnorm);
     if (f[m] < thr) f[m] = 0.;
     sf += f[m];
   }
-  for (int m = 0; m < nb; m++) f[m] = f[m] / sf;
+  for (int m = 0; m < nb; m++) f[m] = qdiv(f[m], sf);
   int matcell = 0, imatpure = -1;
   for (int m = 0; m < nb; m++)
     if (f[m] > 0.) {
@@ -1025,28 +1057,28 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     }
   v.mixte[c] = (matcell > 1) ? 1 : 0;
   v.pure[c] = (matcell > 1) ? -1 : imatpure;
-  for (int m = 0; m < nb; m++) mf[m] = U[(nb + m) * P] / masset;
+  for (int m = 0; m < nb; m++) mf[m] = qdiv(U[(nb + m) * P], masset);
   double fmt = 0.;
   for (int m = 0; m < nb; m++) {
     if (f[m] < thr) mf[m] = 0.;
     fmt += mf[m];
   }
-  for (int m = 0; m < nb; m++) mf[m] /= fmt;
+  for (int m = 0; m < nb; m++) mf[m] = qdiv(mf[m], fmt);
   double dm[3] = {0., 0., 0.}, dens = 0.;
   for (int m = 0; m < nb; m++) {
-    if (f[m] > thr) dm[m] = U[(nb + m) * P] / vn[m];
+    if (f[m] > thr) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
     dens += f[m] * dm[m];
   }
   double em[3] = {0., 0., 0.};
   for (int m = 0; m < nb; m++)
     if ((f[m] > thr) && (U[(nb + m) * P] != 0.))
-      em[m] = U[(2 * nb + m) * P] / U[(nb + m) * P];
+      em[m] = qdiv(U[(2 * nb + m) * P], U[(nb + m) * P]);
   const double rho = dens;
   double e = 0.;
   const double cmass = v.euler_volume * rho;
   v.cell_mass[c] = cmass;
   for (int m = 0; m < nb; m++) v.cmassm[m * P + c] = mf[m] * cmass;
-  v.q[c] = U[3 * nb * P] / vol;
+  v.q[c] = qdiv(U[3 * nb * P], vol);
   for (int m = 0; m < nb; m++) e += mf[m] * em[m];
   double rhom[3], emo[3];
   for (int m = 0; m < nb; m++) {
@@ -1187,7 +1219,7 @@ void launch_node_mass(const RunView& v, cudaStream_t s) {
 const char* const kKernelNames[kNumKernelKinds] = {
     "k_begin",      "k_reset_reductions", "k_lag_nodes", "k_lag_cells",
     "k_sweep_grad", "k_sweep_face",       "k_sweep_update", "k_dual_grad",
-    "k_dual_update", "k_final",           "k_end"};
+    "k_dual_update", "k_final",           "k_end",         "k_face_grad"};
 
 // Enqueues one full cycle on stream s; hook(kind) is called before each
 // launch (and with kind = -1 after the last) when given.  Returns the number
@@ -1205,7 +1237,10 @@ int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook) {
   H(2); k_lag_nodes<<<ng, blk, 0, s>>>(v); ++nk;
   H(3); k_lag_cells<<<cg, blk, 0, s>>>(v); ++nk;
   for (int sweep = 1; sweep <= 2; ++sweep) {
-    if (v.order > 1) { H(4); k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk; }
+    if (v.order > 1) {
+      H(11); k_face_grad<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+      H(4); k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk;
+    }
     H(5); k_sweep_face<<<fg, blk, 0, s>>>(v, sweep); ++nk;
     H(6); k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
     H(7); k_dual_grad<<<ng, blk, 0, s>>>(v, sweep); ++nk;
