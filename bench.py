@@ -226,6 +226,89 @@ def run_reference(args) -> None:
     print(json.dumps(line))
 
 
+BATCH_WORKLOAD = {
+    "workload": "512 independent VNR runs, order-2 remap, minmod or superBee, "
+                "no PenteBorne: 1/3 Sod (X or Y, 1 or 2 materials), 1/3 Sedov, "
+                "1/3 advection step; nx log-uniform 64..1024, ny 64..256 "
+                "(std::mt19937_64 seed 20261203), 100 cycles each",
+    "instances": 512, "seed": 20261203,
+    "l2": "state (~20 GB) >> L2 (129 MB)",
+}
+
+
+def bench_batch(M, ctx, args, local: int) -> dict:
+    """The mixed batch: plain path (each run through its own CUDA graph, one
+    after another) against the batched path (one persistent launch per phase
+    for all 512 runs), on the same runs at nearby cycles."""
+    from mahyco_gb300.workloads import batch_mix
+    mix = batch_mix(args.batch_n)
+    cells = sum(i.cells for i in mix)
+    t0 = time.perf_counter()
+    runs = [M.Run(i.spec(M), ctx) for i in mix]
+    create_s = time.perf_counter() - t0
+    state = sum(r.device_bytes for r in runs)
+    import ctypes
+    lib = M.lib()
+    stream = ctypes.c_void_p(ctx.stream)
+    # plain path: warm (graph capture) then K2 cycles of every run, enqueued
+    # back to back, timed with events on the context's stream
+    K2 = 8
+    for r in runs:
+        r.enqueue(1)
+    for r in runs:
+        r.sync()
+    import torch
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    launches0 = sum(r.kernel_launches for r in runs)
+    with Clocks(local) as clk_plain:
+        ev0.record(ext)
+        for r in runs:
+            r.enqueue(K2)
+        ev1.record(ext)
+        ev1.synchronize()
+    plain_ms = ev0.elapsed_time(ev1)
+    plain_launches = sum(r.kernel_launches for r in runs) - launches0
+    plain_val = cells * K2 / (plain_ms * 1e-3)
+    # batched path: tuning cycles + warm-up, then K timed cycles
+    batch = M.Batch(runs, ctx)
+    batch.step(11 + 3)  # 11 tuning cycles (10 candidates + warm-up), 3 warm
+    K = args.batch_steps
+    b0 = batch.kernel_launches
+    with Clocks(local) as clk_batch:
+        bms = batch.timed(K)
+    b_launches = batch.kernel_launches - b0
+    bval = cells * K / (bms * 1e-3)
+    prof = batch.profile(2)
+    kinds = {k: v for k, v in prof.items() if v[1] > 0}
+    t1 = time.perf_counter()
+    left = batch.step(100)
+    fetched = sum(r.fetch("density").nbytes for r in runs)
+    finish_s = time.perf_counter() - t1
+    cyc = [r.time()[2] for r in runs]
+    errs = sum(1 for r in runs if r.error()[0] & ~M.ERR_NEGATIVE)
+    cfg = batch.config()
+    for r in runs:
+        r.close()
+    return {
+        "value": bval, "unit": UNIT, "ms_per_step": bms / K, "steps": K,
+        "gpu_launches": b_launches,
+        "plain_mix": {"value": plain_val, "unit": UNIT, "ms_per_step": plain_ms / K2,
+                      "steps": K2, "gpu_launches": plain_launches,
+                      "clocks": clk_plain.summary(),
+                      "how": "each run's own CUDA graph (8 cycles), runs enqueued "
+                             "one after another, events around the sweep"},
+        "speedup_vs_plain_mix": bval / plain_val,
+        "cells": cells, "state_bytes": state, "create_s": create_s,
+        "finish_s": finish_s, "fetch_bytes": fetched, "runs_left": left,
+        "cycles_done": [min(cyc), max(cyc)], "runs_in_error": errs,
+        "tuning": cfg, "clocks": clk_batch.summary(),
+        "kernel_ms": {k: [round(v[0], 4), v[1]] for k, v in kinds.items()},
+        "config": BATCH_WORKLOAD,
+    }
+
+
 def run_ours(args) -> None:
     rank, world, local = dist_env()
     if world > 1:
@@ -310,6 +393,7 @@ def run_ours(args) -> None:
     if n != 2048:
         cfg["mesh"] = [n, n]
         cfg["workload"] = cfg["workload"].replace("2048x2048", f"{n}x{n}")
+    batched = None if args.no_batch else bench_batch(M, ctx, args, local)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
@@ -318,6 +402,7 @@ def run_ours(args) -> None:
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
         "gpu_launches": launches,
         "kernel_ms": {k: [round(v[0], 4), v[1]] for k, v in kinds.items()},
+        "batched": batched,
     }
     print(json.dumps(line))
 
@@ -330,6 +415,9 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mesh", type=int, default=2048)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-n", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=40)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

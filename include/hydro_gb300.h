@@ -139,6 +139,29 @@ const char* hydro_kernel_name(int kind);
 int hydro_kernel_kinds(void);
 int hydro_fp64_peak(int device, double* tflops);
 
+/* Batched form (no counterpart in the reference, which advances one mesh
+ * per scheme object; each run's cycle is Vnr::executeTimeLoopN's cycle).
+ * Advances every run of the list by up to ncycles cycles with one
+ * persistent launch per phase for all of them; runs that end stop
+ * independently.  All runs must belong to ctx.  The first cycles of a new
+ * list tune tile widths and grid sizes on the real work (results do not
+ * depend on the tuning).  *nactive = runs still going. */
+int hydro_batch_step(hydro_ctx* ctx, hydro_run* const* runs, int nruns,
+                     int ncycles, int* nactive);
+int hydro_batch_enqueue(hydro_ctx* ctx, hydro_run* const* runs, int nruns,
+                        int ncycles);
+int hydro_batch_timed(hydro_ctx* ctx, hydro_run* const* runs, int nruns,
+                      int ncycles, float* ms);
+int hydro_batch_profile(hydro_ctx* ctx, hydro_run* const* runs, int nruns,
+                        int ncycles, double* ms, long long* launches,
+                        int nkinds);
+/* Tile width and height (items) and grid (blocks) chosen per batched phase;
+ * returns 1 once a timed tuning pass has chosen them. */
+int hydro_batch_config(hydro_ctx* ctx, int* width, int* height, int* grid,
+                       int nphases);
+int hydro_batch_set_tuning(hydro_ctx* ctx, int enable);
+long long hydro_batch_kernel_launches(hydro_ctx* ctx);
+
 /* CFL time step of a VNR state held in caller device memory, allocating
  * nothing (no counterpart in the reference; it restates the reduction of
  * Vnr::computeDeltaT with the remap on).  For callers that may not call

@@ -106,6 +106,16 @@ def lib() -> C.CDLL:
         L.hydro_kernel_name.restype = C.c_char_p
         L.hydro_kernel_kinds.restype = i
         L.hydro_fp64_peak.argtypes = [i, C.POINTER(C.c_double)]
+        runs_t = C.POINTER(vp)
+        L.hydro_batch_step.argtypes = [vp, runs_t, i, i, C.POINTER(i)]
+        L.hydro_batch_enqueue.argtypes = [vp, runs_t, i, i]
+        L.hydro_batch_timed.argtypes = [vp, runs_t, i, i, C.POINTER(C.c_float)]
+        L.hydro_batch_profile.argtypes = [vp, runs_t, i, i, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_longlong), i]
+        L.hydro_batch_config.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i), i]
+        L.hydro_batch_set_tuning.argtypes = [vp, i]
+        L.hydro_batch_kernel_launches.argtypes = [vp]
+        L.hydro_batch_kernel_launches.restype = C.c_longlong
         _lib = L
     return _lib
 
@@ -254,3 +264,65 @@ class Run:
     @property
     def device_bytes(self) -> int:
         return int(lib().hydro_run_device_bytes(self.h))
+
+
+BATCH_PHASES = ("lag_nodes", "lag_cells", "face_grad", "sweep_grad",
+                "sweep_face", "sweep_update", "dual_grad", "dual_update",
+                "final")
+
+
+class Batch:
+    """Many runs of one context advanced together, one persistent launch per
+    phase for all of them (hydro_batch_step)."""
+
+    def __init__(self, runs: list[Run], ctx: Context | None = None):
+        self.ctx = ctx or runs[0].ctx
+        self.runs = list(runs)
+        self._arr = (C.c_void_p * len(self.runs))(*[r.h.value for r in self.runs])
+
+    @property
+    def cells(self) -> int:
+        return sum(r.spec.nx * r.spec.ny for r in self.runs)
+
+    def step(self, ncycles: int = 1) -> int:
+        """Advances every run by up to ncycles; returns the runs still going."""
+        act = C.c_int(0)
+        _check(lib().hydro_batch_step(self.ctx.h, self._arr, len(self.runs), ncycles,
+                                      C.byref(act)), "hydro_batch_step")
+        return act.value
+
+    def enqueue(self, ncycles: int) -> None:
+        _check(lib().hydro_batch_enqueue(self.ctx.h, self._arr, len(self.runs), ncycles),
+               "hydro_batch_enqueue")
+
+    def timed(self, ncycles: int) -> float:
+        ms = C.c_float()
+        _check(lib().hydro_batch_timed(self.ctx.h, self._arr, len(self.runs), ncycles,
+                                       C.byref(ms)), "hydro_batch_timed")
+        return ms.value
+
+    def profile(self, ncycles: int) -> dict:
+        nk = lib().hydro_kernel_kinds()
+        ms = (C.c_double * nk)()
+        cnt = (C.c_longlong * nk)()
+        _check(lib().hydro_batch_profile(self.ctx.h, self._arr, len(self.runs), ncycles,
+                                         ms, cnt, nk), "hydro_batch_profile")
+        return {lib().hydro_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(nk)}
+
+    def config(self) -> dict:
+        n = len(BATCH_PHASES)
+        w, h, g = (C.c_int * n)(), (C.c_int * n)(), (C.c_int * n)()
+        rc = lib().hydro_batch_config(self.ctx.h, w, h, g, n)
+        if rc < 0:
+            _check(rc, "hydro_batch_config")
+        return {"tuned": bool(rc),
+                "phases": {BATCH_PHASES[k]: {"tile": [w[k], h[k]], "grid": g[k]}
+                           for k in range(n)}}
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().hydro_batch_kernel_launches(self.ctx.h))
+
+
+def set_batch_tuning(ctx: Context, enable: bool) -> None:
+    _check(lib().hydro_batch_set_tuning(ctx.h, int(enable)), "hydro_batch_set_tuning")

@@ -64,9 +64,21 @@ void lpc_npc(const double* xp, const double* xpp, const double* xpm,
 
 int init_bc(const hydro_spec& s, HostInit& h) {
   const int t = s.test_case;
-  if (t == 4 || t == 15 || t == 5 || t == 16 || t == 1 || t == 12) {
-    // Sod / BiSod (vnr_remap/Init.cc:10-37); Sedov extension: walls
+  if (t == 4 || t == 15 || t == 5 || t == 16) {
+    // Sod / BiSod (vnr_remap/Init.cc:10-37): walls
     h.bc_left = h.bc_right = h.bc_top = h.bc_bottom = kBcSym;
+  } else if (t == 1) {
+    // Sedov (extension for VNR): the boundary conditions of the Eucclhyd
+    // Sedov case (eucclhyd_remap/Init.cc:47-64): symmetry on the left and
+    // bottom, zero imposed velocity on the right and top
+    h.bc_left = kBcSym;
+    h.bc_bottom = kBcSym;
+    h.bc_right = kBcImposed;
+    h.v_right[0] = 0.0;
+    h.v_right[1] = 0.0;
+    h.bc_top = kBcImposed;
+    h.v_top[0] = 0.0;
+    h.v_top[1] = 0.0;
   } else if (t == 7 || t == 18 || t == 9 || t == 20) {
     // Advection X (Init.cc:38-50)
     h.bc_right = kBcImposed;
@@ -207,6 +219,54 @@ int build_initial_state(const hydro_spec& s, HostInit& h) {
         F(h.cm, 1, c) = std::sqrt(g * r1 / p1);
         h.c[c] = smin(F(h.cm, 0, c), F(h.cm, 1, c));
       }
+    }
+  } else if (t == 1) {
+    // Sedov (extension for VNR, after eucclhyd_remap/Init.cc:303-332): rho 1,
+    // p 1e-6, the energy 0.244816 deposited in the cell that touches the
+    // origin, expressed as that cell's pressure; sound speed as the VNR Sod
+    // initialisation writes it (Init.cc:139-142)
+    const double e1 = 1.e-6 / ((s.gamma[0] - 1.0) * 1.0);
+    for (long long c = 0; c < nc; ++c) {
+      long long nd[4];
+      M.nodes(c, nd);
+      bool centre = false;
+      for (int k = 0; k < 4; ++k)
+        if (norm2(X[2 * nd[k]], X[2 * nd[k] + 1]) < s.threshold) centre = true;
+      const double e = centre ? e1 + 0.244816 / (s.dx * s.dy) : e1;
+      F(h.fm, 0, c) = 1.;
+      F(h.mfm, 0, c) = 1.;
+      h.rho[c] = 1.0;
+      F(h.rhom, 0, c) = 1.0;
+      h.p[c] = (s.gamma[0] - 1.0) * 1.0 * e;
+      F(h.pm, 0, c) = h.p[c];
+      F(h.cm, 0, c) = std::sqrt(g * F(h.rhom, 0, c) / F(h.pm, 0, c));
+      h.c[c] = F(h.cm, 0, c);
+    }
+  } else if (t == 18 && s.init_variant == 2) {
+    // advection step (extension): material 1 with rho 1 left of x = 0.5,
+    // material 2 with rho 0.1 right of it, uniform velocity (1, 0); pressure,
+    // energy and sound speed as the reference advection cases (Init.cc
+    // :185-260)
+    for (long long c = 0; c < nc; ++c) {
+      const double r = Xc[2 * c];
+      const int m = (r < 0.5) ? 0 : 1;
+      const double d = (m == 0) ? 1.0 : 0.1;
+      F(h.fm, m, c) = 1.;
+      F(h.mfm, m, c) = 1.;
+      h.rho[c] = d;
+      h.p[c] = 0.0;
+      F(h.rhom, m, c) = d;
+      F(h.pm, m, c) = 0.0;
+      F(h.cm, 0, c) = 1.;
+      F(h.cm, 1, c) = 1.;
+      h.c[c] = smin(F(h.cm, 0, c), F(h.cm, 1, c));
+      F(h.em, 0, c) = 1.;
+      F(h.em, 1, c) = 1.;
+      h.e[c] = 1.;
+    }
+    for (long long pn = 0; pn < nn; ++pn) {
+      h.u[pn] = 1.0;
+      h.u[nn + pn] = 0.0;
     }
   } else if (t == 7 || t == 8 || t == 18 || t == 19 || t == 20 || t == 21) {
     const bool isx = (t == 7 || t == 18 || t == 20);

@@ -10,8 +10,8 @@
 #include <string>
 #include <vector>
 
-#include "../internal.h"
 #include "init.h"
+#include "runtime.h"
 
 namespace hydro {
 
@@ -22,44 +22,9 @@ int fail(int rc, const std::string& msg) {
   return rc;
 }
 
-void launch_prologue(const RunView& v, cudaStream_t s);
-int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook);
-void launch_node_mass(const RunView& v, cudaStream_t s);
-int measure_fp64_peak(int device, double* tflops);
-
-#define CUDA_TRY(expr)                                                     \
-  do {                                                                     \
-    cudaError_t e_ = (expr);                                               \
-    if (e_ != cudaSuccess)                                                 \
-      return fail(-100, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
-
 }  // namespace hydro
 
 using namespace hydro;
-
-struct hydro_ctx {
-  int device = 0;
-  size_t budget = 0;
-  size_t used = 0;
-  cudaStream_t stream = nullptr;
-  std::mutex mu;
-};
-
-struct hydro_run {
-  hydro_ctx* ctx = nullptr;
-  hydro_spec spec{};
-  RunView v{};
-  HostInit init;     // kept for the Euler geometry / sizes
-  void* arena = nullptr;
-  size_t arena_bytes = 0;
-  Ctrl* d_ctrl = nullptr;
-  Ctrl h_ctrl{};
-  cudaGraphExec_t graph = nullptr;
-  int graph_cycles = 0;
-  int kernels_per_cycle = 0;
-  long long kernels_launched = 0;
-};
 
 namespace {
 
@@ -182,6 +147,7 @@ int hydro_ctx_create(int device, size_t budget, hydro_ctx** out) {
   auto* c = new hydro_ctx();
   c->device = device;
   c->budget = budget;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -194,6 +160,10 @@ int hydro_ctx_create(int device, size_t budget, hydro_ctx** out) {
 void hydro_ctx_destroy(hydro_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
+  destroy_serve(c->serve);
+  c->serve = nullptr;
+  destroy_plan(c->plan);
+  c->plan = nullptr;
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -205,11 +175,12 @@ int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out) {
   auto* r = new hydro_run();
   r->ctx = ctx;
   r->spec = *spec;
-  if (int rc = build_initial_state(*spec, r->init)) {
+  HostInit h;
+  if (int rc = build_initial_state(*spec, h)) {
     delete r;
     return rc;
   }
-  const HostInit& h = r->init;
+  r->dt_init = h.dt_init;
   RunView& v = r->v;
   v.nx = spec->nx;
   v.ny = spec->ny;
@@ -356,6 +327,7 @@ int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out) {
 int hydro_run_destroy(hydro_run* r) {
   if (!r) return 0;
   cudaSetDevice(r->ctx->device);
+  plan_forget_run(r->ctx->plan, r);
   if (r->graph) cudaGraphExecDestroy(r->graph);
   if (r->arena) cudaFree(r->arena);
   r->ctx->used -= r->arena_bytes;

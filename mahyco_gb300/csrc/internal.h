@@ -117,6 +117,57 @@ using LaunchHook = std::function<void(int)>;
 constexpr int kNumKernelKinds = 12;
 extern const char* const kKernelNames[kNumKernelKinds];
 
+// ---- batched execution: many independent runs advance in one launch per
+// phase.  The items of every run (cells, or nodes / faces) are cut into
+// tiles of kBatchThreads items; a launch walks a device-resident tile table
+// with a persistent grid, so the table can change without re-capturing the
+// CUDA graph that holds the launch.
+constexpr int kBatchThreads = 128;
+struct Tile {
+  int inst;    // index into the batch's RunView array
+  int i0, j0;  // first row / column of the tile
+  int pad;
+};
+struct BatchArgs {
+  const RunView* views;
+  const Tile* tiles;
+  const int* ntiles;  // device-resident tile count
+  int tw_log2;        // tile width 2^tw_log2
+  int rows;           // item rows per thread row
+  int sweep;
+};
+// Item phases of a cycle, in launch order; the two domains are cells
+// (nx x ny) and nodes ((nx+1) x (ny+1), which also index the faces).
+enum BatchPhase {
+  kPhLagNodes, kPhLagCells, kPhFaceGrad, kPhSweepGrad, kPhSweepFace,
+  kPhSweepUpdate, kPhDualGrad, kPhDualUpdate, kPhFinal, kNumPhases
+};
+constexpr bool phase_on_nodes(int ph) {
+  return ph == kPhLagNodes || ph == kPhFaceGrad || ph == kPhSweepFace ||
+         ph == kPhDualGrad || ph == kPhDualUpdate;
+}
+// Tile shapes: 2^tw_log2 items wide; each of the block's
+// kBatchThreads >> tw_log2 thread rows covers `rows` item rows, so one tile
+// (one staging of the run's view) serves kBatchThreads * rows items.
+struct TileShape {
+  int tw_log2;
+  int rows;
+};
+constexpr int kNumTileShapes = 5;
+constexpr TileShape kTileShapes[kNumTileShapes] = {
+    {5, 1}, {5, 4}, {5, 8}, {6, 4}, {7, 2}};
+struct BatchLaunch {
+  const RunView* views;
+  const int* ninst;      // device-resident number of runs
+  int max_inst;          // capacity of views / done
+  int* done;             // per run: Ctrl.done after the cycle
+  const Tile* tiles[2][kNumTileShapes];   // [on_nodes][shape]
+  const int* ntiles[2][kNumTileShapes];
+  int shape[kNumPhases];  // tile shape index per phase
+  int grid[kNumPhases];   // persistent grid size per phase
+  int any_order2;         // launch the slope phases
+};
+
 }  // namespace hydro
 
 #endif

@@ -31,8 +31,21 @@ constexpr int kBX = 32, kBY = 4;  // 2D cell / node tiles
 
 HD double ld(const double* p, long long i) { return __ldg(p + i); }
 
+// Per-material options read by select rather than by a dynamic index, so a
+// RunView copied into registers (batched launches) is never spilled whole to
+// local memory.
+HD double gamma_of(const RunView& v, int m) {
+  return m == 0 ? v.gamma[0] : (m == 1 ? v.gamma[1] : v.gamma[2]);
+}
+HD int eos_of(const RunView& v, int m) {
+  return m == 0 ? v.eos[0] : (m == 1 ? v.eos[1] : v.eos[2]);
+}
+
 // ----------------------------------------------------------------- control
-__global__ void k_begin(RunView v) {
+// Cycle start: dt_{n+1} and t_{n+1} from the previous cycle's reductions
+// (VnrRemap.cc:190-200), then the reduction slots are reset before this
+// cycle's final kernel accumulates into them.
+__device__ __forceinline__ void begin_at(const RunView& v) {
   Ctrl& C = *v.ctrl;
   if (C.done || (C.err & ~HYDRO_ERR_NEGATIVE)) {
     C.active = 0;
@@ -50,7 +63,16 @@ __global__ void k_begin(RunView v) {
   C.t_np1 = C.t_n + C.dt_np1;
 }
 
-__global__ void k_end(RunView v) {
+__device__ __forceinline__ void reset_at(const RunView& v) {
+  Ctrl& C = *v.ctrl;
+  if (!C.active) return;
+  C.pmax_prev = from_ord(C.pmax_bits);
+  C.dt_min_bits = ord_bits(1.7976931348623157e308);
+  C.pmax_bits = ord_bits(-1.7976931348623157e308);
+}
+
+// Loop condition and time swap (VnrRemap.cc:194-221).
+__device__ __forceinline__ void end_at(const RunView& v) {
   Ctrl& C = *v.ctrl;
   if (!C.active) return;
   bool cont = (C.n + 1 < v.max_iter && C.t_np1 < v.final_time);
@@ -63,15 +85,9 @@ __global__ void k_end(RunView v) {
   if (C.err & ~HYDRO_ERR_NEGATIVE) C.done = 1;
 }
 
-// Resets the reduction slots of the control block before a cycle's final
-// kernel accumulates into them.
-__global__ void k_reset_reductions(RunView v) {
-  Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  C.pmax_prev = from_ord(C.pmax_bits);
-  C.dt_min_bits = ord_bits(1.7976931348623157e308);
-  C.pmax_bits = ord_bits(-1.7976931348623157e308);
-}
+__global__ void k_begin(RunView v) { begin_at(v); }
+__global__ void k_reset_reductions(RunView v) { reset_at(v); }
+__global__ void k_end(RunView v) { end_at(v); }
 
 // block-wide min / max of ordered encodings, one atomic per block
 __device__ void block_reduce_minmax(unsigned long long dtv,
@@ -105,6 +121,8 @@ __device__ void block_reduce_minmax(unsigned long long dtv,
       atomicMax(&C->pmax_bits, pv);
     }
   }
+  // the shared slots are reused by the next tile of a batched block
+  __syncthreads();
 }
 
 // dt candidate of one cell (Vnr::computeDeltaT, VnrRemap.cc:26-46) with
@@ -122,120 +140,120 @@ HD double cell_dt(const RunView& v, long long c, int i, int j) {
 // Vnr::computeNodeMass (PhaseLagrange.cc:31-48), updateVelocity (:167-197),
 // updateVelocityBoundaryConditions (ConditionsLimites.cc:12-185),
 // updatePosition (:203-208).
-__global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) {
-  const Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  const int j = blockIdx.x * kBX + threadIdx.x;
-  const int i = blockIdx.y * kBY + threadIdx.y;
-  if (i > v.ny || j > v.nx) return;
-  const long long p = (long long)i * (v.nx + 1) + j;
-  // cells of node, getCellsOfNode order (CartesianMesh2D.cc:97-108); loc is
-  // the node's position in each cell's node list
-  long long cells[4];
-  int loc[4], k = 0;
-  if (i < v.ny && j < v.nx) { cells[k] = (long long)i * v.nx + j; loc[k++] = 0; }
-  if (i < v.ny && j > 0) { cells[k] = (long long)i * v.nx + j - 1; loc[k++] = 1; }
-  if (i > 0 && j < v.nx) { cells[k] = (long long)(i - 1) * v.nx + j; loc[k++] = 3; }
-  if (i > 0 && j > 0) { cells[k] = (long long)(i - 1) * v.nx + j - 1; loc[k++] = 2; }
-  double msum = 0.0;
-  for (int t = 0; t < k; ++t) msum = msum + v.cell_mass[cells[t]];
-  const double m = div_pow2(msum, k);  // msum / k, k in {1, 2, 4}
-  v.node_mass[p] = m;
+struct LagNodes {
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    const Ctrl& C = *v.ctrl;
+    if (i > v.ny || j > v.nx) return;
+    const long long p = (long long)i * (v.nx + 1) + j;
+    // cells of node, getCellsOfNode order (CartesianMesh2D.cc:97-108); loc is
+    // the node's position in each cell's node list
+    long long cells[4];
+    int loc[4], k = 0;
+    if (i < v.ny && j < v.nx) { cells[k] = (long long)i * v.nx + j; loc[k++] = 0; }
+    if (i < v.ny && j > 0) { cells[k] = (long long)i * v.nx + j - 1; loc[k++] = 1; }
+    if (i > 0 && j < v.nx) { cells[k] = (long long)(i - 1) * v.nx + j; loc[k++] = 3; }
+    if (i > 0 && j > 0) { cells[k] = (long long)(i - 1) * v.nx + j - 1; loc[k++] = 2; }
+    double msum = 0.0;
+    for (int t = 0; t < k; ++t) msum = msum + v.cell_mass[cells[t]];
+    const double m = div_pow2(msum, k);  // msum / k, k in {1, 2, 4}
+    v.node_mass[p] = m;
 
-  double ux = v.u[p], uy = v.u[v.npitch + p];
-  if (v.sans_lagrange == 0) {
-    const double dt = 0.5 * (C.dt_np1 + C.dt_n);
-    const double s = dt / m;
-    auto force = [&](bool sym, double sx, double sy, double& r0, double& r1) {
-      r0 = 0.0;
-      r1 = 0.0;
-      for (int t = 0; t < k; ++t) {
-        const long long c = cells[t];
-        const double C0 = ld(v.cqs, (2 * loc[t]) * v.pitch + c);
-        const double C1 = ld(v.cqs, (2 * loc[t] + 1) * v.pitch + c);
-        const double w = v.p[c] + v.q[c];
-        if (!sym) {
-          r0 = r0 + w * C0;
-          r1 = r1 + w * C1;
-        } else {
-          double d = 0.0;
-          d = d + C0 * sx;
-          d = d + C1 * sy;
-          const double s2 = 2.0 * d;
-          const double sv0 = sx * s2 - C0, sv1 = sy * s2 - C1;
-          r0 = r0 + w * (C0 + sv0);
-          r1 = r1 + w * (C1 + sv1);
+    double ux = v.u[p], uy = v.u[v.npitch + p];
+    if (v.sans_lagrange == 0) {
+      const double dt = 0.5 * (C.dt_np1 + C.dt_n);
+      const double s = dt / m;
+      auto force = [&](bool sym, double sx, double sy, double& r0, double& r1) {
+        r0 = 0.0;
+        r1 = 0.0;
+        for (int t = 0; t < k; ++t) {
+          const long long c = cells[t];
+          const double C0 = ld(v.cqs, (2 * loc[t]) * v.pitch + c);
+          const double C1 = ld(v.cqs, (2 * loc[t] + 1) * v.pitch + c);
+          const double w = v.p[c] + v.q[c];
+          if (!sym) {
+            r0 = r0 + w * C0;
+            r1 = r1 + w * C1;
+          } else {
+            double d = 0.0;
+            d = d + C0 * sx;
+            d = d + C1 * sy;
+            const double s2 = 2.0 * d;
+            const double sv0 = sx * s2 - C0, sv1 = sy * s2 - C1;
+            r0 = r0 + w * (C0 + sv0);
+            r1 = r1 + w * (C1 + sv1);
+          }
+        }
+      };
+      const double u0x = ux, u0y = uy;
+      double r0, r1;
+      if (i > 0 && i < v.ny && j > 0 && j < v.nx) {
+        force(false, 0., 0., r0, r1);
+        ux = u0x + s * r0;
+        uy = u0y + s * r1;
+      }
+      // sides in the reference's order: bottom, top, left, right
+      if (i == 0) {
+        if (v.bc_bottom == kBcSym) {
+          force(true, 1.0, 0.0, r0, r1);
+          ux = u0x + s * r0;
+          uy = u0y + s * r1;
+        } else if (v.bc_bottom == kBcImposed) {
+          ux = v.v_bottom[0];
+          uy = v.v_bottom[1];
         }
       }
-    };
-    const double u0x = ux, u0y = uy;
-    double r0, r1;
-    if (i > 0 && i < v.ny && j > 0 && j < v.nx) {
-      force(false, 0., 0., r0, r1);
-      ux = u0x + s * r0;
-      uy = u0y + s * r1;
-    }
-    // sides in the reference's order: bottom, top, left, right
-    if (i == 0) {
-      if (v.bc_bottom == kBcSym) {
-        force(true, 1.0, 0.0, r0, r1);
-        ux = u0x + s * r0;
-        uy = u0y + s * r1;
-      } else if (v.bc_bottom == kBcImposed) {
-        ux = v.v_bottom[0];
-        uy = v.v_bottom[1];
+      if (i == v.ny) {
+        if (v.bc_top == kBcSym) {
+          force(true, 1.0, 0.0, r0, r1);
+          ux = u0x + s * r0;
+          uy = u0y + s * r1;
+        } else if (v.bc_top == kBcImposed) {
+          ux = v.v_top[0];
+          uy = v.v_top[1];
+        }
       }
-    }
-    if (i == v.ny) {
-      if (v.bc_top == kBcSym) {
-        force(true, 1.0, 0.0, r0, r1);
-        ux = u0x + s * r0;
-        uy = u0y + s * r1;
-      } else if (v.bc_top == kBcImposed) {
-        ux = v.v_top[0];
-        uy = v.v_top[1];
+      if (j == 0) {
+        if (v.bc_left == kBcSym) {
+          force(true, 0.0, 1.0, r0, r1);
+          ux = u0x + s * r0;
+          uy = u0y + s * r1;
+        } else if (v.bc_left == kBcImposed) {
+          ux = v.v_left[0];
+          uy = v.v_left[1];
+        }
       }
-    }
-    if (j == 0) {
-      if (v.bc_left == kBcSym) {
-        force(true, 0.0, 1.0, r0, r1);
-        ux = u0x + s * r0;
-        uy = u0y + s * r1;
-      } else if (v.bc_left == kBcImposed) {
-        ux = v.v_left[0];
-        uy = v.v_left[1];
+      if (j == v.nx) {
+        if (v.bc_right == kBcSym) {
+          force(true, 0.0, 1.0, r0, r1);
+          ux = u0x + s * r0;
+          uy = u0y + s * r1;
+        } else if (v.bc_right == kBcImposed) {
+          ux = v.v_right[0];
+          uy = v.v_right[1];
+        }
       }
-    }
-    if (j == v.nx) {
-      if (v.bc_right == kBcSym) {
-        force(true, 0.0, 1.0, r0, r1);
-        ux = u0x + s * r0;
-        uy = u0y + s * r1;
-      } else if (v.bc_right == kBcImposed) {
-        ux = v.v_right[0];
-        uy = v.v_right[1];
+      // corners (ConditionsLimites.cc:133-184)
+      const bool top = (i == v.ny), bot = (i == 0), lft = (j == 0), rgt = (j == v.nx);
+      if ((top || bot) && (lft || rgt)) {
+        const int bv = top ? v.bc_top : v.bc_bottom;
+        const int bh = lft ? v.bc_left : v.bc_right;
+        const double vh0 = lft ? v.v_left[0] : v.v_right[0];
+      const double vh1 = lft ? v.v_left[1] : v.v_right[1];
+        if (bv == kBcSym && bh == kBcSym) {
+          ux = 0.0;
+          uy = 0.0;
+        } else if (bv == kBcImposed && bh == kBcImposed) {
+          ux = vh0;
+          uy = vh1;
+        }
       }
+      v.u[p] = ux;
+      v.u[v.npitch + p] = uy;
     }
-    // corners (ConditionsLimites.cc:133-184)
-    const bool top = (i == v.ny), bot = (i == 0), lft = (j == 0), rgt = (j == v.nx);
-    if ((top || bot) && (lft || rgt)) {
-      const int bv = top ? v.bc_top : v.bc_bottom;
-      const int bh = lft ? v.bc_left : v.bc_right;
-      const double* vh = lft ? v.v_left : v.v_right;
-      if (bv == kBcSym && bh == kBcSym) {
-        ux = 0.0;
-        uy = 0.0;
-      } else if (bv == kBcImposed && bh == kBcImposed) {
-        ux = vh[0];
-        uy = vh[1];
-      }
-    }
-    v.u[p] = ux;
-    v.u[v.npitch + p] = uy;
+    v.XL[p] = ld(v.xs, j) + C.dt_np1 * ux;
+    v.XL[v.npitch + p] = ld(v.ys, i) + C.dt_np1 * uy;
   }
-  v.XL[p] = ld(v.xs, j) + C.dt_np1 * ux;
-  v.XL[v.npitch + p] = ld(v.ys, i) + C.dt_np1 * uy;
-}
+};
 
 // ------------------------------------------------------- Lagrange: cells
 // updateCellPos, computeSubVol, updateRho (PhaseLagrange.cc:214-296),
@@ -245,192 +263,191 @@ __global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) {
 // then computeVariablesForRemap / computeCellQuantitesForRemap
 // (vnr_remap/PrepareRemap.cc:65-176) and the Lagrangian face lengths that
 // give HvLagrange (remap/PhaseRemap1.cc:57-71, 104-119).
-__global__ void __launch_bounds__(kBX* kBY) k_lag_cells(RunView v) {
-  Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  const int j = blockIdx.x * kBX + threadIdx.x;
-  const int i = blockIdx.y * kBY + threadIdx.y;
-  if (i >= v.ny || j >= v.nx) return;
-  const long long c = (long long)i * v.nx + j;
-  const long long P = v.pitch, NP = v.npitch;
-  const long long n0 = (long long)i * (v.nx + 1) + j;
-  const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
-  double X[4][2];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    X[k][0] = v.XL[nd[k]];
-    X[k][1] = v.XL[NP + nd[k]];
-  }
-  // centre and sub-volumes
-  double xc0 = 0.0, xc1 = 0.0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    xc0 = xc0 + X[k][0];
-    xc1 = xc1 + X[k][1];
-  }
-  xc0 = 0.25 * xc0;
-  xc1 = 0.25 * xc1;
-  double vol = 0.0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int km = (k + 3) & 3, kp = (k + 1) & 3;
-    const double x2a = 0.5 * (X[km][0] + X[k][0]), x2b = 0.5 * (X[km][1] + X[k][1]);
-    const double x4a = 0.5 * (X[kp][0] + X[k][0]), x4b = 0.5 * (X[kp][1] + X[k][1]);
-    const double c12 = xc0 * x2b - xc1 * x2a;
-    const double c23 = x2a * X[k][1] - x2b * X[k][0];
-    const double c34 = X[k][0] * x4b - X[k][1] * x4a;
-    const double c41 = x4a * xc1 - x4b * xc0;
-    vol = vol + 0.5 * (c12 + c23 + c34 + c41);
-  }
-  const int nb = v.nbmat;
-  const double thr = v.threshold;
-  double f[3], mf[3], rhom_new[3];
-  double rho_new = 0.;
-#pragma unroll
-  for (int m = 0; m < 3; ++m) {
-    if (m >= nb) break;
-    f[m] = v.fm[m * P + c];
-    mf[m] = v.mfm[m * P + c];
-    const double rm = v.rhom[m * P + c];
-    rhom_new[m] = rm;
-    if (f[m] > thr) rhom_new[m] = v.cmassm[m * P + c] / (f[m] * vol);
-    rho_new += f[m] * rhom_new[m];
-  }
-  double e_new, q_new;
-  if (v.sans_lagrange == 0) {
-    const double rho_old = v.rho[c];
-    const double tau = 0.5 * (1.0 / rho_new + 1.0 / rho_old);
-    const double divu_new = 1.0 / C.dt_np1 * (1.0 / rho_new - 1.0 / rho_old) / tau;
-    const double c_old = v.c[c];
-    if (v.divu[c] < 0.0) {
-      const double s0 = ld(v.s0, c);
-      q_new = 1.0 / tau *
-              (-0.5 * ld(v.sqs0, c) * c_old * divu_new +
-               (v.gamma_scalar + 1) / 2.0 * s0 * divu_new * divu_new);
+struct LagCells {
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    Ctrl& C = *v.ctrl;
+    if (i >= v.ny || j >= v.nx) return;
+    const long long c = (long long)i * v.nx + j;
+    const long long P = v.pitch, NP = v.npitch;
+    const long long n0 = (long long)i * (v.nx + 1) + j;
+    const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
+    double X[4][2];
+  #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      X[k][0] = v.XL[nd[k]];
+      X[k][1] = v.XL[NP + nd[k]];
+    }
+    // centre and sub-volumes
+    double xc0 = 0.0, xc1 = 0.0;
+  #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      xc0 = xc0 + X[k][0];
+      xc1 = xc1 + X[k][1];
+    }
+    xc0 = 0.25 * xc0;
+    xc1 = 0.25 * xc1;
+    double vol = 0.0;
+  #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int km = (k + 3) & 3, kp = (k + 1) & 3;
+      const double x2a = 0.5 * (X[km][0] + X[k][0]), x2b = 0.5 * (X[km][1] + X[k][1]);
+      const double x4a = 0.5 * (X[kp][0] + X[k][0]), x4b = 0.5 * (X[kp][1] + X[k][1]);
+      const double c12 = xc0 * x2b - xc1 * x2a;
+      const double c23 = x2a * X[k][1] - x2b * X[k][0];
+      const double c34 = X[k][0] * x4b - X[k][1] * x4a;
+      const double c41 = x4a * xc1 - x4b * xc0;
+      vol = vol + 0.5 * (c12 + c23 + c34 + c41);
+    }
+    const int nb = v.nbmat;
+    const double thr = v.threshold;
+    double f[3], mf[3], rhom_new[3];
+    double rho_new = 0.;
+  #pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      f[m] = v.fm[m * P + c];
+      mf[m] = v.mfm[m * P + c];
+      const double rm = v.rhom[m * P + c];
+      rhom_new[m] = rm;
+      if (f[m] > thr) rhom_new[m] = v.cmassm[m * P + c] / (f[m] * vol);
+      rho_new += f[m] * rhom_new[m];
+    }
+    double e_new, q_new;
+    if (v.sans_lagrange == 0) {
+      const double rho_old = v.rho[c];
+      const double tau = 0.5 * (1.0 / rho_new + 1.0 / rho_old);
+      const double divu_new = 1.0 / C.dt_np1 * (1.0 / rho_new - 1.0 / rho_old) / tau;
+      const double c_old = v.c[c];
+      if (v.divu[c] < 0.0) {
+        const double s0 = ld(v.s0, c);
+        q_new = 1.0 / tau *
+                (-0.5 * ld(v.sqs0, c) * c_old * divu_new +
+                 (v.gamma_scalar + 1) / 2.0 * s0 * divu_new * divu_new);
+      } else {
+        q_new = 0.0;
+      }
+      if (q_new > C.pmax_prev) q_new = C.pmax_prev;
+      v.divu[c] = divu_new;
+      // energies (updateEnergy) and EOS
+      e_new = 0.;
+      double pm_new[3], cm_new[3], em_new[3];
+      bool bad = false;
+  #pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        const double qm_old = v.qm[m * P + c];
+        const double qm_new = f[m] * q_new;
+        v.qm[m * P + c] = qm_new;
+        const double rn = rhom_new[m], ro = v.rhom[m * P + c];
+        em_new[m] = 0.;
+        if ((rn > thr) && (ro > thr)) {
+          double pseudo = 0.;
+          if ((v.pseudo_centree == 1) && ((qm_new + qm_old) * (1.0 / rn - 1.0 / ro) > 0.))
+            pseudo = 0.5 * (qm_new + qm_old);
+          if (v.pseudo_centree == 0) pseudo = qm_new;
+          const double den = 1 + 0.5 * (gamma_of(v, m) - 1.0) * rn * (1.0 / rn - 1.0 / ro);
+          const double num = v.em[m * P + c] - (0.5 * v.pm[m * P + c] + pseudo) * (1.0 / rn - 1.0 / ro);
+          em_new[m] = num / den;
+          e_new += mf[m] * em_new[m];
+          if (v.energy_limit > 0 && fabs(em_new[m]) > v.energy_limit) bad = true;
+        }
+      }
+      if (bad) {
+        atomicOr(&C.err, HYDRO_ERR_ENERGY);
+        atomicMin((unsigned long long*)&C.err_cell, (unsigned long long)c);
+      }
+  #pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
+          const double g = gamma_of(v, m);
+          pm_new[m] = (g - 1.0) * rhom_new[m] * em_new[m];
+          cm_new[m] = sqrt(g * (g - 1.0) * em_new[m]);
+        } else {  // Void: state kept
+          pm_new[m] = v.pm[m * P + c];
+          cm_new[m] = v.cm[m * P + c];
+          em_new[m] = v.em[m * P + c];
+        }
+      }
+      for (int m = 0; m < nb; ++m)
+        if (eos_of(v, m) == HYDRO_EOS_VOID) e_new = 0.;
+      // computePressionMoyenne: the stale max argument is the in-place c
+      double cc = c_old;
+      for (int m = 0; m < nb; ++m) cc = smax(cc, cm_new[m]);
+      if (rho_new > 0.) {
+        const double g0 = v.gamma[0];
+        cc = sqrt(g0 * (g0 - 1.0) * e_new);
+      }
+      for (int m = 0; m < nb; ++m)
+        if (eos_of(v, m) == HYDRO_EOS_VOID) e_new += mf[m] * em_new[m];
+      v.c[c] = cc;
+      (void)pm_new;
     } else {
-      q_new = 0.0;
+      // no Lagrange phase (advection cases): energy and q are carried over
+      e_new = v.e[c];
+      q_new = v.q[c];
+      // updatePeriodicBoundaryConditions: first and last column take the
+      // initial density of the row's first cell
+      if (v.periodic_x && (j == v.nx - 1 || j == 0)) rho_new = ld(v.rho0_left, i);
     }
-    if (q_new > C.pmax_prev) q_new = C.pmax_prev;
-    v.divu[c] = divu_new;
-    // energies (updateEnergy) and EOS
-    e_new = 0.;
-    double pm_new[3], cm_new[3], em_new[3];
-    bool bad = false;
-#pragma unroll
+    // ---- PrepareRemap (cell part)
+    const int ncomp = v.ncomp;
+    double U[kMaxComp];
+  #pragma unroll
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
-      const double qm_old = v.qm[m * P + c];
-      const double qm_new = f[m] * q_new;
-      v.qm[m * P + c] = qm_new;
-      const double rn = rhom_new[m], ro = v.rhom[m * P + c];
-      em_new[m] = 0.;
-      if ((rn > thr) && (ro > thr)) {
-        double pseudo = 0.;
-        if ((v.pseudo_centree == 1) && ((qm_new + qm_old) * (1.0 / rn - 1.0 / ro) > 0.))
-          pseudo = 0.5 * (qm_new + qm_old);
-        if (v.pseudo_centree == 0) pseudo = qm_new;
-        const double den = 1 + 0.5 * (v.gamma[m] - 1.0) * rn * (1.0 / rn - 1.0 / ro);
-        const double num = v.em[m * P + c] - (0.5 * v.pm[m * P + c] + pseudo) * (1.0 / rn - 1.0 / ro);
-        em_new[m] = num / den;
-        e_new += mf[m] * em_new[m];
-        if (v.energy_limit > 0 && fabs(em_new[m]) > v.energy_limit) bad = true;
+      U[m] = f[m] * vol;
+      U[nb + m] = mf[m] * vol * rho_new;
+      U[2 * nb + m] = mf[m] * vol * rho_new * e_new;
+    }
+    U[3 * nb] = q_new * vol;  // reference slot 3*nbmat+3
+    for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
+    if (v.pb == 1) {
+      double sv = 0.;
+      for (int m = 0; m < nb; ++m) sv += U[m];
+      for (int m = 0; m < nb; ++m) {
+        v.Phi[m * P + c] = qdiv(U[m], sv);
+        v.Phi[(nb + m) * P + c] = (U[m] != 0.) ? qdiv(U[nb + m], U[m]) : 0.;
+        v.Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
       }
+      v.Phi[3 * nb * P + c] = q_new;
+    } else {
+      for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv(U[k], vol);
     }
-    if (bad) {
-      atomicOr(&C.err, HYDRO_ERR_ENERGY);
-      atomicMin((unsigned long long*)&C.err_cell, (unsigned long long)c);
+    v.vL[c] = vol;
+    v.rL[c] = rho_new;
+    // Lagrangian centroid (PrepareRemap.cc:65-90)
+    double r0 = 0.0, r1 = 0.0;
+  #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int kp = (k + 1) & 3;
+      const double cr = X[k][0] * X[kp][1] - X[k][1] * X[kp][0];
+      r0 = r0 + cr * (X[k][0] + X[kp][0]);
+      r1 = r1 + cr * (X[k][1] + X[kp][1]);
     }
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-      if (m >= nb) break;
-      if (v.eos[m] == HYDRO_EOS_PERFECT_GAS) {
-        const double g = v.gamma[m];
-        pm_new[m] = (g - 1.0) * rhom_new[m] * em_new[m];
-        cm_new[m] = sqrt(g * (g - 1.0) * em_new[m]);
-      } else {  // Void: state kept
-        pm_new[m] = v.pm[m * P + c];
-        cm_new[m] = v.cm[m * P + c];
-        em_new[m] = v.em[m * P + c];
-      }
+    const double sc = 1.0 / (6.0 * vol);
+    v.XcL[c] = sc * r0;
+    v.XcL[P + c] = sc * r1;
+    // Lagrangian face lengths -> HvLagrange for both sweep directions
+    if (v.order > 1) {
+      auto len = [&](int a, int b) {
+        const double d0 = X[b][0] - X[a][0], d1 = X[b][1] - X[a][1];
+        double r = 0.0;
+        r = r + d0 * d0;
+        r = r + d1 * d1;
+        return sqrt(r);
+      };
+      double hx = 0.;
+      hx += 0.5 * len(0, 1);  // bottom face
+      hx += 0.5 * len(3, 2);  // top face
+      double hy = 0.;
+      hy += 0.5 * len(1, 2);  // right face
+      hy += 0.5 * len(0, 3);  // left face
+      v.Hx[c] = hx;
+      v.Hy[c] = hy;
     }
-    for (int m = 0; m < nb; ++m)
-      if (v.eos[m] == HYDRO_EOS_VOID) e_new = 0.;
-    // computePressionMoyenne: the stale max argument is the in-place c
-    double cc = c_old;
-    for (int m = 0; m < nb; ++m) cc = smax(cc, cm_new[m]);
-    if (rho_new > 0.) {
-      const double g0 = v.gamma[0];
-      cc = sqrt(g0 * (g0 - 1.0) * e_new);
-    }
-    for (int m = 0; m < nb; ++m)
-      if (v.eos[m] == HYDRO_EOS_VOID) e_new += mf[m] * em_new[m];
-    v.c[c] = cc;
-    (void)pm_new;
-  } else {
-    // no Lagrange phase (advection cases): energy and q are carried over
-    e_new = v.e[c];
-    q_new = v.q[c];
-    // updatePeriodicBoundaryConditions: first and last column take the
-    // initial density of the row's first cell
-    if (v.periodic_x && (j == v.nx - 1 || j == 0)) rho_new = ld(v.rho0_left, i);
   }
-  // ---- PrepareRemap (cell part)
-  const int ncomp = v.ncomp;
-  double U[kMaxComp];
-#pragma unroll
-  for (int m = 0; m < 3; ++m) {
-    if (m >= nb) break;
-    U[m] = f[m] * vol;
-    U[nb + m] = mf[m] * vol * rho_new;
-    U[2 * nb + m] = mf[m] * vol * rho_new * e_new;
-  }
-  U[3 * nb] = q_new * vol;  // reference slot 3*nbmat+3
-  for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
-  if (v.pb == 1) {
-    double sv = 0.;
-    for (int m = 0; m < nb; ++m) sv += U[m];
-    for (int m = 0; m < nb; ++m) {
-      v.Phi[m * P + c] = qdiv(U[m], sv);
-      v.Phi[(nb + m) * P + c] = (U[m] != 0.) ? qdiv(U[nb + m], U[m]) : 0.;
-      v.Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
-    }
-    v.Phi[3 * nb * P + c] = q_new;
-  } else {
-    for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv(U[k], vol);
-  }
-  v.vL[c] = vol;
-  v.rL[c] = rho_new;
-  // Lagrangian centroid (PrepareRemap.cc:65-90)
-  double r0 = 0.0, r1 = 0.0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int kp = (k + 1) & 3;
-    const double cr = X[k][0] * X[kp][1] - X[k][1] * X[kp][0];
-    r0 = r0 + cr * (X[k][0] + X[kp][0]);
-    r1 = r1 + cr * (X[k][1] + X[kp][1]);
-  }
-  const double sc = 1.0 / (6.0 * vol);
-  v.XcL[c] = sc * r0;
-  v.XcL[P + c] = sc * r1;
-  // Lagrangian face lengths -> HvLagrange for both sweep directions
-  if (v.order > 1) {
-    auto len = [&](int a, int b) {
-      const double d0 = X[b][0] - X[a][0], d1 = X[b][1] - X[a][1];
-      double r = 0.0;
-      r = r + d0 * d0;
-      r = r + d1 * d1;
-      return sqrt(r);
-    };
-    double hx = 0.;
-    hx += 0.5 * len(0, 1);  // bottom face
-    hx += 0.5 * len(3, 2);  // top face
-    double hy = 0.;
-    hy += 0.5 * len(1, 2);  // right face
-    hy += 0.5 * len(0, 3);  // left face
-    v.Hx[c] = hx;
-    v.Hy[c] = hy;
-  }
-}
+};
 
 // Face normal velocity (PrepareRemap.cc:42-63): mean of the two nodes'
 // Lagrange velocities along the face normal; "+ 0.0" is the dot product's
@@ -447,575 +464,577 @@ HD double fnv_horizontal(const RunView& v, long long na, long long nb) {
 // remap/PhaseRemap1.cc:22-55, PhaseRemap2.cc:21-55): one thread per inner
 // face perpendicular to the sweep, (Phi(front) - Phi(back)) / deltaxLagrange,
 // stored in the face-value planes (k_sweep_face overwrites them later).
-__global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) {
-  const Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  const int j = blockIdx.x * kBX + threadIdx.x;
-  const int i = blockIdx.y * kBY + threadIdx.y;
-  const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
-  const long long P = v.pitch, FP = v.fpitch;
-  long long back, front, fidx;
-  int ax;
-  if (dirx) {
-    if (i >= v.ny || j < 1 || j >= v.nx) return;
-    front = (long long)i * v.nx + j;
-    back = front - 1;
-    fidx = (long long)i * (v.nx + 1) + j;
-    ax = 0;
-  } else {
-    if (j >= v.nx || i < 1 || i >= v.ny) return;
-    back = (long long)i * v.nx + j;
-    front = back - v.nx;
-    fidx = (long long)i * v.nx + j;
-    ax = 1;
+struct FaceGrad {
+  int sweep;
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    if (v.order <= 1) return;  // no slopes at order 1 (batched launches)
+    const Ctrl& C = *v.ctrl;
+    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+    const long long P = v.pitch, FP = v.fpitch;
+    long long back, front, fidx;
+    int ax;
+    if (dirx) {
+      if (i >= v.ny || j < 1 || j >= v.nx) return;
+      front = (long long)i * v.nx + j;
+      back = front - 1;
+      fidx = (long long)i * (v.nx + 1) + j;
+      ax = 0;
+    } else {
+      if (j >= v.nx || i < 1 || i >= v.ny) return;
+      back = (long long)i * v.nx + j;
+      front = back - v.nx;
+      fidx = (long long)i * v.nx + j;
+      ax = 1;
+    }
+    const double dx = (v.XcL[ax * P + front] - v.XcL[ax * P + back]) + 0.0;
+    for (int k = 0; k < v.ncomp; ++k)
+      v.phiF[k * FP + fidx] = qdiv(v.Phi[k * P + front] - v.Phi[k * P + back], dx);
   }
-  const double dx = (v.XcL[ax * P + front] - v.XcL[ax * P + back]) + 0.0;
-  for (int k = 0; k < v.ncomp; ++k)
-    v.phiF[k * FP + fidx] = qdiv(v.Phi[k * P + front] - v.Phi[k * P + back], dx);
-}
+};
 
 // Limited slopes and plateau-slope integrals of one sweep
 // (Remap::computeGradPhiFace{1,2} + computeGradPhi{1,2},
 // remap/PhaseRemap1.cc:22-323, remap/PhaseRemap2.cc:21-323).
-__global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) {
-  const Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  const int j = blockIdx.x * kBX + threadIdx.x;
-  const int i = blockIdx.y * kBY + threadIdx.y;
-  if (i >= v.ny || j >= v.nx) return;
-  const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
-  const long long P = v.pitch;
-  const long long c = (long long)i * v.nx + j;
-  const double* H = dirx ? v.Hx : v.Hy;
-  // reference naming: cf = "front" (right / below), cb = "back" (left / above)
-  long long cf, cb;
-  bool has_gp, has_gm;       // gradient faces exist (inner)
-  if (dirx) {
-    cf = (j < v.nx - 1) ? c + 1 : c;
-    cb = (j > 0) ? c - 1 : c;
-    has_gp = (j < v.nx - 1);  // right face
-    has_gm = (j > 0);         // left face
-  } else {
-    cf = (i > 0) ? c - v.nx : c;
-    cb = (i < v.ny - 1) ? c + v.nx : c;
-    has_gp = (i > 0);          // bottom face
-    has_gm = (i < v.ny - 1);   // top face
-  }
-  // face gradients written by k_face_grad
-  const long long FP = v.fpitch;
-  long long fp_idx, fm_idx;
-  if (dirx) {
-    fm_idx = (long long)i * (v.nx + 1) + j;  // left face
-    fp_idx = fm_idx + 1;                     // right face
-  } else {
-    fp_idx = (long long)i * v.nx + j;        // bottom face
-    fm_idx = fp_idx + v.nx;                  // top face
-  }
-  const bool vp = (v.pb_mixte == 1) &&
-                  (v.mixte[c] == 0 && v.mixte[cf] == 0 && v.mixte[cb] == 0 &&
-                   v.pure[c] == v.pure[cf] && v.pure[c] == v.pure[cb]);
-  int lim = v.limiter;
-  if ((v.pb == 1) && vp) lim = v.limiter_pure;
-  // "plus" / "minus" neighbours in computeAndLimitGradPhi's argument order
-  const long long cp = dirx ? cf : cb, cm = dirx ? cb : cf;
-  const double h0 = H[c], hp = H[cp], hm = H[cm];
-  const int ncomp = v.ncomp, nb = v.nbmat;
-  double grad[kMaxComp];
-  for (int k = 0; k < ncomp; ++k) {
-    const double y0 = v.Phi[k * P + c];
-    const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
-    const double gp = has_gp ? v.phiF[k * FP + fp_idx] : 0.;
-    const double gm = has_gm ? v.phiF[k * FP + fm_idx] : 0.;
-    grad[k] = limit_grad1(lim, gp, gm, yp, ym, h0, hp, hm);
-    if (v.pb == 0) v.gP[k * P + c] = grad[k];
-  }
-  if (v.pb == 1) {
-    // Flux_sortant of the two faces, dual normal velocity, face lengths
-    const long long n0 = (long long)i * (v.nx + 1) + j;
-    double Fa, Fb, fa_v, fb_v, flen;
+struct SweepGrad {
+  int sweep;
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    if (v.order <= 1) return;  // no slopes at order 1 (batched launches)
+    const Ctrl& C = *v.ctrl;
+    if (i >= v.ny || j >= v.nx) return;
+    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+    const long long P = v.pitch;
+    const long long c = (long long)i * v.nx + j;
+    const double* H = dirx ? v.Hx : v.Hy;
+    // reference naming: cf = "front" (right / below), cb = "back" (left / above)
+    long long cf, cb;
+    bool has_gp, has_gm;       // gradient faces exist (inner)
     if (dirx) {
-      fa_v = fnv_vertical(v, n0, n0 + v.nx + 1);          // left face
-      fb_v = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);      // right face
-      Fa = ld(v.nout, 0 * P + c) * fa_v;
-      Fb = ld(v.nout, 1 * P + c) * fb_v;
-      flen = (ld(v.flv, i) + ld(v.flv, i)) * 0.5;
+      cf = (j < v.nx - 1) ? c + 1 : c;
+      cb = (j > 0) ? c - 1 : c;
+      has_gp = (j < v.nx - 1);  // right face
+      has_gm = (j > 0);         // left face
     } else {
-      fa_v = fnv_horizontal(v, n0, n0 + 1);               // bottom face
-      fb_v = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);  // top face
-      Fa = ld(v.nout, 2 * P + c) * fa_v;
-      Fb = ld(v.nout, 3 * P + c) * fb_v;
-      flen = (ld(v.flh, j) + ld(v.flh, j)) * 0.5;
+      cf = (i > 0) ? c - v.nx : c;
+      cb = (i < v.ny - 1) ? c + v.nx : c;
+      has_gp = (i > 0);          // bottom face
+      has_gm = (i < v.ny - 1);   // top face
     }
-    const double fdual = 0.5 * (fa_v + fb_v);
-    const double dt = C.dt_n;
-    const double ppa = 0.5 * (Fa + fabs(Fa)) * dt;
-    const double ppb = 0.5 * (Fb + fabs(Fb)) * dt;
-    const double ppd = 0.5 * (fdual + fabs(fdual)) * dt;
-    const bool cfd = (v.dual_method == 2);
-    const int plim = vp ? v.limiter_pure : v.limiter;
-    // which components are integrated: volumes always; masses for the pure
-    // variant; masses + energies for the "complet" variant; the dual flux
-    // needs the mass components (computeFluxPP, UtilesRemap-Impl.h:259-313)
-    const int nint = (v.pb_complet == 1) ? 3 * nb : (vp ? 2 * nb : nb);
-    const int nuse = (cfd && nint < 2 * nb) ? 2 * nb : nint;
-    double Fr[kMaxComp], Fv[kMaxComp];
-    const double hh = h0;
-    for (int k = 0; k < nuse; ++k) {
+    // face gradients written by k_face_grad
+    const long long FP = v.fpitch;
+    long long fp_idx, fm_idx;
+    if (dirx) {
+      fm_idx = (long long)i * (v.nx + 1) + j;  // left face
+      fp_idx = fm_idx + 1;                     // right face
+    } else {
+      fp_idx = (long long)i * v.nx + j;        // bottom face
+      fm_idx = fp_idx + v.nx;                  // top face
+    }
+    const bool vp = (v.pb_mixte == 1) &&
+                    (v.mixte[c] == 0 && v.mixte[cf] == 0 && v.mixte[cb] == 0 &&
+                     v.pure[c] == v.pure[cf] && v.pure[c] == v.pure[cb]);
+    int lim = v.limiter;
+    if ((v.pb == 1) && vp) lim = v.limiter_pure;
+    // "plus" / "minus" neighbours in computeAndLimitGradPhi's argument order
+    const long long cp = dirx ? cf : cb, cm = dirx ? cb : cf;
+    const double h0 = H[c], hp = H[cp], hm = H[cm];
+    const int ncomp = v.ncomp, nb = v.nbmat;
+    double grad[kMaxComp];
+    for (int k = 0; k < ncomp; ++k) {
       const double y0 = v.Phi[k * P + c];
       const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
-      const bool dual_k = cfd && k >= nb && k < 2 * nb;
-      double fa_, fb_, fd_;
-      if (((yp - y0) * (ym - y0)) >= 0.) {
-        // "formule 16" (UtilesRemap-Impl.h:201-203): the reference replaces
-        // every integral of this component by y0 * swept length, so the
-        // reconstruction is not built
-        fa_ = y0 * ppa;
-        fb_ = y0 * ppb;
-        fd_ = y0 * ppd;
-      } else {
-        const PPShape sh = pp_shape(plim, v.threshold, y0, yp, ym, hh, hp, hm, grad[k]);
-        fa_ = (k < nint) ? pp_integral(sh, -hh / 2., -hh / 2. + ppa, hh, y0, yp, ym, ppa) : 0.;
-        fb_ = (k < nint) ? pp_integral(sh, hh / 2. - ppb, hh / 2., hh, y0, yp, ym, ppb) : 0.;
-        fd_ = dual_k ? pp_integral(sh, 0., ppd, hh, y0, yp, ym, ppd) : 0.;
-      }
-      if (k < nint) {
-        Fr[k] = fa_;
-        Fv[k] = fb_;
-      }
-      if (dual_k) {
-        double d = fd_;
-        if (ppd == 0.) d = 0.;
-        v.DPF[(k - nb) * P + c] = d * flen;
-      }
+      const double gp = has_gp ? v.phiF[k * FP + fp_idx] : 0.;
+      const double gm = has_gm ? v.phiF[k * FP + fm_idx] : 0.;
+      grad[k] = limit_grad1(lim, gp, gm, yp, ym, h0, hp, hm);
+      if (v.pb == 0) v.gP[k * P + c] = grad[k];
     }
-    // derived fluxes
-    auto finish = [&](double* F, double ppv, double* out) {
-      if (v.pb_complet == 1) {
-        double sfm = 0., sfv = 0.;
-        for (int m = 0; m < nb; m++) sfv += F[m];
-        if (fabs(sfv) > v.threshold) {
+    if (v.pb == 1) {
+      // Flux_sortant of the two faces, dual normal velocity, face lengths
+      const long long n0 = (long long)i * (v.nx + 1) + j;
+      double Fa, Fb, fa_v, fb_v, flen;
+      if (dirx) {
+        fa_v = fnv_vertical(v, n0, n0 + v.nx + 1);          // left face
+        fb_v = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);      // right face
+        Fa = ld(v.nout, 0 * P + c) * fa_v;
+        Fb = ld(v.nout, 1 * P + c) * fb_v;
+        flen = (ld(v.flv, i) + ld(v.flv, i)) * 0.5;
+      } else {
+        fa_v = fnv_horizontal(v, n0, n0 + 1);               // bottom face
+        fb_v = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);  // top face
+        Fa = ld(v.nout, 2 * P + c) * fa_v;
+        Fb = ld(v.nout, 3 * P + c) * fb_v;
+        flen = (ld(v.flh, j) + ld(v.flh, j)) * 0.5;
+      }
+      const double fdual = 0.5 * (fa_v + fb_v);
+      const double dt = C.dt_n;
+      const double ppa = 0.5 * (Fa + fabs(Fa)) * dt;
+      const double ppb = 0.5 * (Fb + fabs(Fb)) * dt;
+      const double ppd = 0.5 * (fdual + fabs(fdual)) * dt;
+      const bool cfd = (v.dual_method == 2);
+      const int plim = vp ? v.limiter_pure : v.limiter;
+      // which components are integrated: volumes always; masses for the pure
+      // variant; masses + energies for the "complet" variant; the dual flux
+      // needs the mass components (computeFluxPP, UtilesRemap-Impl.h:259-313)
+      const int nint = (v.pb_complet == 1) ? 3 * nb : (vp ? 2 * nb : nb);
+      const int nuse = (cfd && nint < 2 * nb) ? 2 * nb : nint;
+      double Fr[kMaxComp], Fv[kMaxComp];
+      const double hh = h0;
+      for (int k = 0; k < nuse; ++k) {
+        const double y0 = v.Phi[k * P + c];
+        const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
+        const bool dual_k = cfd && k >= nb && k < 2 * nb;
+        double fa_, fb_, fd_;
+        if (((yp - y0) * (ym - y0)) >= 0.) {
+          // "formule 16" (UtilesRemap-Impl.h:201-203): the reference replaces
+          // every integral of this component by y0 * swept length, so the
+          // reconstruction is not built
+          fa_ = y0 * ppa;
+          fb_ = y0 * ppb;
+          fd_ = y0 * ppd;
+        } else {
+          const PPShape sh = pp_shape(plim, v.threshold, y0, yp, ym, hh, hp, hm, grad[k]);
+          fa_ = (k < nint) ? pp_integral(sh, -hh / 2., -hh / 2. + ppa, hh, y0, yp, ym, ppa) : 0.;
+          fb_ = (k < nint) ? pp_integral(sh, hh / 2. - ppb, hh / 2., hh, y0, yp, ym, ppb) : 0.;
+          fd_ = dual_k ? pp_integral(sh, 0., ppd, hh, y0, yp, ym, ppd) : 0.;
+        }
+        if (k < nint) {
+          Fr[k] = fa_;
+          Fv[k] = fb_;
+        }
+        if (dual_k) {
+          double d = fd_;
+          if (ppd == 0.) d = 0.;
+          v.DPF[(k - nb) * P + c] = d * flen;
+        }
+      }
+      // derived fluxes
+      auto finish = [&](double* F, double ppv, double* out) {
+        if (v.pb_complet == 1) {
+          double sfm = 0., sfv = 0.;
+          for (int m = 0; m < nb; m++) sfv += F[m];
+          if (fabs(sfv) > v.threshold) {
+            for (int m = 0; m < nb; m++) {
+              if (!vp) F[nb + m] = (F[nb + m] / sfv) * F[m];
+              F[2 * nb + m] = (F[2 * nb + m] / sfv) * F[nb + m];
+              sfm += F[nb + m];
+            }
+            F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
+          } else {
+            for (int k = 0; k < ncomp; ++k) F[k] = 0.0;
+          }
+        } else {
+          double sfv = 0.;
           for (int m = 0; m < nb; m++) {
-            if (!vp) F[nb + m] = (F[nb + m] / sfv) * F[m];
-            F[2 * nb + m] = (F[2 * nb + m] / sfv) * F[nb + m];
-            sfm += F[nb + m];
+            if (!vp) F[nb + m] = v.Phi[(nb + m) * P + c] * F[m];
+            F[2 * nb + m] = v.Phi[(2 * nb + m) * P + c] * F[nb + m];
+            sfv += F[m];
           }
           F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
-        } else {
-          for (int k = 0; k < ncomp; ++k) F[k] = 0.0;
         }
-      } else {
-        double sfv = 0.;
-        for (int m = 0; m < nb; m++) {
-          if (!vp) F[nb + m] = v.Phi[(nb + m) * P + c] * F[m];
-          F[2 * nb + m] = v.Phi[(2 * nb + m) * P + c] * F[nb + m];
-          sfv += F[m];
-        }
-        F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
-      }
-      for (int k = 0; k < ncomp; ++k) out[k * P] = (ppv == 0.) ? 0.0 : F[k];
-    };
-    finish(Fr, ppa, v.dPAr + c);
-    finish(Fv, ppb, v.dPAv + c);
+        for (int k = 0; k < ncomp; ++k) out[k * P] = (ppv == 0.) ? 0.0 : F[k];
+      };
+      finish(Fr, ppa, v.dPAr + c);
+      finish(Fv, ppb, v.dPAv + c);
+    }
   }
-}
+};
 
 // Face values of one sweep (Remap::computeUpwindFaceQuantitiesForProjection
 // {1,2}, remap/PhaseRemap1.cc:331-452, PhaseRemap2.cc:331-447).  One thread
 // per inner face perpendicular to the sweep; face (i, j) is the left face of
 // cell (i, j) (x sweep) or the bottom face of cell (i, j) (y sweep).
-__global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) {
-  const Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  const int j = blockIdx.x * kBX + threadIdx.x;
-  const int i = blockIdx.y * kBY + threadIdx.y;
-  const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
-  const long long P = v.pitch, FP = v.fpitch;
-  const int ncomp = v.ncomp;
-  long long cb, cf, fidx;
-  double fnv;
-  if (dirx) {
-    if (i >= v.ny || j < 1 || j >= v.nx) return;
-    cb = (long long)i * v.nx + j - 1;  // back = left
-    cf = cb + 1;                        // front = right
-    fidx = (long long)i * (v.nx + 1) + j;
-    const long long n0 = (long long)i * (v.nx + 1) + j;
-    fnv = fnv_vertical(v, n0, n0 + v.nx + 1);
-  } else {
-    if (j >= v.nx || i < 1 || i >= v.ny) return;
-    cb = (long long)i * v.nx + j;       // back = above
-    cf = cb - v.nx;                     // front = below
-    fidx = (long long)i * v.nx + j;
-    const long long n0 = (long long)i * (v.nx + 1) + j;
-    fnv = fnv_horizontal(v, n0, n0 + 1);
-  }
-  double* out = v.phiF + fidx;
-  const int ax = dirx ? 0 : 1;
-  if (v.order <= 2) {
-    if (v.pb == 0) {
-      const double dxl = (v.XcL[ax * P + cf] - v.XcL[ax * P + cb]) + 0.0;
-      const double xf = dirx ? ld(v.xs, j) : ld(v.ys, i);
-      const long long cu = (fnv * dxl > 0.0) ? cb : cf;
-      const double s = (xf - v.XcL[ax * P + cu]) + 0.0;
-      for (int k = 0; k < ncomp; ++k)
-        out[k * FP] = v.Phi[k * P + cu] + s * v.gP[k * P + cu];
-    } else {
-      const long long av = dirx ? cb : cf, ar = dirx ? cf : cb;
-      for (int k = 0; k < ncomp; ++k)
-        out[k * FP] = v.dPAv[k * P + av] - v.dPAr[k * P + ar];
-    }
-  } else {
-    // order 3: six cells along the sweep, "minus" side first, clamped
-    long long cs[6];
+struct SweepFace {
+  int sweep;
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    const Ctrl& C = *v.ctrl;
+    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+    const long long P = v.pitch, FP = v.fpitch;
+    const int ncomp = v.ncomp;
+    long long cb, cf, fidx;
+    double fnv;
     if (dirx) {
-      const int jb = j - 1, jf = j;
-      const int jbb = jb > 0 ? jb - 1 : jb, jbbb = jbb > 0 ? jbb - 1 : jbb;
-      const int jff = jf < v.nx - 1 ? jf + 1 : jf;
-      const int jfff = jff < v.nx - 1 ? jff + 1 : jff;
-      const long long r = (long long)i * v.nx;
-      cs[0] = r + jbbb; cs[1] = r + jbb; cs[2] = cb; cs[3] = cf;
-      cs[4] = r + jff; cs[5] = r + jfff;
+      if (i >= v.ny || j < 1 || j >= v.nx) return;
+      cb = (long long)i * v.nx + j - 1;  // back = left
+      cf = cb + 1;                        // front = right
+      fidx = (long long)i * (v.nx + 1) + j;
+      const long long n0 = (long long)i * (v.nx + 1) + j;
+      fnv = fnv_vertical(v, n0, n0 + v.nx + 1);
     } else {
-      const int i_f = i - 1, i_b = i;
-      const int iff = i_f > 0 ? i_f - 1 : i_f, ifff = iff > 0 ? iff - 1 : iff;
-      const int ibb = i_b < v.ny - 1 ? i_b + 1 : i_b;
-      const int ibbb = ibb < v.ny - 1 ? ibb + 1 : ibb;
-      cs[0] = (long long)ifff * v.nx + j; cs[1] = (long long)iff * v.nx + j;
-      cs[2] = cf; cs[3] = cb;
-      cs[4] = (long long)ibb * v.nx + j; cs[5] = (long long)ibbb * v.nx + j;
+      if (j >= v.nx || i < 1 || i >= v.ny) return;
+      cb = (long long)i * v.nx + j;       // back = above
+      cf = cb - v.nx;                     // front = below
+      fidx = (long long)i * v.nx + j;
+      const long long n0 = (long long)i * (v.nx + 1) + j;
+      fnv = fnv_horizontal(v, n0, n0 + 1);
     }
-    const double* H = dirx ? v.Hx : v.Hy;
-    const double* Uin = (sweep == 1) ? v.UL : v.U1;
-    const double vdt = fnv * C.dt_n;
-    double h[6];
-    for (int t = 0; t < 6; ++t) h[t] = H[cs[t]];
-    for (int k = 0; k < ncomp; ++k) {
-      double y[6];
-      for (int t = 0; t < 6; ++t) y[t] = Uin[k * P + cs[t]] / v.vL[cs[t]];
-      out[k * FP] = flux_ordre3(y[0], y[1], y[2], y[3], y[4], y[5], h[0], h[1],
-                                h[2], h[3], h[4], h[5], vdt);
+    double* out = v.phiF + fidx;
+    const int ax = dirx ? 0 : 1;
+    if (v.order <= 2) {
+      if (v.pb == 0) {
+        const double dxl = (v.XcL[ax * P + cf] - v.XcL[ax * P + cb]) + 0.0;
+        const double xf = dirx ? ld(v.xs, j) : ld(v.ys, i);
+        const long long cu = (fnv * dxl > 0.0) ? cb : cf;
+        const double s = (xf - v.XcL[ax * P + cu]) + 0.0;
+        for (int k = 0; k < ncomp; ++k)
+          out[k * FP] = v.Phi[k * P + cu] + s * v.gP[k * P + cu];
+      } else {
+        const long long av = dirx ? cb : cf, ar = dirx ? cf : cb;
+        for (int k = 0; k < ncomp; ++k)
+          out[k * FP] = v.dPAv[k * P + av] - v.dPAr[k * P + ar];
+      }
+    } else {
+      // order 3: six cells along the sweep, "minus" side first, clamped
+      long long cs[6];
+      if (dirx) {
+        const int jb = j - 1, jf = j;
+        const int jbb = jb > 0 ? jb - 1 : jb, jbbb = jbb > 0 ? jbb - 1 : jbb;
+        const int jff = jf < v.nx - 1 ? jf + 1 : jf;
+        const int jfff = jff < v.nx - 1 ? jff + 1 : jff;
+        const long long r = (long long)i * v.nx;
+        cs[0] = r + jbbb; cs[1] = r + jbb; cs[2] = cb; cs[3] = cf;
+        cs[4] = r + jff; cs[5] = r + jfff;
+      } else {
+        const int i_f = i - 1, i_b = i;
+        const int iff = i_f > 0 ? i_f - 1 : i_f, ifff = iff > 0 ? iff - 1 : iff;
+        const int ibb = i_b < v.ny - 1 ? i_b + 1 : i_b;
+        const int ibbb = ibb < v.ny - 1 ? ibb + 1 : ibb;
+        cs[0] = (long long)ifff * v.nx + j; cs[1] = (long long)iff * v.nx + j;
+        cs[2] = cf; cs[3] = cb;
+        cs[4] = (long long)ibb * v.nx + j; cs[5] = (long long)ibbb * v.nx + j;
+      }
+      const double* H = dirx ? v.Hx : v.Hy;
+      const double* Uin = (sweep == 1) ? v.UL : v.U1;
+      const double vdt = fnv * C.dt_n;
+      double h[6];
+      for (int t = 0; t < 6; ++t) h[t] = H[cs[t]];
+      for (int k = 0; k < ncomp; ++k) {
+        double y[6];
+        for (int t = 0; t < 6; ++t) y[t] = Uin[k * P + cs[t]] / v.vL[cs[t]];
+        out[k * FP] = flux_ordre3(y[0], y[1], y[2], y[3], y[4], y[5], h[0], h[1],
+                                  h[2], h[3], h[4], h[5], vdt);
+      }
     }
   }
-}
+};
 
 // Conservative update of one sweep (Remap::computeUremap{1,2},
 // remap/PhaseRemap1.cc:459-568, PhaseRemap2.cc:454-497).
-__global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) {
-  const Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  const int j = blockIdx.x * kBX + threadIdx.x;
-  const int i = blockIdx.y * kBY + threadIdx.y;
-  if (i >= v.ny || j >= v.nx) return;
-  const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
-  const long long P = v.pitch, FP = v.fpitch;
-  const long long c = (long long)i * v.nx + j;
-  const int ncomp = v.ncomp, nb = v.nbmat;
-  const double* Uin = (sweep == 1) ? v.UL : v.U1;
-  double* Uout = (sweep == 1) ? v.U1 : v.UL;
-  const double dt = C.dt_n;
-  // the two faces perpendicular to the sweep, in getNeighbourCells order
-  // (below before above, left before right); faces parallel to the sweep
-  // contribute 0 * phiFace and are skipped.
-  bool has[2];
-  long long fidx[2];
-  double coef[2];
-  const long long n0 = (long long)i * (v.nx + 1) + j;
-  if (dirx) {
-    has[0] = (j >= 1);
-    has[1] = (j < v.nx - 1);
-    fidx[0] = (long long)i * (v.nx + 1) + j;
-    fidx[1] = fidx[0] + 1;
-    const double fl = ld(v.flv, i);
-    const double va = fnv_vertical(v, n0, n0 + v.nx + 1);
-    const double vb = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);
-    const double na = ld(v.nout, 0 * P + c), nb_ = ld(v.nout, 1 * P + c);
-    if (v.pb == 0) {
-      coef[0] = na * va * fl * dt;
-      coef[1] = nb_ * vb * fl * dt;
-    } else {
-      coef[0] = na * fl;
-      coef[1] = nb_ * fl;
-    }
-  } else {
-    has[0] = (i >= 1);
-    has[1] = (i < v.ny - 1);
-    fidx[0] = (long long)i * v.nx + j;
-    fidx[1] = fidx[0] + v.nx;
-    const double fl = ld(v.flh, j);
-    const double va = fnv_horizontal(v, n0, n0 + 1);
-    const double vb = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);
-    const double na = ld(v.nout, 2 * P + c), nb_ = ld(v.nout, 3 * P + c);
-    if (v.pb == 0) {
-      coef[0] = na * va * fl * dt;
-      coef[1] = nb_ * vb * fl * dt;
-    } else {
-      coef[0] = na * fl;
-      coef[1] = nb_ * fl;
-    }
-  }
-  // dual-method components: masses (A1) or volumes (A2)
-  const int doff = (v.dual_method == 1) ? 0 : nb;
-  double U[kMaxComp];
-  for (int k = 0; k < ncomp; ++k) {
-    double red = 0.0;
-    double F0 = 0., F1 = 0.;
-    if (has[0]) {
-      F0 = coef[0] * v.phiF[k * FP + fidx[0]];
-      red = red + F0;
-    }
-    if (has[1]) {
-      F1 = coef[1] * v.phiF[k * FP + fidx[1]];
-      red = red + F1;
-    }
-    U[k] = Uin[k * P + c] - red;
-    Uout[k * P + c] = U[k];
-    if (v.dual_method != 2 && k >= doff && k < doff + nb) {
-      v.FFd[(k - doff) * P + c] = F0;
-      v.FFd[(nb + k - doff) * P + c] = F1;
-    }
-  }
-  if (sweep == 1) {
-    double* Phi = v.Phi;
-    if (v.pb == 1) {
-      double sv = 0.;
-      for (int m = 0; m < nb; m++) sv += U[m];
-      double sm = 0.;
-      for (int m = 0; m < nb; m++) {
-        Phi[m * P + c] = qdiv(U[m], sv);
-        Phi[(nb + m) * P + c] = (U[m] != 0.) ? qdiv(U[nb + m], U[m]) : 0.;
-        sm += U[nb + m];
+struct SweepUpdate {
+  int sweep;
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    const Ctrl& C = *v.ctrl;
+    if (i >= v.ny || j >= v.nx) return;
+    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+    const long long P = v.pitch, FP = v.fpitch;
+    const long long c = (long long)i * v.nx + j;
+    const int ncomp = v.ncomp, nb = v.nbmat;
+    const double* Uin = (sweep == 1) ? v.UL : v.U1;
+    double* Uout = (sweep == 1) ? v.U1 : v.UL;
+    const double dt = C.dt_n;
+    // the two faces perpendicular to the sweep, in getNeighbourCells order
+    // (below before above, left before right); faces parallel to the sweep
+    // contribute 0 * phiFace and are skipped.
+    bool has[2];
+    long long fidx[2];
+    double coef[2];
+    const long long n0 = (long long)i * (v.nx + 1) + j;
+    if (dirx) {
+      has[0] = (j >= 1);
+      has[1] = (j < v.nx - 1);
+      fidx[0] = (long long)i * (v.nx + 1) + j;
+      fidx[1] = fidx[0] + 1;
+      const double fl = ld(v.flv, i);
+      const double va = fnv_vertical(v, n0, n0 + v.nx + 1);
+      const double vb = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);
+      const double na = ld(v.nout, 0 * P + c), nb_ = ld(v.nout, 1 * P + c);
+      if (v.pb == 0) {
+        coef[0] = na * va * fl * dt;
+        coef[1] = nb_ * vb * fl * dt;
+      } else {
+        coef[0] = na * fl;
+        coef[1] = nb_ * fl;
       }
+    } else {
+      has[0] = (i >= 1);
+      has[1] = (i < v.ny - 1);
+      fidx[0] = (long long)i * v.nx + j;
+      fidx[1] = fidx[0] + v.nx;
+      const double fl = ld(v.flh, j);
+      const double va = fnv_horizontal(v, n0, n0 + 1);
+      const double vb = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);
+      const double na = ld(v.nout, 2 * P + c), nb_ = ld(v.nout, 3 * P + c);
+      if (v.pb == 0) {
+        coef[0] = na * va * fl * dt;
+        coef[1] = nb_ * vb * fl * dt;
+      } else {
+        coef[0] = na * fl;
+        coef[1] = nb_ * fl;
+      }
+    }
+    // dual-method components: masses (A1) or volumes (A2)
+    const int doff = (v.dual_method == 1) ? 0 : nb;
+    double U[kMaxComp];
+    for (int k = 0; k < ncomp; ++k) {
+      double red = 0.0;
+      double F0 = 0., F1 = 0.;
+      if (has[0]) {
+        F0 = coef[0] * v.phiF[k * FP + fidx[0]];
+        red = red + F0;
+      }
+      if (has[1]) {
+        F1 = coef[1] * v.phiF[k * FP + fidx[1]];
+        red = red + F1;
+      }
+      U[k] = Uin[k * P + c] - red;
+      Uout[k * P + c] = U[k];
+      if (v.dual_method != 2 && k >= doff && k < doff + nb) {
+        v.FFd[(k - doff) * P + c] = F0;
+        v.FFd[(nb + k - doff) * P + c] = F1;
+      }
+    }
+    if (sweep == 1) {
+      double* Phi = v.Phi;
+      if (v.pb == 1) {
+        double sv = 0.;
+        for (int m = 0; m < nb; m++) sv += U[m];
+        double sm = 0.;
+        for (int m = 0; m < nb; m++) {
+          Phi[m * P + c] = qdiv(U[m], sv);
+          Phi[(nb + m) * P + c] = (U[m] != 0.) ? qdiv(U[nb + m], U[m]) : 0.;
+          sm += U[nb + m];
+        }
+        for (int m = 0; m < nb; m++)
+          Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
+        (void)sm;
+      } else {
+        const double vl = v.vL[c];
+        for (int k = 0; k < ncomp; ++k) Phi[k * P + c] = qdiv(U[k], vl);
+      }
+      int matcell = 0, imatpure = -1;
       for (int m = 0; m < nb; m++)
-        Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
-      (void)sm;
-    } else {
-      const double vl = v.vL[c];
-      for (int k = 0; k < ncomp; ++k) Phi[k * P + c] = qdiv(U[k], vl);
-    }
-    int matcell = 0, imatpure = -1;
-    for (int m = 0; m < nb; m++)
-      if (Phi[m * P + c] > 0.) {
-        matcell++;
-        imatpure = m;
+        if (Phi[m * P + c] > 0.) {
+          matcell++;
+          imatpure = m;
+        }
+      if (matcell > 1) {
+        v.mixte[c] = 1;
+        v.pure[c] = -1;
+      } else {
+        v.mixte[c] = 0;
+        v.pure[c] = imatpure;
       }
-    if (matcell > 1) {
-      v.mixte[c] = 1;
-      v.pure[c] = -1;
-    } else {
-      v.mixte[c] = 0;
-      v.pure[c] = imatpure;
     }
   }
-}
+};
 
 // ------------------------------------------------------------- dual remap
 // Limited nodal velocity gradient along the sweep
 // (Remap::computeDualHorizontalGradPhi / computeDualVerticalGradPhi,
 // remap/UtilesRemap-Impl.h:8-97).  Only the two velocity components are
 // consumed downstream.
-__global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) {
-  const Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  const int j = blockIdx.x * kBX + threadIdx.x;
-  const int i = blockIdx.y * kBY + threadIdx.y;
-  if (i > v.ny || j > v.nx) return;
-  const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
-  const long long NP = v.npitch;
-  const long long p = (long long)i * (v.nx + 1) + j;
-  const double* D = (sweep == 1) ? v.u : v.DPv;  // DualPhi velocity
-  double g0 = 0.0, g1 = 0.0;
-  if (v.order > 1) {
-    const int ax = dirx ? 0 : 1;
-    const int pos = dirx ? j : i, lastpos = dirx ? v.nx : v.ny;
-    const long long stride = dirx ? 1 : (v.nx + 1);
-    if (pos != 0 && pos != lastpos) {
-      const long long L = p - stride, R = p + stride;
-      const double xp = v.XL[ax * NP + p], xr = v.XL[ax * NP + R],
-                   xl = v.XL[ax * NP + L];
-      double hm, hp;
-      const double h0 = 0.5 * (xr - xl);
-      const bool hasLL = (pos - 1 != 0), hasRR = (pos + 1 != lastpos);
-      if (!hasLL) {
-        hm = 0.;
-        const double xrr = hasRR ? v.XL[ax * NP + R + stride] : 0.0;
-        hp = 0.5 * (xrr - xp);
-      } else if (!hasRR) {
-        hp = 0.;
-        hm = 0.5 * (xp - v.XL[ax * NP + L - stride]);
-      } else {
-        hm = 0.5 * (xp - v.XL[ax * NP + L - stride]);
-        hp = 0.5 * (v.XL[ax * NP + R + stride] - xp);
+struct DualGrad {
+  int sweep;
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    const Ctrl& C = *v.ctrl;
+    if (i > v.ny || j > v.nx) return;
+    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+    const long long NP = v.npitch;
+    const long long p = (long long)i * (v.nx + 1) + j;
+    const double* D = (sweep == 1) ? v.u : v.DPv;  // DualPhi velocity
+    double g0 = 0.0, g1 = 0.0;
+    if (v.order > 1) {
+      const int ax = dirx ? 0 : 1;
+      const int pos = dirx ? j : i, lastpos = dirx ? v.nx : v.ny;
+      const long long stride = dirx ? 1 : (v.nx + 1);
+      if (pos != 0 && pos != lastpos) {
+        const long long L = p - stride, R = p + stride;
+        const double xp = v.XL[ax * NP + p], xr = v.XL[ax * NP + R],
+                     xl = v.XL[ax * NP + L];
+        double hm, hp;
+        const double h0 = 0.5 * (xr - xl);
+        const bool hasLL = (pos - 1 != 0), hasRR = (pos + 1 != lastpos);
+        if (!hasLL) {
+          hm = 0.;
+          const double xrr = hasRR ? v.XL[ax * NP + R + stride] : 0.0;
+          hp = 0.5 * (xrr - xp);
+        } else if (!hasRR) {
+          hp = 0.;
+          hm = 0.5 * (xp - v.XL[ax * NP + L - stride]);
+        } else {
+          hm = 0.5 * (xp - v.XL[ax * NP + L - stride]);
+          hp = 0.5 * (v.XL[ax * NP + R + stride] - xp);
+        }
+        double g[2];
+  #pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const double dp = D[k * NP + p], dr = D[k * NP + R], dl = D[k * NP + L];
+          const double gr = qdiv(dr - dp, xr - xp);
+          const double gl = qdiv(dp - dl, xp - xl);
+          g[k] = limit_grad1(v.limiter, gr, gl, dr, dl, h0, hp, hm);
+        }
+        g0 = g[0];
+        g1 = g[1];
       }
-      double g[2];
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const double dp = D[k * NP + p], dr = D[k * NP + R], dl = D[k * NP + L];
-        const double gr = qdiv(dr - dp, xr - xp);
-        const double gl = qdiv(dp - dl, xp - xl);
-        g[k] = limit_grad1(v.limiter, gr, gl, dr, dl, h0, hp, hm);
-      }
-      g0 = g[0];
-      g1 = g[1];
     }
+    v.gD[p] = g0;
+    v.gD[NP + p] = g1;
   }
-  v.gD[p] = g0;
-  v.gD[NP + p] = g1;
-}
+};
 
 // Nodal mass fluxes, upwind velocities and nodal momentum update
 // (Remap::computeDualUremap{1,2}, remap/DualPhaseRemap1.cc:33-135,
 // DualPhaseRemap2.cc:36-125; mass fluxes remap/UtilesDualRemap.cc A1
 // :10-233, A2 :401-644, PB :648-818; upwind velocities :234-397).
-__global__ void __launch_bounds__(kBX* kBY) k_dual_update(RunView v, int sweep) {
-  Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  const int j = blockIdx.x * kBX + threadIdx.x;
-  const int i = blockIdx.y * kBY + threadIdx.y;
-  if (i > v.ny || j > v.nx) return;
-  const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
-  const long long P = v.pitch, NP = v.npitch;
-  const long long p = (long long)i * (v.nx + 1) + j;
-  const int nb = v.nbmat;
-  const int ax = dirx ? 0 : 1;
-  // inner faces of the sweep through this node (Vertical/HorizontalFaceOfNode,
-  // remap/UtilesMesh.cc:53-108): for an x sweep the vertical faces below and
-  // above the node, for a y sweep the horizontal faces left and right of it.
-  // cplus[s] / cminus[s]: the cells right/above and left/below of face s.
-  long long cplus[2], cminus[2];
-  int nface = 0;
-  if (dirx) {
-    if (j >= 1 && j <= v.nx - 1) {
-      if (i >= 1) {
-        cminus[nface] = (long long)(i - 1) * v.nx + j - 1;
-        cplus[nface++] = (long long)(i - 1) * v.nx + j;
-      }
-      if (i <= v.ny - 1) {
-        cminus[nface] = (long long)i * v.nx + j - 1;
-        cplus[nface++] = (long long)i * v.nx + j;
-      }
-    }
-  } else {
-    if (i >= 1 && i <= v.ny - 1) {
-      if (j >= 1) {
-        cminus[nface] = (long long)(i - 1) * v.nx + j - 1;
-        cplus[nface++] = (long long)i * v.nx + j - 1;
-      }
-      if (j <= v.nx - 1) {
-        cminus[nface] = (long long)(i - 1) * v.nx + j;
-        cplus[nface++] = (long long)i * v.nx + j;
-      }
-    }
-  }
-  // outer-normal planes of the near / far faces: x: plus cell (left=near,
-  // right=far), minus cell (right=near, left=far); y: plus cell (bottom,
-  // top), minus cell (top, bottom).  Plane order of nout: L.x R.x B.y T.y.
-  const int pl_pn = dirx ? 0 : 2, pl_pf = dirx ? 1 : 3;
-  const int pl_mn = dirx ? 1 : 3, pl_mf = dirx ? 0 : 2;
-  double Fp = 0., Fm = 0.;
-  for (int m = 0; m < nb; ++m) {
-    double pp = 0., pm = 0.;
-    for (int s = 0; s < nface; ++s) {
-      const long long a = cplus[s], b = cminus[s];
-      if (v.dual_method == 2) {
-        pp += v.DPF[m * P + a];
-        pm += v.DPF[m * P + b];
-      } else {
-        // FFd planes: [0..nb) flux through the cell's minus face,
-        // [nb..2nb) through its plus face
-        double va = v.FFd[m * P + a] * ld(v.nout, pl_pn * P + a) +
-                    v.FFd[(nb + m) * P + a] * ld(v.nout, pl_pf * P + a);
-        double vb = v.FFd[(nb + m) * P + b] * ld(v.nout, pl_mn * P + b) +
-                    v.FFd[m * P + b] * ld(v.nout, pl_mf * P + b);
-        if (v.dual_method == 1) {
-          va = v.rL[a] * va;
-          vb = v.rL[b] * vb;
+struct DualUpdate {
+  int sweep;
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    Ctrl& C = *v.ctrl;
+    if (i > v.ny || j > v.nx) return;
+    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+    const long long P = v.pitch, NP = v.npitch;
+    const long long p = (long long)i * (v.nx + 1) + j;
+    const int nb = v.nbmat;
+    const int ax = dirx ? 0 : 1;
+    // inner faces of the sweep through this node (Vertical/HorizontalFaceOfNode,
+    // remap/UtilesMesh.cc:53-108): for an x sweep the vertical faces below and
+    // above the node, for a y sweep the horizontal faces left and right of it.
+    // cplus[s] / cminus[s]: the cells right/above and left/below of face s.
+    long long cplus[2], cminus[2];
+    int nface = 0;
+    if (dirx) {
+      if (j >= 1 && j <= v.nx - 1) {
+        if (i >= 1) {
+          cminus[nface] = (long long)(i - 1) * v.nx + j - 1;
+          cplus[nface++] = (long long)(i - 1) * v.nx + j;
         }
-        pp += va;
-        pm += vb;
+        if (i <= v.ny - 1) {
+          cminus[nface] = (long long)i * v.nx + j - 1;
+          cplus[nface++] = (long long)i * v.nx + j;
+        }
+      }
+    } else {
+      if (i >= 1 && i <= v.ny - 1) {
+        if (j >= 1) {
+          cminus[nface] = (long long)(i - 1) * v.nx + j - 1;
+          cplus[nface++] = (long long)i * v.nx + j - 1;
+        }
+        if (j <= v.nx - 1) {
+          cminus[nface] = (long long)(i - 1) * v.nx + j;
+          cplus[nface++] = (long long)i * v.nx + j;
+        }
       }
     }
-    if (v.dual_method == 2) {
-      if (nface != 0) {
-        pp = div_pow2(pp, nface);
-        pm = div_pow2(pm, nface);
+    // outer-normal planes of the near / far faces: x: plus cell (left=near,
+    // right=far), minus cell (right=near, left=far); y: plus cell (bottom,
+    // top), minus cell (top, bottom).  Plane order of nout: L.x R.x B.y T.y.
+    const int pl_pn = dirx ? 0 : 2, pl_pf = dirx ? 1 : 3;
+    const int pl_mn = dirx ? 1 : 3, pl_mf = dirx ? 0 : 2;
+    double Fp = 0., Fm = 0.;
+    for (int m = 0; m < nb; ++m) {
+      double pp = 0., pm = 0.;
+      for (int s = 0; s < nface; ++s) {
+        const long long a = cplus[s], b = cminus[s];
+        if (v.dual_method == 2) {
+          pp += v.DPF[m * P + a];
+          pm += v.DPF[m * P + b];
+        } else {
+          // FFd planes: [0..nb) flux through the cell's minus face,
+          // [nb..2nb) through its plus face
+          double va = v.FFd[m * P + a] * ld(v.nout, pl_pn * P + a) +
+                      v.FFd[(nb + m) * P + a] * ld(v.nout, pl_pf * P + a);
+          double vb = v.FFd[(nb + m) * P + b] * ld(v.nout, pl_mn * P + b) +
+                      v.FFd[m * P + b] * ld(v.nout, pl_mf * P + b);
+          if (v.dual_method == 1) {
+            va = v.rL[a] * va;
+            vb = v.rL[b] * vb;
+          }
+          pp += va;
+          pm += vb;
+        }
       }
-    } else if (nface != 0) {
-      pp = div_pow2(pp, 2 * nface);
-      pm = div_pow2(pm, 2 * nface);
+      if (v.dual_method == 2) {
+        if (nface != 0) {
+          pp = div_pow2(pp, nface);
+          pm = div_pow2(pm, nface);
+        }
+      } else if (nface != 0) {
+        pp = div_pow2(pp, 2 * nface);
+        pm = div_pow2(pm, 2 * nface);
+      }
+      Fp += pp;
+      Fm += pm;
     }
-    Fp += pp;
-    Fm += pm;
-  }
-  // previous nodal conserved values and DualPhi
-  const double* D = (sweep == 1) ? v.u : v.DPv;
-  double Ui0, Ui1, Ui2;
-  if (sweep == 1) {
-    const double m = v.node_mass[p];
-    Ui0 = m * v.u[p];
-    Ui1 = m * v.u[NP + p];
-    Ui2 = m;
-  } else {
-    Ui0 = v.UD1[p];
-    Ui1 = v.UD1[NP + p];
-    Ui2 = v.UD1[2 * NP + p];
-  }
-  const double Un2 = Ui2 + Fm - Fp;
-  const int pos = dirx ? j : i, lastpos = dirx ? v.nx : v.ny;
-  const long long stride = dirx ? 1 : (v.nx + 1);
-  const bool hasL = pos != 0, hasR = pos != lastpos;
-  const long long L = p - stride, R = p + stride;
-  const int order2 = v.order - 1;
-  const double dt = C.dt_n;
-  const double dp0 = D[p], dp1 = D[NP + p], xp = v.XL[ax * NP + p];
-  const double gp0 = v.gD[p], gp1 = v.gD[NP + p];
-  // minus side (left / bottom)
-  double um[2], up[2];
-  {
-    const double dn0 = hasL ? D[L] : 0.0, dn1 = hasL ? D[NP + L] : 0.0;
-    const double xn = hasL ? v.XL[ax * NP + L] : 0.0;
-    const double u = 0.5 * ((ax == 0 ? dn0 : dn1) + (ax == 0 ? dp0 : dp1));
-    const int sg = (u > 0) ? 1 : -1;
-    const double dx = xp - xn;
-    if (Fm > 0) {
-      const double g0 = hasL ? v.gD[L] : 0.0, g1 = hasL ? v.gD[NP + L] : 0.0;
-      um[0] = dn0 + order2 * (0.5 * g0 * (sg * dx - dt * u));
-      um[1] = dn1 + order2 * (0.5 * g1 * (sg * dx - dt * u));
+    // previous nodal conserved values and DualPhi
+    const double* D = (sweep == 1) ? v.u : v.DPv;
+    double Ui0, Ui1, Ui2;
+    if (sweep == 1) {
+      const double m = v.node_mass[p];
+      Ui0 = m * v.u[p];
+      Ui1 = m * v.u[NP + p];
+      Ui2 = m;
     } else {
-      um[0] = dp0 + order2 * (0.5 * gp0 * (sg * dx - dt * u));
-      um[1] = dp1 + order2 * (0.5 * gp1 * (sg * dx - dt * u));
+      Ui0 = v.UD1[p];
+      Ui1 = v.UD1[NP + p];
+      Ui2 = v.UD1[2 * NP + p];
     }
-  }
-  // plus side (right / top)
-  {
-    const double dn0 = hasR ? D[R] : 0.0, dn1 = hasR ? D[NP + R] : 0.0;
-    const double xn = hasR ? v.XL[ax * NP + R] : 0.0;
-    const double u = 0.5 * ((ax == 0 ? dp0 : dp1) + (ax == 0 ? dn0 : dn1));
-    const int sg = (u > 0) ? 1 : -1;
-    const double dx = xn - xp;
-    if (Fp < 0) {
-      const double g0 = hasR ? v.gD[R] : 0.0, g1 = hasR ? v.gD[NP + R] : 0.0;
-      up[0] = dn0 + order2 * (0.5 * g0 * (sg * dx - dt * u));
-      up[1] = dn1 + order2 * (0.5 * g1 * (sg * dx - dt * u));
+    const double Un2 = Ui2 + Fm - Fp;
+    const int pos = dirx ? j : i, lastpos = dirx ? v.nx : v.ny;
+    const long long stride = dirx ? 1 : (v.nx + 1);
+    const bool hasL = pos != 0, hasR = pos != lastpos;
+    const long long L = p - stride, R = p + stride;
+    const int order2 = v.order - 1;
+    const double dt = C.dt_n;
+    const double dp0 = D[p], dp1 = D[NP + p], xp = v.XL[ax * NP + p];
+    const double gp0 = v.gD[p], gp1 = v.gD[NP + p];
+    // minus side (left / bottom)
+    double um[2], up[2];
+    {
+      const double dn0 = hasL ? D[L] : 0.0, dn1 = hasL ? D[NP + L] : 0.0;
+      const double xn = hasL ? v.XL[ax * NP + L] : 0.0;
+      const double u = 0.5 * ((ax == 0 ? dn0 : dn1) + (ax == 0 ? dp0 : dp1));
+      const int sg = (u > 0) ? 1 : -1;
+      const double dx = xp - xn;
+      if (Fm > 0) {
+        const double g0 = hasL ? v.gD[L] : 0.0, g1 = hasL ? v.gD[NP + L] : 0.0;
+        um[0] = dn0 + order2 * (0.5 * g0 * (sg * dx - dt * u));
+        um[1] = dn1 + order2 * (0.5 * g1 * (sg * dx - dt * u));
+      } else {
+        um[0] = dp0 + order2 * (0.5 * gp0 * (sg * dx - dt * u));
+        um[1] = dp1 + order2 * (0.5 * gp1 * (sg * dx - dt * u));
+      }
+    }
+    // plus side (right / top)
+    {
+      const double dn0 = hasR ? D[R] : 0.0, dn1 = hasR ? D[NP + R] : 0.0;
+      const double xn = hasR ? v.XL[ax * NP + R] : 0.0;
+      const double u = 0.5 * ((ax == 0 ? dp0 : dp1) + (ax == 0 ? dn0 : dn1));
+      const int sg = (u > 0) ? 1 : -1;
+      const double dx = xn - xp;
+      if (Fp < 0) {
+        const double g0 = hasR ? v.gD[R] : 0.0, g1 = hasR ? v.gD[NP + R] : 0.0;
+        up[0] = dn0 + order2 * (0.5 * g0 * (sg * dx - dt * u));
+        up[1] = dn1 + order2 * (0.5 * g1 * (sg * dx - dt * u));
+      } else {
+        up[0] = dp0 + order2 * (0.5 * gp0 * (sg * dx - dt * u));
+        up[1] = dp1 + order2 * (0.5 * gp1 * (sg * dx - dt * u));
+      }
+    }
+    const double Un0 = Ui0 + Fm * um[0] - Fp * up[0];
+    const double Un1 = Ui1 + Fm * um[1] - Fp * up[1];
+    if (sweep == 1) {
+      v.UD1[p] = Un0;
+      v.UD1[NP + p] = Un1;
+      v.UD1[2 * NP + p] = Un2;
+      v.DPv[p] = Un0 / Un2;
+      v.DPv[NP + p] = Un1 / Un2;
     } else {
-      up[0] = dp0 + order2 * (0.5 * gp0 * (sg * dx - dt * u));
-      up[1] = dp1 + order2 * (0.5 * gp1 * (sg * dx - dt * u));
+      // remapVariables node part (vnr_remap/PhaseRemapFinal.cc:207-234)
+      const double ux = Un0 / Un2, uy = Un1 / Un2;
+      v.u[p] = ux;
+      v.u[NP + p] = uy;
+      v.speed[p] = sqrt(ux * ux + uy * uy);
     }
   }
-  const double Un0 = Ui0 + Fm * um[0] - Fp * up[0];
-  const double Un1 = Ui1 + Fm * um[1] - Fp * up[1];
-  if (sweep == 1) {
-    v.UD1[p] = Un0;
-    v.UD1[NP + p] = Un1;
-    v.UD1[2 * NP + p] = Un2;
-    v.DPv[p] = Un0 / Un2;
-    v.DPv[NP + p] = Un1 / Un2;
-  } else {
-    // remapVariables node part (vnr_remap/PhaseRemapFinal.cc:207-234)
-    const double ux = Un0 / Un2, uy = Un1 / Un2;
-    v.u[p] = ux;
-    v.u[NP + p] = uy;
-    v.speed[p] = sqrt(ux * ux + uy * uy);
-  }
-}
+};
 
 // ----------------------------------------------------------- remap final
 // Vnr::remapVariables cell part (vnr_remap/PhaseRemapFinal.cc:18-205), then
@@ -1101,8 +1120,8 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   // EOS after the remap
   double pm[3], cm[3];
   for (int m = 0; m < nb; m++) {
-    if (v.eos[m] == HYDRO_EOS_PERFECT_GAS) {
-      const double g = v.gamma[m];
+    if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
+      const double g = gamma_of(v, m);
       pm[m] = (g - 1.0) * rhom[m] * emo[m];
       cm[m] = sqrt(g * (g - 1.0) * emo[m]);
     } else {
@@ -1122,7 +1141,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     cc = sqrt(g0 * (g0 - 1.0) * e);
   }
   for (int m = 0; m < nb; m++)
-    if (v.eos[m] == HYDRO_EOS_VOID) e += mf[m] * emo[m];
+    if (eos_of(v, m) == HYDRO_EOS_VOID) e += mf[m] * emo[m];
   v.rho[c] = rho;
   v.e[c] = e;
   v.p[c] = p;
@@ -1143,15 +1162,14 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   if (p == p) pb = ord_bits(p) > pb ? ord_bits(p) : pb;
 }
 
-__global__ void __launch_bounds__(kBX* kBY) k_final(RunView v) {
-  Ctrl& C = *v.ctrl;
-  if (!C.active) return;
-  const int j = blockIdx.x * kBX + threadIdx.x;
-  const int i = blockIdx.y * kBY + threadIdx.y;
-  unsigned long long dtb = ~0ull, pb = 0ull;
-  if (i < v.ny && j < v.nx) final_cell(v, C, i, j, dtb, pb);
-  block_reduce_minmax(dtb, pb, &C);
-}
+struct Final {
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    Ctrl& C = *v.ctrl;
+    unsigned long long dtb = ~0ull, pb = 0ull;
+    if (i < v.ny && j < v.nx) final_cell(v, C, i, j, dtb, pb);
+    block_reduce_minmax(dtb, pb, &C);
+  }
+};
 
 // Initial reductions (dt candidate and max pressure of the initial state).
 __global__ void __launch_bounds__(kBX* kBY) k_init_reductions(RunView v) {
@@ -1193,6 +1211,79 @@ __global__ void k_node_speed(RunView v) {
   const long long p = (long long)i * (v.nx + 1) + j;
   const double ux = v.u[p], uy = v.u[v.npitch + p];
   v.speed[p] = sqrt(ux * ux + uy * uy);
+}
+
+
+// ---------------------------------------------------------------- wrappers
+// Plain launches: one run, a 2D grid of kBX x kBY thread tiles.
+template <class F>
+__device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
+  if (!v.ctrl->active) return;
+  f(v, blockIdx.y * kBY + threadIdx.y, blockIdx.x * kBX + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
+__global__ void __launch_bounds__(kBX* kBY) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
+__global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { plain_items(v, FaceGrad{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) { plain_items(v, SweepGrad{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFace{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdate{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_final(RunView v) { plain_items(v, Final{}); }
+
+// Batched launches: a persistent grid walks the tile table; every thread of
+// a block works on the same tile (the final phase's block reduction relies
+// on it).  The tile's run view is staged in shared memory by the whole block,
+// so its fields are read where they are used instead of being held in
+// registers for the whole tile.
+template <class F>
+__device__ __forceinline__ void batch_items(const BatchArgs& b, const F& f) {
+  __shared__ RunView sv;
+  constexpr int kWords = sizeof(RunView) / sizeof(unsigned long long);
+  static_assert(sizeof(RunView) % sizeof(unsigned long long) == 0, "RunView size");
+  const int n = *b.ntiles;
+  const int tx = threadIdx.x & ((1 << b.tw_log2) - 1);
+  const int ty = threadIdx.x >> b.tw_log2;
+  const int th = kBatchThreads >> b.tw_log2;
+  for (int t = blockIdx.x; t < n; t += gridDim.x) {
+    const Tile T = b.tiles[t];
+    const unsigned long long* src =
+        reinterpret_cast<const unsigned long long*>(b.views + T.inst);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sv);
+    for (int k = threadIdx.x; k < kWords; k += blockDim.x) dst[k] = src[k];
+    __syncthreads();
+    if (sv.ctrl->active)
+      for (int r = 0; r < b.rows; ++r) f(sv, T.i0 + ty + r * th, T.j0 + tx);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kBatchThreads) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFace{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdate{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_final(BatchArgs b) { batch_items(b, Final{}); }
+
+// One thread per run: cycle start (begin + reduction reset) and cycle end.
+__global__ void kb_begin(const RunView* views, const int* ninst) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= *ninst) return;
+  const RunView v = views[r];
+  begin_at(v);
+  reset_at(v);
+}
+
+__global__ void kb_end(const RunView* views, const int* ninst, int* done) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= *ninst) return;
+  const RunView v = views[r];
+  end_at(v);
+  done[r] = v.ctrl->done;
 }
 
 }  // namespace
@@ -1250,6 +1341,60 @@ int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook) {
   H(10); k_end<<<1, 1, 0, s>>>(v); ++nk;
   H(-1);
   return nk;
+}
+
+
+// Kernels of the batched cycle in launch order (same kind ids as above; the
+// batched cycle start covers kinds 0 and 1).
+int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
+                       const LaunchHook* hook) {
+  int nk = 0;
+  auto H = [&](int kind) {
+    if (hook) (*hook)(kind);
+  };
+  auto args = [&](int ph, int sweep) {
+    const int on = phase_on_nodes(ph) ? 1 : 0, w = L.shape[ph];
+    return BatchArgs{L.views, L.tiles[on][w], L.ntiles[on][w],
+                     kTileShapes[w].tw_log2, kTileShapes[w].rows, sweep};
+  };
+  const int T = kBatchThreads;
+  const int rg = (L.max_inst + T - 1) / T;
+  H(0); kb_begin<<<rg, T, 0, s>>>(L.views, L.ninst); ++nk;
+  H(2); kb_lag_nodes<<<L.grid[kPhLagNodes], T, 0, s>>>(args(kPhLagNodes, 0)); ++nk;
+  H(3); kb_lag_cells<<<L.grid[kPhLagCells], T, 0, s>>>(args(kPhLagCells, 0)); ++nk;
+  for (int sweep = 1; sweep <= 2; ++sweep) {
+    if (L.any_order2) {
+      H(11); kb_face_grad<<<L.grid[kPhFaceGrad], T, 0, s>>>(args(kPhFaceGrad, sweep)); ++nk;
+      H(4); kb_sweep_grad<<<L.grid[kPhSweepGrad], T, 0, s>>>(args(kPhSweepGrad, sweep)); ++nk;
+    }
+    H(5); kb_sweep_face<<<L.grid[kPhSweepFace], T, 0, s>>>(args(kPhSweepFace, sweep)); ++nk;
+    H(6); kb_sweep_update<<<L.grid[kPhSweepUpdate], T, 0, s>>>(args(kPhSweepUpdate, sweep)); ++nk;
+    H(7); kb_dual_grad<<<L.grid[kPhDualGrad], T, 0, s>>>(args(kPhDualGrad, sweep)); ++nk;
+    H(8); kb_dual_update<<<L.grid[kPhDualUpdate], T, 0, s>>>(args(kPhDualUpdate, sweep)); ++nk;
+  }
+  H(9); kb_final<<<L.grid[kPhFinal], T, 0, s>>>(args(kPhFinal, 0)); ++nk;
+  H(10); kb_end<<<rg, T, 0, s>>>(L.views, L.ninst, L.done); ++nk;
+  H(-1);
+  return nk;
+}
+
+// Resident blocks per SM of each batched phase kernel at kBatchThreads
+// threads (for the persistent grid sizes).
+int batch_occupancy(int* blocks_per_sm) {
+  const void* fns[kNumPhases] = {
+      (const void*)kb_lag_nodes,   (const void*)kb_lag_cells,
+      (const void*)kb_face_grad,   (const void*)kb_sweep_grad,
+      (const void*)kb_sweep_face,  (const void*)kb_sweep_update,
+      (const void*)kb_dual_grad,   (const void*)kb_dual_update,
+      (const void*)kb_final};
+  for (int ph = 0; ph < kNumPhases; ++ph) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fns[ph], kBatchThreads, 0) !=
+        cudaSuccess)
+      return -1;
+    blocks_per_sm[ph] = n;
+  }
+  return 0;
 }
 
 }  // namespace hydro

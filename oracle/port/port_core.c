@@ -263,9 +263,16 @@ static int vnr_init_bc(port_run* R) {
   R->topV[0] = 1.0; R->topV[1] = 0.0;
   R->bottomV[0] = 1.0; R->bottomV[1] = 0.0;
   R->leftCellBC = R->rightCellBC = R->topCellBC = R->bottomCellBC = 0;
-  if (t == 4 || t == 15 || t == 5 || t == 16 || t == 1 || t == 12) {
-    /* Sod X/Y, BiSod X/Y; Sedov (VNR extension): symmetry walls */
+  if (t == 4 || t == 15 || t == 5 || t == 16) {
+    /* Sod X/Y, BiSod X/Y: symmetry walls */
     R->leftBC = R->rightBC = R->topBC = R->bottomBC = BC_SYM;
+  } else if (t == 1) {
+    /* Sedov (VNR extension): the Eucclhyd Sedov boundary conditions
+     * (eucclhyd_remap/Init.cc:47-64) */
+    R->leftBC = BC_SYM;
+    R->bottomBC = BC_SYM;
+    R->rightBC = BC_IMPOSED; R->rightV[0] = 0.0; R->rightV[1] = 0.0;
+    R->topBC = BC_IMPOSED; R->topV[0] = 0.0; R->topV[1] = 0.0;
   } else if (t == 7 || t == 18 || t == 9 || t == 20) {
     R->rightBC = BC_IMPOSED; R->rightV[0] = 1.0; R->rightV[1] = 0.0;
     R->rightCellBC = BC_PERIODIC;
@@ -336,6 +343,53 @@ static int vnr_init_state(port_run* R) {
       R->c_n0[c] = smin(R->cm_n0[NM * c], R->cm_n0[NM * c + 1]);
     }
     for (long p = 0; p < R->nn; ++p) R->u_n0[2 * p] = R->u_n0[2 * p + 1] = 0.0;
+  } else if (t == 1) {
+    /* Sedov (VNR extension after eucclhyd_remap/Init.cc:303-332): rho 1,
+     * p 1e-6, energy 0.244816 deposited in the cell touching the origin,
+     * written as its pressure; VNR Sod-style sound speed (Init.cc:139-142) */
+    const double e1 = 1.e-6 / ((R->s.gamma[0] - 1.0) * 1.0);
+    for (long c = 0; c < R->nc; ++c) {
+      int centre = 0;
+      const long i = c / R->nx, j = c - i * R->nx;
+      const long n0 = i * (R->nx + 1) + j;
+      const long nd[4] = {n0, n0 + 1, n0 + R->nx + 2, n0 + R->nx + 1};
+      for (int k = 0; k < 4; ++k)
+        if (norm2(R->X0[2 * nd[k]], R->X0[2 * nd[k] + 1]) < R->s.threshold) centre = 1;
+      const double e = centre ? e1 + 0.244816 / (R->s.dx * R->s.dy) : e1;
+      R->fm[NM * c] = 1.0;
+      R->mfm[NM * c] = 1.0;
+      R->rho_n0[c] = 1.0;
+      R->rhom_n0[NM * c] = 1.0;
+      R->p_n0[c] = (R->s.gamma[0] - 1.0) * 1.0 * e;
+      R->pm_n0[NM * c] = R->p_n0[c];
+      R->cm_n0[NM * c] = sqrt(g * R->rhom_n0[NM * c] / R->pm_n0[NM * c]);
+      R->c_n0[c] = R->cm_n0[NM * c];
+    }
+    for (long p = 0; p < R->nn; ++p) R->u_n0[2 * p] = R->u_n0[2 * p + 1] = 0.0;
+  } else if (t == 18 && R->s.init_variant == 2) {
+    /* advection step (extension): material 1, rho 1, left of x = 0.5;
+     * material 2, rho 0.1, right of it; uniform velocity (1, 0) */
+    for (long c = 0; c < R->nc; ++c) {
+      const double r = R->Xc0[2 * c];
+      const int m = (r < 0.5) ? 0 : 1;
+      const double d = (m == 0) ? 1.0 : 0.1;
+      R->fm[NM * c + m] = 1.0;
+      R->mfm[NM * c + m] = 1.0;
+      R->rho_n0[c] = d;
+      R->p_n0[c] = 0.0;
+      R->rhom_n0[NM * c + m] = d;
+      R->pm_n0[NM * c + m] = 0.0;
+      R->cm_n0[NM * c] = 1.0;
+      R->cm_n0[NM * c + 1] = 1.0;
+      R->c_n0[c] = smin(R->cm_n0[NM * c], R->cm_n0[NM * c + 1]);
+      R->em_n0[NM * c] = 1.0;
+      R->em_n0[NM * c + 1] = 1.0;
+      R->e_n0[c] = 1.0;
+    }
+    for (long p = 0; p < R->nn; ++p) {
+      R->u_n0[2 * p] = 1.0;
+      R->u_n0[2 * p + 1] = 0.0;
+    }
   } else if (t == 7 || t == 8 || t == 18 || t == 19 || t == 20 || t == 21) {
     /* (Bi)AdvectionX/Y, BiAdvectionVitX/Y */
     const int isx = (t == 7 || t == 18 || t == 20);

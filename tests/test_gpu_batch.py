@@ -1,0 +1,126 @@
+"""Batched execution (hydro_batch_step) against the plain path and the oracle.
+
+The batch changes only which thread computes which item, so every run of a
+batch must end bit-identical to the same run advanced alone, whatever the
+tile widths and grids the autotuner picks, and to the C restatement.
+"""
+from __future__ import annotations
+
+import pytest
+
+from conftest import (CELL_FIELDS, GOLDEN, NODE_FIELDS, assert_bitwise,
+                      get_field, golden_cases, load_golden)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def M():
+    import mahyco_gb300
+    from mahyco_gb300 import build
+    build.build()
+    return mahyco_gb300
+
+
+def small_mix(n, seed):
+    from mahyco_gb300.workloads import batch_mix
+    return batch_mix(n, seed=seed, cycles=40, nx_range=(16, 160), ny_range=(12, 72))
+
+
+def compare_runs(M, a, b, nbmat, tag):
+    for f in CELL_FIELDS + NODE_FIELDS + ["node_mass"]:
+        assert_bitwise(f"{tag}:{f}", get_field(a, f, nbmat), get_field(b, f, nbmat))
+    assert a.time() == b.time(), tag
+    assert a.error() == b.error(), tag
+
+
+def test_batch_matches_plain_mixed_kinds(M):
+    """A seeded mix of Sod, Sedov and advection runs of uneven sizes, run for
+    40 cycles in one batch (the first cycles tune the launches) and one by
+    one through the plain path."""
+    ctx = M.Context(0)
+    mix = small_mix(24, seed=11)
+    specs = [inst.spec(M) for inst in mix]
+    batched = [M.Run(s, ctx) for s in specs]
+    batch = M.Batch(batched)
+    left = batch.step(40)
+    assert left == 0  # every run stops at its 40-cycle cap
+    cfg = batch.config()
+    assert cfg["tuned"]
+    for inst, s, rb in zip(mix, specs, batched):
+        alone = M.Run(s, ctx)
+        alone.simulate()
+        compare_runs(M, rb, alone, s.nbmat, f"{inst.kind}{inst.nx}x{inst.ny}")
+        assert rb.time()[2] == 40
+
+
+def test_batch_matches_oracle(M, port_lib):
+    from oracle.port import PortRun
+    ctx = M.Context(0)
+    mix = small_mix(6, seed=5)
+    specs = [inst.spec(M) for inst in mix]
+    runs = [M.Run(s, ctx) for s in specs]
+    M.Batch(runs).step(40)
+    for inst, s, r in zip(mix, specs, runs):
+        ref = PortRun(s)
+        ref.step(40)
+        for f in ["density", "pressure", "energy", "pseudo", "fracvol_env",
+                  "density_env", "node_velocity"]:
+            want = ref.fetch(f)
+            if f.endswith("_env"):
+                want = want.reshape(-1, 3)[:, :s.nbmat]
+            assert_bitwise(f"{inst.kind}:{f}", get_field(r, f, s.nbmat), want)
+        assert r.time() == ref.time()
+
+
+def test_batch_of_reference_decks(M):
+    """Every golden deck (orders 1-3, PenteBorne pure / complet, A1 / A2 / PB
+    dual fluxes, one to two materials, advection and Sod) in one batch: runs
+    end at their own final times and match the reference's final state."""
+    ctx = M.Context(0)
+    cases = golden_cases()
+    loaded = [load_golden(GOLDEN / f"{c}.npz") for c in cases]
+    runs = [M.Run(spec, ctx) for spec, _, _ in loaded]
+    batch = M.Batch(runs)
+    while batch.step(256):
+        pass
+    for c, (spec, meta, want), r in zip(cases, loaded, runs):
+        t, dt, n = r.time()
+        assert n == int(meta["cycles"]), c
+        assert t == float(meta["t"]), c
+        for f in CELL_FIELDS + NODE_FIELDS + ["node_mass"]:
+            assert_bitwise(f"{c}:{f}", get_field(r, f, spec.nbmat), want[f])
+
+
+def test_batch_membership_change(M):
+    """The same context batches different run lists one after another; a
+    run can leave a batch and continue alone."""
+    ctx = M.Context(0)
+    mix = small_mix(9, seed=3)
+    specs = [inst.spec(M) for inst in mix]
+    runs = [M.Run(s, ctx) for s in specs]
+    ref = [M.Run(s, ctx) for s in specs]
+    M.Batch(runs).step(10)
+    M.Batch(runs[:5]).step(7)          # smaller list: same device block
+    runs[5].step(7)                    # the others continue alone
+    M.Batch(runs[6:]).step(7)
+    M.Batch(list(reversed(runs))).step(23)
+    for r in ref:
+        r.step(40)
+    for s, a, b in zip(specs, runs, ref):
+        compare_runs(M, a, b, s.nbmat, f"{s.nx}x{s.ny}")
+
+
+def test_batch_untuned_matches_tuned(M):
+    ctx = M.Context(0)
+    M.set_batch_tuning(ctx, False)
+    mix = small_mix(8, seed=17)
+    specs = [inst.spec(M) for inst in mix]
+    a = [M.Run(s, ctx) for s in specs]
+    M.Batch(a).step(40)
+    assert not M.Batch(a).config()["tuned"]
+    ctx2 = M.Context(0)
+    b = [M.Run(s, ctx2) for s in specs]
+    M.Batch(b).step(40)
+    for s, x, y in zip(specs, a, b):
+        compare_runs(M, x, y, s.nbmat, f"{s.nx}x{s.ny}")
