@@ -243,6 +243,9 @@ int get_plan(hydro_ctx* ctx, hydro_run* const* runs, int n, BatchPlan** out) {
       delete p;
       return fail(-3, "batch: occupancy query failed");
     }
+    // defaults until (or without) tuning: the narrowest tile shape, one
+    // block per tile
+    for (int ph = 0; ph < kNumPhases; ++ph) p->mode[ph] = 1;
     if (!ctx->batch_tuning) p->tune_next = kNumCandidates + 1;
     ctx->plan = p;
   }
@@ -476,8 +479,8 @@ int hydro_batch_config(hydro_ctx* ctx, int* width, int* height, int* grid,
   return p->tuned;
 }
 
-// Turns the batch autotuner on (default) or off (fixed 32-wide tiles,
-// persistent grids) for plans created afterwards.
+// Turns the batch autotuner on (default) or off (32 x 4 tiles, one block
+// per tile) for plans created afterwards.
 int hydro_batch_set_tuning(hydro_ctx* ctx, int enable) {
   if (!ctx) return fail(-1, "hydro_batch_set_tuning: null context");
   ctx->batch_tuning = enable ? 1 : 0;

@@ -13,25 +13,87 @@
 
 namespace hydro {
 
-#define HD __device__ __forceinline__
+#define HD __host__ __device__ __forceinline__
 
-HD double smin(double a, double b) { return (b < a) ? b : a; }
-HD double smax(double a, double b) { return (a < b) ? b : a; }
+// ---------------------------------------------------------------------------
+// Comparisons on the integer pipe.  On GB300 a double comparison or min/max
+// occupies the FP64 pipe like an addition (1/16 warp instruction per cycle
+// and SM), and the hot kernels are bound by that pipe; the integer pipe is
+// 32x wider.  Every helper below has exactly the IEEE semantics of the
+// comparison it names: false when an operand is NaN, -0 == +0.
+constexpr unsigned long long kMag = 0x7fffffffffffffffull;
+constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
+
+HD unsigned long long ubits(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long b;
+  __builtin_memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+HD double from_bits(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  __builtin_memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+HD bool is_nan(double x) { return (ubits(x) & kMag) > kInfBits; }
+HD bool is_finite(double x) { return (ubits(x) & kInfBits) != kInfBits; }
+// monotone signed key of a non-NaN double; both zeros map to 0
+HD long long dkey(double x) {
+  const unsigned long long b = ubits(x);
+  const long long m = (long long)(b & kMag);
+  return (b >> 63) ? -m : m;
+}
+HD bool dlt(double a, double b) { return !is_nan(a) && !is_nan(b) && dkey(a) < dkey(b); }
+HD bool dle(double a, double b) { return !is_nan(a) && !is_nan(b) && dkey(a) <= dkey(b); }
+HD bool dgt(double a, double b) { return dlt(b, a); }
+HD bool dge(double a, double b) { return dle(b, a); }
+// x > 0, x < 0, x >= 0, x <= 0
+HD bool pos(double x) { return (unsigned long long)((long long)ubits(x) - 1) < kInfBits; }
+HD bool neg(double x) {
+  const unsigned long long m = ubits(x) & kMag;
+  return (ubits(x) >> 63) && m != 0 && m <= kInfBits;
+}
+HD bool nonneg(double x) { return !is_nan(x) && !neg(x); }
+HD bool nonpos(double x) { return !is_nan(x) && !pos(x); }
+// x != 0 (true for NaN), x == 0
+HD bool nz(double x) { return (ubits(x) & kMag) != 0; }
+HD bool iszero(double x) { return (ubits(x) & kMag) == 0; }
+// |x| < c, |x| > c for a constant c >= 0 (c not NaN)
+HD bool abs_lt(double x, double c) { return (ubits(x) & kMag) < ubits(c); }
+HD bool abs_gt(double x, double c) {
+  const unsigned long long m = ubits(x) & kMag;
+  return m > ubits(c) && m <= kInfBits;
+}
+
+// std::min / std::max: min(a,b) = (b<a)?b:a, max(a,b) = (a<b)?b:a
+HD double smin(double a, double b) { return dlt(b, a) ? b : a; }
+HD double smax(double a, double b) { return dlt(a, b) ? b : a; }
 
 // Order-preserving 64-bit encoding of doubles (for atomicMin/atomicMax).
 HD unsigned long long ord_bits(double x) {
-  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  unsigned long long b = ubits(x);
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 HD double from_ord(unsigned long long o) {
   unsigned long long b = (o >> 63) ? (o & 0x7fffffffffffffffull) : ~o;
-  return __longlong_as_double((long long)b);
+  return from_bits(b);
 }
 
 // IEEE division behind a call: the optimizer cannot if-convert a branch
 // around it into an unconditional division, so divisions on paths that are
 // rarely taken cost nothing when they are not taken.
+#ifdef __CUDA_ARCH__
 static __device__ __noinline__ double ddiv_call(double n, double d) { return n / d; }
+#else
+static inline double ddiv_call(double n, double d) { return n / d; }
+#endif
 
 // n / d with the exact shortcuts decided on the integer pipe:
 //   n = +-0, d finite non-zero   -> zero with sign(n) xor sign(d)
@@ -40,12 +102,12 @@ static __device__ __noinline__ double ddiv_call(double n, double d) { return n /
 // (uniform and single-material cells produce many of these); otherwise the
 // IEEE division.  Bit-identical to n / d (NaN results stay NaN).
 HD double qdiv(double n, double d) {
-  const unsigned long long nb = (unsigned long long)__double_as_longlong(n);
-  const unsigned long long db = (unsigned long long)__double_as_longlong(d);
+  const unsigned long long nb = ubits(n);
+  const unsigned long long db = ubits(d);
   const bool dfin = ((db >> 52) & 0x7ffull) != 0x7ffull;
   const bool dnz = (db << 1) != 0ull;
   if ((nb << 1) == 0ull && dnz && dfin)
-    return __longlong_as_double((long long)((nb ^ db) & 0x8000000000000000ull));
+    return from_bits((nb ^ db) & 0x8000000000000000ull);
   if (db == 0x3ff0000000000000ull) return n;
   if (nb == db && dnz && dfin) return 1.0;
   return ddiv_call(n, d);
@@ -63,15 +125,45 @@ HD double flux_limiter(int id, double r) {
   if (id == HYDRO_LIM_SUPERBEE)
     return smax(0.0, smax(smin(2.0 * r, 1.0), smin(r, 2.0)));
   if (id == HYDRO_LIM_VANLEER) {
-    if (r <= 0.0) return 0.0;
+    if (nonpos(r)) return 0.0;
     return 2.0 * r / (1.0 + r);
   }
   return 0.0;
 }
 
+// 2 * x, exactly as the IEEE product, for a non-NaN x, on the integer pipe.
+HD double twice(double x) {
+  const unsigned long long b = ubits(x), m = b & kMag, e = m >> 52;
+  unsigned long long m2;
+  if (e == 0)
+    m2 = m << 1;                      // zero / subnormal: exact doubling
+  else if (e >= 0x7fe)
+    m2 = kInfBits;                    // overflow (or infinity)
+  else
+    m2 = m + (1ull << 52);            // exponent + 1
+  return from_bits((b & ~kMag) | m2);
+}
+
+// minmod / superBee limiter of a quotient that is not NaN, with the
+// comparisons on the integer pipe (same values as flux_limiter).
+HD double flux_limiter_q(int id, double r) {
+  const long long one = 0x3ff0000000000000ll, two = 0x4000000000000000ll;
+  // for non-NaN x: x < c  <=>  signed bits(x) < bits(c) when c > 0
+  const long long br = (long long)ubits(r);
+  if (id == HYDRO_LIM_MINMOD) {
+    const double t = (br < one) ? r : 1.0;          // smin(1.0, r)
+    return ((long long)ubits(t) > 0) ? t : 0.0;     // smax(0.0, t)
+  }
+  const double u = twice(r);
+  const double s1 = ((long long)ubits(u) > one) ? 1.0 : u;  // smin(2r, 1.0)
+  const double s2 = (br > two) ? 2.0 : r;                   // smin(r, 2.0)
+  const double w = (dkey(s1) < dkey(s2)) ? s2 : s1;        // smax(s1, s2)
+  return ((long long)ubits(w) > 0) ? w : 0.0;              // smax(0.0, w)
+}
+
 // divideNoExcept (includes/Freefunctions.h:86-92)
 HD double divide_no_except(double a, double b) {
-  if (fabs(b) < 1.0E-12) return 0.0;
+  if (abs_lt(b, 1.0E-12)) return 0.0;
   return qdiv(a, b);
 }
 
@@ -79,29 +171,29 @@ HD double divide_no_except(double a, double b) {
 HD double flux_limiter_pp(int id, double gp, double gm, double yp, double ym,
                           double h0, double hp, double hm) {
   double grady = 0.0;
-  if (gp * gm < 0.0) return 0.;
+  if (neg(gp * gm)) return 0.;
   if (id == HYDRO_LIM_MINMODG) {
-    grady = ((yp - ym) > 0.) ? smin(fabs(gp), fabs(gm)) : -smin(fabs(gp), fabs(gm));
+    grady = pos(yp - ym) ? smin(fabs(gp), fabs(gm)) : -smin(fabs(gp), fabs(gm));
   } else if (id == HYDRO_LIM_SUPERBEEG) {
-    grady = ((yp - ym) > 0.) ? smax(fabs(gp), fabs(gm)) : -smax(fabs(gp), fabs(gm));
+    grady = pos(yp - ym) ? smax(fabs(gp), fabs(gm)) : -smax(fabs(gp), fabs(gm));
   } else if (id == HYDRO_LIM_VANLEERG) {
-    double lp = (h0 / 2. + hp) / (h0 + hp + hm);
-    double lm = (h0 / 2. + hm) / (h0 + hp + hm);
-    if ((lp * gp + lm * gm) != 0.)
+    double lp = (h0 * 0.5 + hp) / (h0 + hp + hm);
+    double lm = (h0 * 0.5 + hm) / (h0 + hp + hm);
+    if (nz(lp * gp + lm * gm))
       grady = gp * gm / (lp * gp + lm * gm);
     else
       grady = 0.;
   } else if (id == HYDRO_LIM_ULTRABEEG) {
     grady = (yp - ym) / h0;
   } else if (id == HYDRO_LIM_ARITHMETICG) {
-    double lp = (h0 / 2. + hp) / (h0 + hp + hm);
-    double lm = (h0 / 2. + hm) / (h0 + hp + hm);
+    double lp = (h0 * 0.5 + hp) / (h0 + hp + hm);
+    double lm = (h0 * 0.5 + hm) / (h0 + hp + hm);
     grady = lm * gp + lp * gm;
   }
   double gMp = gp * (h0 + hp) / h0;
   double gMm = gm * (h0 + hm) / h0;
   double gM = smin(fabs(gMp), fabs(gMm));
-  if ((yp - ym) > 0.)
+  if (pos(yp - ym))
     grady = smin(fabs(gM), fabs(grady));
   else
     grady = -smin(fabs(gM), fabs(grady));
@@ -122,47 +214,66 @@ HD double flux_limiter_pp(int id, double gp, double gm, double yp, double ym,
 HD double limit_grad1(int id, double gp, double gm, double yp, double ym,
                       double h0, double hp, double hm) {
   if (id >= HYDRO_LIM_MINMODG) return flux_limiter_pp(id, gp, gm, yp, ym, h0, hp, hm);
-  const double a = fabs(gp), b = fabs(gm);
-  if ((id == HYDRO_LIM_MINMOD || id == HYDRO_LIM_SUPERBEE) && isfinite(gp) &&
-      isfinite(gm)) {
-    double f1, f2;  // phi(r1), phi(r2)
-    if (b < 1.0E-12) {
-      f1 = 0.0;
-      f2 = flux_limiter(id, divide_no_except(gm, gp));
-    } else if (a < 1.0E-12) {
-      f2 = 0.0;
-      f1 = flux_limiter(id, qdiv(gp, gm));
-    } else if ((gp < 0.0) != (gm < 0.0)) {
-      f1 = 0.0;  // r1, r2 < 0 (or -0 after underflow)
-      f2 = 0.0;
+  if ((id == HYDRO_LIM_MINMOD || id == HYDRO_LIM_SUPERBEE) && is_finite(gp) &&
+      is_finite(gm)) {
+    // every case needs at most one quotient: q = gp / gm gives phi(r1)
+    // (which = 1), q = gm / gp gives phi(r2) (which = 2); the other phi is
+    // a constant.  One division call site for the whole warp.
+    const unsigned long long ma = ubits(gp) & kMag, mb = ubits(gm) & kMag;
+    const unsigned long long eps = 0x3d719799812dea11ull;  // bits of 1.0E-12
+    int which;
+    double c1, c2;  // the constant phi(r1) / phi(r2) of the case
+    bool zero_q = false;
+    if (mb < eps) {  // b < 1e-12: phi(r1) = 0, r2 = divideNoExcept(gm, gp)
+      which = 2;
+      c1 = 0.0;
+      c2 = 0.0;
+      zero_q = ma < eps;
+    } else if (ma < eps) {  // a < 1e-12: phi(r2) = 0
+      which = 1;
+      c1 = 0.0;
+      c2 = 0.0;
+    } else if ((ubits(gp) ^ ubits(gm)) >> 63) {  // opposite signs (non-zero)
+      which = 0;
+      c1 = 0.0;
+      c2 = 0.0;
     } else if (id == HYDRO_LIM_MINMOD) {
-      if (a <= b) {
-        f1 = flux_limiter(id, qdiv(gp, gm));
-        f2 = 1.0;  // r2 >= 1
-      } else {
-        f1 = 1.0;  // r1 >= 1
-        f2 = flux_limiter(id, qdiv(gm, gp));
-      }
+      which = (ma <= mb) ? 1 : 2;  // the other ratio is >= 1: phi = 1
+      c1 = 1.0;
+      c2 = 1.0;
     } else {  // superBee: 2r on [0,1/2], 1 on [1/2,1], r on [1,2], 2 above
-      if (a <= 0.5 * b) {
-        f1 = flux_limiter(id, qdiv(gp, gm));
-        f2 = 2.0;  // r2 >= 2
-      } else if (a <= b) {
-        f1 = 1.0;  // r1 in [1/2, 1]
-        f2 = flux_limiter(id, qdiv(gm, gp));
-      } else if (a <= 2.0 * b) {
-        f1 = flux_limiter(id, qdiv(gp, gm));
-        f2 = 1.0;  // r2 in [1/2, 1]
+      // 0.5 * b and 2 * b exactly (b >= 1e-12 is normal)
+      const unsigned long long hb = mb - (1ull << 52);
+      const unsigned long long db = (mb >= 0x7fe0000000000000ull) ? kInfBits : mb + (1ull << 52);
+      if (ma <= hb) {
+        which = 1;
+        c2 = 2.0;  // r2 >= 2
+        c1 = 0.0;
+      } else if (ma <= mb) {
+        which = 2;
+        c1 = 1.0;  // r1 in [1/2, 1]
+        c2 = 0.0;
+      } else if (ma <= db) {
+        which = 1;
+        c2 = 1.0;  // r2 in [1/2, 1]
+        c1 = 0.0;
       } else {
-        f1 = 2.0;  // r1 >= 2
-        f2 = flux_limiter(id, qdiv(gm, gp));
+        which = 2;
+        c1 = 2.0;  // r1 >= 2
+        c2 = 0.0;
       }
     }
-    return (f1 * gm + f2 * gp) / 2.0;
+    const bool dodiv = which != 0 && !zero_q;
+    const double num = dodiv ? (which == 1 ? gp : gm) : 0.0;
+    const double den = dodiv ? (which == 1 ? gm : gp) : 1.0;
+    const double phi = flux_limiter_q(id, qdiv(num, den));
+    const double f1 = (which == 1) ? phi : c1;
+    const double f2 = (which == 2) ? phi : c2;
+    return (f1 * gm + f2 * gp) * 0.5;
   }
   return (flux_limiter(id, divide_no_except(gp, gm)) * gm +
-          flux_limiter(id, divide_no_except(gm, gp)) * gp) /
-         2.0;
+          flux_limiter(id, divide_no_except(gm, gp)) * gp) *
+         0.5;
 }
 
 // Remap::computeY0 (remap/UtilesRemap.cc:74-125): both thresholds at once.
@@ -188,8 +299,8 @@ HD void compute_y0(int id, double yp, double ym, double h0, double hp,
     y0p = smin(smax(xp, a), b);
     y0m = smin(smax(xm, a), b);
   } else if (id == HYDRO_LIM_ULTRABEEG) {
-    y0p = (yp + ym) / 2.;
-    y0m = (yp + ym) / 2.;
+    y0p = (yp + ym) * 0.5;
+    y0m = (yp + ym) * 0.5;
   } else if (id == HYDRO_LIM_ARITHMETICG) {
     y0p = ((h0 + hm + hp) * yp + h0 * ym) / (2 * h0 + hm + hp);
     y0m = ((h0 + hm + hp) * ym + h0 * yp) / (2 * h0 + hm + hp);
@@ -207,13 +318,13 @@ HD void compute_y0(int id, double yp, double ym, double h0, double hp,
 HD double int2y(double X, double x0, double y0, double x1, double y1) {
   double flux = 0.;
   const double d = x1 - x0;
-  if (fabs(d) > 1.e-14) {
+  if (abs_gt(d, 1.e-14)) {
     const double n = X - x0;
     double eta;
-    const bool fin = isfinite(n) && isfinite(d);
-    if (fin && (d > 0. ? n <= 0. : n >= 0.))
+    const bool fin = is_finite(n) && is_finite(d);
+    if (fin && (pos(d) ? nonpos(n) : nonneg(n)))
       eta = 0.;
-    else if (fin && (d > 0. ? n >= d : n <= d))
+    else if (fin && (pos(d) ? dge(n, d) : dle(n, d)))
       eta = 1.;
     else
       eta = smin(smax(0., ddiv_call(n, d)), 1.);
@@ -232,13 +343,13 @@ HD PPShape pp_shape(int lim, double thr, double y0, double yp, double ym,
   double y0p, y0m;
   compute_y0(lim, yp, ym, h0, hp, hm, y0p, y0m);
   double xp = 1., xm = 1.;
-  if (fabs(y0p - yp) > thr) xp = qdiv(y0 - yp, y0p - yp) - 1. / 2.;
-  if (fabs(y0m - ym) > thr) xm = qdiv(y0 - ym, y0m - ym) - 1. / 2.;
+  if (dgt(fabs(y0p - yp), thr)) xp = qdiv(y0 - yp, y0p - yp) - 0.5;
+  if (dgt(fabs(y0m - ym), thr)) xm = qdiv(y0 - ym, y0m - ym) - 0.5;
   PPShape s;
-  s.xd = +h0 * smin(smax(xp, -1. / 2.), 1. / 2.);
-  s.xg = -h0 * smin(smax(xm, -1. / 2.), 1. / 2.);
-  double xtd = y0 + h0 / 2 * grad;
-  double xtg = y0 - h0 / 2 * grad;
+  s.xd = +h0 * smin(smax(xp, -0.5), 0.5);
+  s.xg = -h0 * smin(smax(xm, -0.5), 0.5);
+  double xtd = y0 + h0 * 0.5 * grad;
+  double xtg = y0 - h0 * 0.5 * grad;
   double ad = smin(yp, 2. * y0m - ym);
   double bd = smax(yp, 2. * y0m - ym);
   double ag = smin(ym, 2. * y0p - yp);
@@ -253,14 +364,14 @@ HD PPShape pp_shape(int lim, double thr, double y0, double yp, double ym,
 // "formule 16" replacement at extrema.
 HD double pp_integral(const PPShape& s, double a, double b, double h0,
                       double y0, double yp, double ym, double ppv) {
-  double f1b = int2y(b, -h0 / 2., ym, s.xg, s.yg);
-  double f1a = int2y(a, -h0 / 2., ym, s.xg, s.yg);
+  double f1b = int2y(b, -h0 * 0.5, ym, s.xg, s.yg);
+  double f1a = int2y(a, -h0 * 0.5, ym, s.xg, s.yg);
   double f2b = int2y(b, s.xg, s.yg, s.xd, s.yd);
   double f2a = int2y(a, s.xg, s.yg, s.xd, s.yd);
-  double f3b = int2y(b, s.xd, s.yd, h0 / 2., yp);
-  double f3a = int2y(a, s.xd, s.yd, h0 / 2., yp);
+  double f3b = int2y(b, s.xd, s.yd, h0 * 0.5, yp);
+  double f3a = int2y(a, s.xd, s.yd, h0 * 0.5, yp);
   double F = smax(((f1b - f1a) + (f2b - f2a) + (f3b - f3a)), 0.);
-  if (((yp - y0) * (ym - y0)) >= 0.) F = y0 * ppv;
+  if (nonneg((yp - y0) * (ym - y0))) F = y0 * ppv;
   return F;
 }
 
@@ -297,7 +408,7 @@ HD double flux_ordre3(double ymmm, double ymm, double ym, double yp,
   double ym6 = 6. * (ym - 0.5 * (ystarm + ystar));
   double yp6 = 6. * (yp - 0.5 * (ystar + ystarp));
   double flux;
-  if (vdt >= 0.) {
+  if (nonneg(vdt)) {
     double x = vdt, dx = hm;
     flux = ystar - 0.5 * x / dx * (grad_m - (1. - 2. / 3. * x / dx) * ym6);
   } else {
@@ -308,7 +419,7 @@ HD double flux_ordre3(double ymmm, double ymm, double ym, double yp,
   double ym_ym = ym + (1. - num) / num * (ym - ymm);
   double yp_ym = yp - (1. + nup) / nup * (yp - ypp);
   double i1inf = smin(ym, yp), i1sup = smax(ym, yp), i2inf, i2sup;
-  if (vdt >= 0.) {
+  if (nonneg(vdt)) {
     i2inf = smin(ym, ym_ym);
     i2sup = smax(ym, ym_ym);
   } else {
@@ -316,15 +427,15 @@ HD double flux_ordre3(double ymmm, double ymm, double ym, double yp,
     i2sup = smax(yp, yp_ym);
   }
   double linf, lsup;
-  if ((i1sup < i2inf) || (i2sup < i1inf)) {
+  if (dlt(i1sup, i2inf) || dlt(i2sup, i1inf)) {
     linf = 0.;
     lsup = 0.;
   } else {
     linf = smax(i1inf, i2inf);
     lsup = smin(i1sup, i2sup);
   }
-  if (flux < linf) flux = linf;
-  if (flux > lsup) flux = lsup;
+  if (dlt(flux, linf)) flux = linf;
+  if (dgt(flux, lsup)) flux = lsup;
   return flux;
 }
 

@@ -29,15 +29,17 @@ namespace {
 
 constexpr int kBX = 32, kBY = 4;  // 2D cell / node tiles
 
-HD double ld(const double* p, long long i) { return __ldg(p + i); }
+#define DV __device__ __forceinline__
+
+DV double ld(const double* p, long long i) { return __ldg(p + i); }
 
 // Per-material options read by select rather than by a dynamic index, so a
 // RunView copied into registers (batched launches) is never spilled whole to
 // local memory.
-HD double gamma_of(const RunView& v, int m) {
+DV double gamma_of(const RunView& v, int m) {
   return m == 0 ? v.gamma[0] : (m == 1 ? v.gamma[1] : v.gamma[2]);
 }
-HD int eos_of(const RunView& v, int m) {
+DV int eos_of(const RunView& v, int m) {
   return m == 0 ? v.eos[0] : (m == 1 ? v.eos[1] : v.eos[2]);
 }
 
@@ -127,7 +129,7 @@ __device__ void block_reduce_minmax(unsigned long long dtv,
 
 // dt candidate of one cell (Vnr::computeDeltaT, VnrRemap.cc:26-46) with
 // projection: cfl*sqrt(sum V_pc) / (uc + c), uc = sum_p 0.25*|u_p|.
-HD double cell_dt(const RunView& v, long long c, int i, int j) {
+DV double cell_dt(const RunView& v, long long c, int i, int j) {
   const long long n0 = (long long)i * (v.nx + 1) + j;
   const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
   double uc = 0.0;
@@ -309,7 +311,7 @@ struct LagCells {
       mf[m] = v.mfm[m * P + c];
       const double rm = v.rhom[m * P + c];
       rhom_new[m] = rm;
-      if (f[m] > thr) rhom_new[m] = v.cmassm[m * P + c] / (f[m] * vol);
+      if (dgt(f[m], thr)) rhom_new[m] = v.cmassm[m * P + c] / (f[m] * vol);
       rho_new += f[m] * rhom_new[m];
     }
     double e_new, q_new;
@@ -318,15 +320,15 @@ struct LagCells {
       const double tau = 0.5 * (1.0 / rho_new + 1.0 / rho_old);
       const double divu_new = 1.0 / C.dt_np1 * (1.0 / rho_new - 1.0 / rho_old) / tau;
       const double c_old = v.c[c];
-      if (v.divu[c] < 0.0) {
+      if (neg(v.divu[c])) {
         const double s0 = ld(v.s0, c);
         q_new = 1.0 / tau *
                 (-0.5 * ld(v.sqs0, c) * c_old * divu_new +
-                 (v.gamma_scalar + 1) / 2.0 * s0 * divu_new * divu_new);
+                 (v.gamma_scalar + 1) * 0.5 * s0 * divu_new * divu_new);
       } else {
         q_new = 0.0;
       }
-      if (q_new > C.pmax_prev) q_new = C.pmax_prev;
+      if (dgt(q_new, C.pmax_prev)) q_new = C.pmax_prev;
       v.divu[c] = divu_new;
       // energies (updateEnergy) and EOS
       e_new = 0.;
@@ -340,16 +342,16 @@ struct LagCells {
         v.qm[m * P + c] = qm_new;
         const double rn = rhom_new[m], ro = v.rhom[m * P + c];
         em_new[m] = 0.;
-        if ((rn > thr) && (ro > thr)) {
+        if (dgt(rn, thr) && dgt(ro, thr)) {
           double pseudo = 0.;
-          if ((v.pseudo_centree == 1) && ((qm_new + qm_old) * (1.0 / rn - 1.0 / ro) > 0.))
+          if ((v.pseudo_centree == 1) && pos((qm_new + qm_old) * (1.0 / rn - 1.0 / ro)))
             pseudo = 0.5 * (qm_new + qm_old);
           if (v.pseudo_centree == 0) pseudo = qm_new;
           const double den = 1 + 0.5 * (gamma_of(v, m) - 1.0) * rn * (1.0 / rn - 1.0 / ro);
           const double num = v.em[m * P + c] - (0.5 * v.pm[m * P + c] + pseudo) * (1.0 / rn - 1.0 / ro);
           em_new[m] = num / den;
           e_new += mf[m] * em_new[m];
-          if (v.energy_limit > 0 && fabs(em_new[m]) > v.energy_limit) bad = true;
+          if (pos(v.energy_limit) && abs_gt(em_new[m], v.energy_limit)) bad = true;
         }
       }
       if (bad) {
@@ -374,7 +376,7 @@ struct LagCells {
       // computePressionMoyenne: the stale max argument is the in-place c
       double cc = c_old;
       for (int m = 0; m < nb; ++m) cc = smax(cc, cm_new[m]);
-      if (rho_new > 0.) {
+      if (pos(rho_new)) {
         const double g0 = v.gamma[0];
         cc = sqrt(g0 * (g0 - 1.0) * e_new);
       }
@@ -407,8 +409,8 @@ struct LagCells {
       for (int m = 0; m < nb; ++m) sv += U[m];
       for (int m = 0; m < nb; ++m) {
         v.Phi[m * P + c] = qdiv(U[m], sv);
-        v.Phi[(nb + m) * P + c] = (U[m] != 0.) ? qdiv(U[nb + m], U[m]) : 0.;
-        v.Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
+        v.Phi[(nb + m) * P + c] = nz(U[m]) ? qdiv(U[nb + m], U[m]) : 0.;
+        v.Phi[(2 * nb + m) * P + c] = nz(U[nb + m]) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
       }
       v.Phi[3 * nb * P + c] = q_new;
     } else {
@@ -452,10 +454,10 @@ struct LagCells {
 // Face normal velocity (PrepareRemap.cc:42-63): mean of the two nodes'
 // Lagrange velocities along the face normal; "+ 0.0" is the dot product's
 // zero start for the other axis.
-HD double fnv_vertical(const RunView& v, long long na, long long nb) {
+DV double fnv_vertical(const RunView& v, long long na, long long nb) {
   return 0.5 * (v.u[na] + v.u[nb]) + 0.0;
 }
-HD double fnv_horizontal(const RunView& v, long long na, long long nb) {
+DV double fnv_horizontal(const RunView& v, long long na, long long nb) {
   return 0.5 * (v.u[v.npitch + na] + v.u[v.npitch + nb]) + 0.0;
 }
 
@@ -583,7 +585,7 @@ struct SweepGrad {
         const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
         const bool dual_k = cfd && k >= nb && k < 2 * nb;
         double fa_, fb_, fd_;
-        if (((yp - y0) * (ym - y0)) >= 0.) {
+        if (nonneg((yp - y0) * (ym - y0))) {
           // "formule 16" (UtilesRemap-Impl.h:201-203): the reference replaces
           // every integral of this component by y0 * swept length, so the
           // reconstruction is not built
@@ -592,8 +594,8 @@ struct SweepGrad {
           fd_ = y0 * ppd;
         } else {
           const PPShape sh = pp_shape(plim, v.threshold, y0, yp, ym, hh, hp, hm, grad[k]);
-          fa_ = (k < nint) ? pp_integral(sh, -hh / 2., -hh / 2. + ppa, hh, y0, yp, ym, ppa) : 0.;
-          fb_ = (k < nint) ? pp_integral(sh, hh / 2. - ppb, hh / 2., hh, y0, yp, ym, ppb) : 0.;
+          fa_ = (k < nint) ? pp_integral(sh, -hh * 0.5, -hh * 0.5 + ppa, hh, y0, yp, ym, ppa) : 0.;
+          fb_ = (k < nint) ? pp_integral(sh, hh * 0.5 - ppb, hh * 0.5, hh, y0, yp, ym, ppb) : 0.;
           fd_ = dual_k ? pp_integral(sh, 0., ppd, hh, y0, yp, ym, ppd) : 0.;
         }
         if (k < nint) {
@@ -602,7 +604,7 @@ struct SweepGrad {
         }
         if (dual_k) {
           double d = fd_;
-          if (ppd == 0.) d = 0.;
+          if (iszero(ppd)) d = 0.;
           v.DPF[(k - nb) * P + c] = d * flen;
         }
       }
@@ -611,7 +613,7 @@ struct SweepGrad {
         if (v.pb_complet == 1) {
           double sfm = 0., sfv = 0.;
           for (int m = 0; m < nb; m++) sfv += F[m];
-          if (fabs(sfv) > v.threshold) {
+          if (dgt(fabs(sfv), v.threshold)) {
             for (int m = 0; m < nb; m++) {
               if (!vp) F[nb + m] = (F[nb + m] / sfv) * F[m];
               F[2 * nb + m] = (F[2 * nb + m] / sfv) * F[nb + m];
@@ -630,7 +632,7 @@ struct SweepGrad {
           }
           F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
         }
-        for (int k = 0; k < ncomp; ++k) out[k * P] = (ppv == 0.) ? 0.0 : F[k];
+        for (int k = 0; k < ncomp; ++k) out[k * P] = iszero(ppv) ? 0.0 : F[k];
       };
       finish(Fr, ppa, v.dPAr + c);
       finish(Fv, ppb, v.dPAv + c);
@@ -672,7 +674,7 @@ struct SweepFace {
       if (v.pb == 0) {
         const double dxl = (v.XcL[ax * P + cf] - v.XcL[ax * P + cb]) + 0.0;
         const double xf = dirx ? ld(v.xs, j) : ld(v.ys, i);
-        const long long cu = (fnv * dxl > 0.0) ? cb : cf;
+        const long long cu = pos(fnv * dxl) ? cb : cf;
         const double s = (xf - v.XcL[ax * P + cu]) + 0.0;
         for (int k = 0; k < ncomp; ++k)
           out[k * FP] = v.Phi[k * P + cu] + s * v.gP[k * P + cu];
@@ -799,11 +801,11 @@ struct SweepUpdate {
         double sm = 0.;
         for (int m = 0; m < nb; m++) {
           Phi[m * P + c] = qdiv(U[m], sv);
-          Phi[(nb + m) * P + c] = (U[m] != 0.) ? qdiv(U[nb + m], U[m]) : 0.;
+          Phi[(nb + m) * P + c] = nz(U[m]) ? qdiv(U[nb + m], U[m]) : 0.;
           sm += U[nb + m];
         }
         for (int m = 0; m < nb; m++)
-          Phi[(2 * nb + m) * P + c] = (U[nb + m] != 0.) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
+          Phi[(2 * nb + m) * P + c] = nz(U[nb + m]) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
         (void)sm;
       } else {
         const double vl = v.vL[c];
@@ -811,7 +813,7 @@ struct SweepUpdate {
       }
       int matcell = 0, imatpure = -1;
       for (int m = 0; m < nb; m++)
-        if (Phi[m * P + c] > 0.) {
+        if (pos(Phi[m * P + c])) {
           matcell++;
           imatpure = m;
         }
@@ -843,15 +845,15 @@ struct DualGrad {
     double g0 = 0.0, g1 = 0.0;
     if (v.order > 1) {
       const int ax = dirx ? 0 : 1;
-      const int pos = dirx ? j : i, lastpos = dirx ? v.nx : v.ny;
+      const int at = dirx ? j : i, lastpos = dirx ? v.nx : v.ny;
       const long long stride = dirx ? 1 : (v.nx + 1);
-      if (pos != 0 && pos != lastpos) {
+      if (at != 0 && at != lastpos) {
         const long long L = p - stride, R = p + stride;
         const double xp = v.XL[ax * NP + p], xr = v.XL[ax * NP + R],
                      xl = v.XL[ax * NP + L];
         double hm, hp;
         const double h0 = 0.5 * (xr - xl);
-        const bool hasLL = (pos - 1 != 0), hasRR = (pos + 1 != lastpos);
+        const bool hasLL = (at - 1 != 0), hasRR = (at + 1 != lastpos);
         if (!hasLL) {
           hm = 0.;
           const double xrr = hasRR ? v.XL[ax * NP + R + stride] : 0.0;
@@ -977,9 +979,9 @@ struct DualUpdate {
       Ui2 = v.UD1[2 * NP + p];
     }
     const double Un2 = Ui2 + Fm - Fp;
-    const int pos = dirx ? j : i, lastpos = dirx ? v.nx : v.ny;
+    const int at = dirx ? j : i, lastpos = dirx ? v.nx : v.ny;
     const long long stride = dirx ? 1 : (v.nx + 1);
-    const bool hasL = pos != 0, hasR = pos != lastpos;
+    const bool hasL = at != 0, hasR = at != lastpos;
     const long long L = p - stride, R = p + stride;
     const int order2 = v.order - 1;
     const double dt = C.dt_n;
@@ -991,9 +993,9 @@ struct DualUpdate {
       const double dn0 = hasL ? D[L] : 0.0, dn1 = hasL ? D[NP + L] : 0.0;
       const double xn = hasL ? v.XL[ax * NP + L] : 0.0;
       const double u = 0.5 * ((ax == 0 ? dn0 : dn1) + (ax == 0 ? dp0 : dp1));
-      const int sg = (u > 0) ? 1 : -1;
+      const int sg = pos(u) ? 1 : -1;
       const double dx = xp - xn;
-      if (Fm > 0) {
+      if (pos(Fm)) {
         const double g0 = hasL ? v.gD[L] : 0.0, g1 = hasL ? v.gD[NP + L] : 0.0;
         um[0] = dn0 + order2 * (0.5 * g0 * (sg * dx - dt * u));
         um[1] = dn1 + order2 * (0.5 * g1 * (sg * dx - dt * u));
@@ -1007,9 +1009,9 @@ struct DualUpdate {
       const double dn0 = hasR ? D[R] : 0.0, dn1 = hasR ? D[NP + R] : 0.0;
       const double xn = hasR ? v.XL[ax * NP + R] : 0.0;
       const double u = 0.5 * ((ax == 0 ? dp0 : dp1) + (ax == 0 ? dn0 : dn1));
-      const int sg = (u > 0) ? 1 : -1;
+      const int sg = pos(u) ? 1 : -1;
       const double dx = xn - xp;
-      if (Fp < 0) {
+      if (neg(Fp)) {
         const double g0 = hasR ? v.gD[R] : 0.0, g1 = hasR ? v.gD[NP + R] : 0.0;
         up[0] = dn0 + order2 * (0.5 * g0 * (sg * dx - dt * u));
         up[1] = dn1 + order2 * (0.5 * g1 * (sg * dx - dt * u));
@@ -1064,13 +1066,13 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   double f[3], mf[3], sf = 0.;
   for (int m = 0; m < nb; m++) {
     f[m] = qdiv(vn[m], vnorm);
-    if (f[m] < thr) f[m] = 0.;
+    if (dlt(f[m], thr)) f[m] = 0.;
     sf += f[m];
   }
   for (int m = 0; m < nb; m++) f[m] = qdiv(f[m], sf);
   int matcell = 0, imatpure = -1;
   for (int m = 0; m < nb; m++)
-    if (f[m] > 0.) {
+    if (pos(f[m])) {
       matcell++;
       imatpure = m;
     }
@@ -1079,18 +1081,18 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   for (int m = 0; m < nb; m++) mf[m] = qdiv(U[(nb + m) * P], masset);
   double fmt = 0.;
   for (int m = 0; m < nb; m++) {
-    if (f[m] < thr) mf[m] = 0.;
+    if (dlt(f[m], thr)) mf[m] = 0.;
     fmt += mf[m];
   }
   for (int m = 0; m < nb; m++) mf[m] = qdiv(mf[m], fmt);
   double dm[3] = {0., 0., 0.}, dens = 0.;
   for (int m = 0; m < nb; m++) {
-    if (f[m] > thr) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
+    if (dgt(f[m], thr)) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
     dens += f[m] * dm[m];
   }
   double em[3] = {0., 0., 0.};
   for (int m = 0; m < nb; m++)
-    if ((f[m] > thr) && (U[(nb + m) * P] != 0.))
+    if (dgt(f[m], thr) && nz(U[(nb + m) * P]))
       em[m] = qdiv(U[(2 * nb + m) * P], U[(nb + m) * P]);
   const double rho = dens;
   double e = 0.;
@@ -1105,7 +1107,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     emo[m] = em[m];
   }
   for (int m = 0; m < nb; m++) {
-    if (em[m] < 0. || dm[m] < 0.) {
+    if (neg(em[m]) || neg(dm[m])) {
       rhom[m] = 0.;
       emo[m] = 0.;
       mf[m] = 0.;
@@ -1113,7 +1115,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
       atomicOr(&C.err, HYDRO_ERR_NEGATIVE);
     }
   }
-  if (e != e || rho != rho) {
+  if (is_nan(e) || is_nan(rho)) {
     atomicOr(&C.err, HYDRO_ERR_NAN);
     atomicMin((unsigned long long*)&C.err_cell, (unsigned long long)c);
   }
@@ -1136,7 +1138,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     p += f[m] * pm[m];
     cc = smax(cc, cm[m]);
   }
-  if (rho > 0.) {
+  if (pos(rho)) {
     const double g0 = v.gamma[0];
     cc = sqrt(g0 * (g0 - 1.0) * e);
   }
@@ -1157,9 +1159,9 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   // reductions feeding the next cycle
   if (v.sans_lagrange == 0) {
     const double d = cell_dt(v, c, i, j);
-    if (d == d) dtb = ord_bits(d) < dtb ? ord_bits(d) : dtb;
+    if (!is_nan(d)) dtb = ord_bits(d) < dtb ? ord_bits(d) : dtb;
   }
-  if (p == p) pb = ord_bits(p) > pb ? ord_bits(p) : pb;
+  if (!is_nan(p)) pb = ord_bits(p) > pb ? ord_bits(p) : pb;
 }
 
 struct Final {
@@ -1181,10 +1183,10 @@ __global__ void __launch_bounds__(kBX* kBY) k_init_reductions(RunView v) {
     const long long c = (long long)i * v.nx + j;
     if (v.sans_lagrange == 0) {
       const double d = cell_dt(v, c, i, j);
-      if (d == d) dtb = ord_bits(d);
+      if (!is_nan(d)) dtb = ord_bits(d);
     }
     const double p = v.p[c];
-    if (p == p) pb = ord_bits(p);
+    if (!is_nan(p)) pb = ord_bits(p);
   }
   block_reduce_minmax(dtb, pb, &C);
 }

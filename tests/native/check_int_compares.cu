@@ -1,0 +1,111 @@
+// Host-side check of the integer-pipe comparison helpers and the one-division
+// limiter of scheme_math.cuh against the plain IEEE expressions they replace
+// (compiled by nvcc for the host, run on the CPU).  Exit status 0 = all equal.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "kernels/scheme_math.cuh"
+
+using namespace hydro;
+
+static double ref_smin(double a, double b) { return (b < a) ? b : a; }
+static double ref_smax(double a, double b) { return (a < b) ? b : a; }
+static double ref_flux_limiter(int id, double r) {
+  if (id == HYDRO_LIM_MINMOD) return ref_smax(0.0, ref_smin(1.0, r));
+  return ref_smax(0.0, ref_smax(ref_smin(2.0 * r, 1.0), ref_smin(r, 2.0)));
+}
+static double ref_dne(double a, double b) {
+  if (std::fabs(b) < 1.0E-12) return 0.0;
+  return a / b;
+}
+static double ref_limit(int id, double gp, double gm) {
+  return (ref_flux_limiter(id, ref_dne(gp, gm)) * gm +
+          ref_flux_limiter(id, ref_dne(gm, gp)) * gp) / 2.0;
+}
+static bool same(double a, double b) {
+  unsigned long long x, y;
+  memcpy(&x, &a, 8);
+  memcpy(&y, &b, 8);
+  if (std::isnan(a) && std::isnan(b)) return true;
+  return x == y;
+}
+
+int main() {
+  std::vector<double> v = {0.0, -0.0, 1.0, -1.0, 0.5, -0.5, 2.0, -2.0, 1e-12, -1e-12,
+                           std::nextafter(1e-12, 0.0), std::nextafter(1e-12, 1.0),
+                           4.9e-324, -4.9e-324, 2.2250738585072014e-308,
+                           -2.2250738585072014e-308, 1.7976931348623157e308,
+                           -1.7976931348623157e308, 8.98846567431158e307,
+                           INFINITY, -INFINITY, NAN, -NAN, 3.0, 1e-300, -7.5,
+                           std::nextafter(1.0, 0.0), std::nextafter(1.0, 2.0),
+                           std::nextafter(2.0, 0.0), std::nextafter(0.5, 1.0)};
+  std::mt19937_64 g(12345);
+  for (int i = 0; i < 2000; ++i) {
+    unsigned long long b = g();
+    double d;
+    memcpy(&d, &b, 8);
+    v.push_back(d);
+    v.push_back(std::ldexp((double)(g() % 1000) - 500.0, (int)(g() % 80) - 40));
+  }
+  long bad = 0, n = 0;
+  for (double a : v)
+    for (double b : v) {
+      ++n;
+      bad += dlt(a, b) != (a < b);
+      bad += dle(a, b) != (a <= b);
+      bad += dgt(a, b) != (a > b);
+      bad += dge(a, b) != (a >= b);
+      bad += !same(smin(a, b), ref_smin(a, b));
+      bad += !same(smax(a, b), ref_smax(a, b));
+    }
+  for (double a : v) {
+    bad += pos(a) != (a > 0.0);
+    bad += neg(a) != (a < 0.0);
+    bad += nonneg(a) != (a >= 0.0);
+    bad += nonpos(a) != (a <= 0.0);
+    bad += is_nan(a) != (bool)std::isnan(a);
+    bad += is_finite(a) != (bool)std::isfinite(a);
+    bad += abs_lt(a, 1e-12) != (std::fabs(a) < 1e-12);
+    bad += abs_gt(a, 1e-14) != (std::fabs(a) > 1e-14);
+    if (!std::isnan(a)) {
+      bad += !same(twice(a), 2.0 * a);
+      for (int id : {HYDRO_LIM_MINMOD, HYDRO_LIM_SUPERBEE})
+        bad += !same(flux_limiter_q(id, a), ref_flux_limiter(id, a));
+    }
+  }
+  // limiter on gradient pairs: specials, random, and ratios near breakpoints
+  std::vector<std::pair<double, double>> pairs;
+  for (double a : v)
+    for (double b : v) pairs.push_back({a, b});
+  for (int i = 0; i < 400000; ++i) {
+    double b = std::ldexp((double)(g() % 100000) + 1.0, (int)(g() % 60) - 50);
+    if (g() & 1) b = -b;
+    const double k[] = {0.5, 1.0, 2.0, 0.25, 4.0};
+    double r = k[g() % 5];
+    double a = b * r;
+    unsigned long long ab;
+    memcpy(&ab, &a, 8);
+    ab += (long long)(g() % 5) - 2;  // a few ulps around the breakpoint
+    memcpy(&a, &ab, 8);
+    if (g() & 1) a = -a;
+    pairs.push_back({a, b});
+  }
+  long lbad = 0;
+  for (auto& pr : pairs)
+    for (int id : {HYDRO_LIM_MINMOD, HYDRO_LIM_SUPERBEE}) {
+      const double got = limit_grad1(id, pr.first, pr.second, 0, 0, 1, 1, 1);
+      const double want = ref_limit(id, pr.first, pr.second);
+      if (!same(got, want)) {
+        if (lbad < 5)
+          printf("limit_grad1(%d, %.17g, %.17g) = %.17g, want %.17g\n", id, pr.first,
+                 pr.second, got, want);
+        ++lbad;
+      }
+    }
+  printf("compares: %ld value pairs, %ld mismatches; limiter: %zu pairs, %ld mismatches\n",
+         n, bad, pairs.size(), lbad);
+  return (bad || lbad) ? 1 : 0;
+}
