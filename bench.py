@@ -309,6 +309,67 @@ def bench_batch(M, ctx, args, local: int) -> dict:
     }
 
 
+SERVE_WORKLOAD = {
+    "workload": "Poisson request streams; each request one VNR run drawn like the "
+                "batch mix (Sod / Sedov / advection, order-2 remap, minmod or "
+                "superBee) with nx, ny log-uniform 32..2048, 1-3 materials, "
+                "50-500 cycles (std::mt19937_64 seed 7 + rate); admission against a "
+                "150 GB HBM budget, runs resident until they end",
+    "budget_bytes": 150 * 10**9,
+}
+
+
+def bench_serve(M, args, local: int) -> dict:
+    """Continuous batching under Poisson arrivals: per rate, n requests are
+    submitted at their arrival times; latency is submission -> retirement;
+    throughput is the cell-updates of all requests over first arrival ->
+    last retirement."""
+    from mahyco_gb300.workloads import request_stream
+    rates = [float(x) for x in args.serve_rates.split(",") if x]
+    out = []
+    for lam in rates:
+        reqs = request_stream(lam, args.serve_n)
+        ctx = M.Context(local)
+        srv = M.Server(ctx, budget=SERVE_WORKLOAD["budget_bytes"], tick_cycles=8,
+                       prep_threads=8)
+        lat = []
+        t0 = time.perf_counter()
+        with Clocks(local) as clk:
+            for r in reqs:
+                dt = r.arrival - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                srv.submit(r.inst.spec(M))
+                while (d := srv.poll(0.0)) is not None:
+                    lat.append(d)
+            while len(lat) < len(reqs):
+                d = srv.poll(5.0)
+                if d is not None:
+                    lat.append(d)
+                if time.perf_counter() - t0 > args.serve_timeout:
+                    break
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.stop(drain=False)
+        ctx.close()
+        ls = sorted(d.latency_s for d in lat)
+        work = sum(d.cells * d.cycles for d in lat)
+
+        def pct(q):
+            return ls[min(len(ls) - 1, int(q * len(ls)))] if ls else None
+        out.append({
+            "rate_req_s": lam, "requests": len(reqs), "completed": len(lat),
+            "failed": sum(1 for d in lat if d.status < 0),
+            "p50_latency_s": pct(0.50), "p99_latency_s": pct(0.99),
+            "cell_updates": work, "wall_s": wall,
+            "value": work / wall if wall > 0 else None, "unit": UNIT,
+            "peak_resident": st["peak_resident"], "peak_bytes": st["peak_bytes"],
+            "ticks": st["ticks"], "clocks": clk.summary(),
+        })
+    return {"rates": out, "config": SERVE_WORKLOAD,
+            "value": max((o["value"] or 0) for o in out) if out else None, "unit": UNIT}
+
+
 def run_ours(args) -> None:
     rank, world, local = dist_env()
     if world > 1:
@@ -394,6 +455,7 @@ def run_ours(args) -> None:
         cfg["mesh"] = [n, n]
         cfg["workload"] = cfg["workload"].replace("2048x2048", f"{n}x{n}")
     batched = None if args.no_batch else bench_batch(M, ctx, args, local)
+    served = None if args.no_serve else bench_serve(M, args, local)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
@@ -403,6 +465,7 @@ def run_ours(args) -> None:
         "gpu_launches": launches,
         "kernel_ms": {k: [round(v[0], 4), v[1]] for k, v in kinds.items()},
         "batched": batched,
+        "served": served,
     }
     print(json.dumps(line))
 
@@ -418,6 +481,10 @@ def main() -> None:
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-n", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=40)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-rates", default="50,200,1000,2000")
+    ap.add_argument("--serve-n", type=int, default=24)
+    ap.add_argument("--serve-timeout", type=float, default=120.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -162,6 +162,43 @@ int hydro_batch_config(hydro_ctx* ctx, int* width, int* height, int* grid,
 int hydro_batch_set_tuning(hydro_ctx* ctx, int enable);
 long long hydro_batch_kernel_launches(hydro_ctx* ctx);
 
+/* Serving (no counterpart in the reference): requests are hydro runs that
+ * arrive at any time; a worker thread of the context admits them in arrival
+ * order while the HBM budget (their arenas' bytes) and the slot limit allow,
+ * advances every resident run together in batched ticks, and retires each run
+ * at its own end.  Results equal the same run advanced alone. */
+typedef struct hydro_serve_done {
+  long req_id;
+  int status;        /* device error word; -1 when the run could not start */
+  double latency_s;  /* submission to retirement                          */
+  long cycles;       /* cycles the run did                                */
+  long cells;
+} hydro_serve_done;
+typedef struct hydro_serve_stats {
+  long submitted, admitted, completed, failed;
+  long resident, waiting, peak_resident;
+  long ticks, cycles;
+  size_t bytes_in_use, peak_bytes;
+  double cell_updates;  /* of completed runs                         */
+  double busy_s;        /* first admission to last retirement        */
+} hydro_serve_stats;
+/* budget_bytes 0: the context's budget (0 there: none); other arguments
+ * <= 0 keep the defaults (256 slots, ticks of up to 8 cycles, 4 host
+ * threads preparing initial states). */
+int hydro_serve_config(hydro_ctx* ctx, size_t budget_bytes, int max_resident,
+                       int tick_cycles, int prep_threads);
+/* keep = 1 holds the finished run for hydro_serve_result until
+ * hydro_serve_release; keep = 0 frees it at retirement. */
+int hydro_serve_submit(hydro_ctx* ctx, const hydro_spec* spec, int keep,
+                       long* req_id);
+/* 1: one completion popped into *out; 0: none within timeout_s. */
+int hydro_serve_poll(hydro_ctx* ctx, double timeout_s, hydro_serve_done* out);
+hydro_run* hydro_serve_result(hydro_ctx* ctx, long req_id);
+int hydro_serve_release(hydro_ctx* ctx, long req_id);
+int hydro_serve_stats_get(hydro_ctx* ctx, hydro_serve_stats* out);
+/* drain = 1 waits for every submitted request to finish. */
+int hydro_serve_stop(hydro_ctx* ctx, int drain);
+
 /* CFL time step of a VNR state held in caller device memory, allocating
  * nothing (no counterpart in the reference; it restates the reduction of
  * Vnr::computeDeltaT with the remap on).  For callers that may not call

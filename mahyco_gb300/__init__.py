@@ -63,6 +63,21 @@ class HydroSpec(C.Structure):
         return out
 
 
+class ServeDone(C.Structure):
+    """struct hydro_serve_done"""
+    _fields_ = [("req_id", C.c_long), ("status", C.c_int), ("latency_s", C.c_double),
+                ("cycles", C.c_long), ("cells", C.c_long)]
+
+
+class ServeStats(C.Structure):
+    """struct hydro_serve_stats"""
+    _fields_ = [("submitted", C.c_long), ("admitted", C.c_long), ("completed", C.c_long),
+                ("failed", C.c_long), ("resident", C.c_long), ("waiting", C.c_long),
+                ("peak_resident", C.c_long), ("ticks", C.c_long), ("cycles", C.c_long),
+                ("bytes_in_use", C.c_size_t), ("peak_bytes", C.c_size_t),
+                ("cell_updates", C.c_double), ("busy_s", C.c_double)]
+
+
 _lib = None
 
 
@@ -116,6 +131,14 @@ def lib() -> C.CDLL:
         L.hydro_batch_set_tuning.argtypes = [vp, i]
         L.hydro_batch_kernel_launches.argtypes = [vp]
         L.hydro_batch_kernel_launches.restype = C.c_longlong
+        L.hydro_serve_config.argtypes = [vp, sz, i, i, i]
+        L.hydro_serve_submit.argtypes = [vp, C.POINTER(HydroSpec), i, C.POINTER(C.c_long)]
+        L.hydro_serve_poll.argtypes = [vp, C.c_double, C.POINTER(ServeDone)]
+        L.hydro_serve_result.argtypes = [vp, C.c_long]
+        L.hydro_serve_result.restype = vp
+        L.hydro_serve_release.argtypes = [vp, C.c_long]
+        L.hydro_serve_stats_get.argtypes = [vp, C.POINTER(ServeStats)]
+        L.hydro_serve_stop.argtypes = [vp, i]
         _lib = L
     return _lib
 
@@ -187,14 +210,23 @@ class Run:
     def __init__(self, spec: HydroSpec, ctx: Context | None = None):
         self.ctx = ctx or default_context()
         self.spec = spec
+        self.owner = True
         self.h = C.c_void_p()
         _check(lib().hydro_run_create(self.ctx.h, C.byref(spec), C.byref(self.h)),
                "hydro_run_create")
 
+    @classmethod
+    def borrowed(cls, handle: int, spec: HydroSpec, ctx: Context) -> "Run":
+        """A view of a run owned by someone else (e.g. the serving loop)."""
+        r = cls.__new__(cls)
+        r.ctx, r.spec, r.owner = ctx, spec, False
+        r.h = C.c_void_p(handle)
+        return r
+
     def close(self):
-        if self.h:
+        if self.h and self.owner:
             lib().hydro_run_destroy(self.h)
-            self.h = C.c_void_p()
+        self.h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -326,3 +358,50 @@ class Batch:
 
 def set_batch_tuning(ctx: Context, enable: bool) -> None:
     _check(lib().hydro_batch_set_tuning(ctx.h, int(enable)), "hydro_batch_set_tuning")
+
+
+class Server:
+    """Continuous batching of hydro runs on one context (hydro_serve_*):
+    submit() returns at once; a worker thread admits requests against the
+    HBM budget, advances all resident runs in batched ticks and retires each
+    at its end; poll() returns completions with their latency."""
+
+    def __init__(self, ctx: Context | None = None, budget: int = 0, max_resident: int = 0,
+                 tick_cycles: int = 0, prep_threads: int = 0):
+        self.ctx = ctx or default_context()
+        self.specs: dict[int, HydroSpec] = {}
+        _check(lib().hydro_serve_config(self.ctx.h, budget, max_resident, tick_cycles,
+                                        prep_threads), "hydro_serve_config")
+
+    def submit(self, spec: HydroSpec, keep: bool = False) -> int:
+        rid = C.c_long()
+        _check(lib().hydro_serve_submit(self.ctx.h, C.byref(spec), int(keep), C.byref(rid)),
+               "hydro_serve_submit")
+        if keep:
+            self.specs[rid.value] = spec.copy()
+        return rid.value
+
+    def poll(self, timeout: float = 0.0) -> ServeDone | None:
+        d = ServeDone()
+        rc = lib().hydro_serve_poll(self.ctx.h, timeout, C.byref(d))
+        if rc < 0:
+            _check(rc, "hydro_serve_poll")
+        return d if rc == 1 else None
+
+    def result(self, req_id: int) -> Run:
+        h = lib().hydro_serve_result(self.ctx.h, req_id)
+        if not h:
+            raise KeyError(req_id)
+        return Run.borrowed(h, self.specs[req_id], self.ctx)
+
+    def release(self, req_id: int) -> None:
+        _check(lib().hydro_serve_release(self.ctx.h, req_id), "hydro_serve_release")
+        self.specs.pop(req_id, None)
+
+    def stats(self) -> dict:
+        st = ServeStats()
+        _check(lib().hydro_serve_stats_get(self.ctx.h, C.byref(st)), "hydro_serve_stats_get")
+        return {name: getattr(st, name) for name, _ in ServeStats._fields_}
+
+    def stop(self, drain: bool = True) -> None:
+        _check(lib().hydro_serve_stop(self.ctx.h, int(drain)), "hydro_serve_stop")

@@ -168,20 +168,20 @@ void hydro_ctx_destroy(hydro_ctx* c) {
   delete c;
 }
 
-int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out) {
-  if (!ctx || !spec || !out) return fail(-1, "hydro_run_create: null argument");
-  if (int rc = validate(*spec)) return rc;
-  CUDA_TRY(cudaSetDevice(ctx->device));
-  auto* r = new hydro_run();
-  r->ctx = ctx;
-  r->spec = *spec;
-  HostInit h;
-  if (int rc = build_initial_state(*spec, h)) {
-    delete r;
-    return rc;
-  }
-  r->dt_init = h.dt_init;
-  RunView& v = r->v;
+}  // extern "C"
+
+namespace hydro {
+
+// Host part of run creation: validation, initial state, sizes and options
+// of the device view (no CUDA call; safe on any thread).
+int prepare_run(const hydro_spec& spec_in, PreparedRun& pr) {
+  if (int rc = validate(spec_in)) return rc;
+  pr.spec = spec_in;
+  const hydro_spec* spec = &pr.spec;
+  if (int rc = build_initial_state(*spec, pr.h)) return rc;
+  const HostInit& h = pr.h;
+  RunView& v = pr.v;
+  v = RunView{};
   v.nx = spec->nx;
   v.ny = spec->ny;
   v.nc = h.nc;
@@ -233,19 +233,58 @@ int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out) {
     v.v_top[d] = h.v_top[d];
   }
   v.periodic_x = h.periodic_x;
+  pr.bytes = layout(v, nullptr);
+  return 0;
+}
 
-  const size_t bytes = layout(v, nullptr);
-  if (ctx->budget && ctx->used + bytes > ctx->budget) {
-    delete r;
-    return fail(-30, "HBM budget exceeded");
+// Bytes of a run's arena for spec (layout sizes only).
+size_t run_arena_bytes(const hydro_spec& spec) {
+  RunView v{};
+  const long long nc = (long long)spec.nx * spec.ny;
+  const long long nn = (long long)(spec.nx + 1) * (spec.ny + 1);
+  v.nx = spec.nx;
+  v.ny = spec.ny;
+  v.pitch = round_up(nc, 32);
+  v.npitch = round_up(nn, 32);
+  v.fpitch = round_up(std::max((long long)(spec.nx + 1) * spec.ny,
+                               (long long)spec.nx * (spec.ny + 1)),
+                      32);
+  v.nbmat = spec.nbmat;
+  v.ncomp = 3 * spec.nbmat + 1;
+  return layout(v, nullptr);
+}
+
+// Device part: allocates the run's arena, uploads the prepared state on the
+// context's stream and queues the prologue.  With wait, returns after the
+// upload has finished; without, the caller orders later work on the same
+// stream (the host copies are staged before this returns, so `pr` may be
+// released at once).
+int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait) {
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  const size_t bytes = pr.bytes;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->budget && ctx->used + bytes > ctx->budget)
+      return fail(-30, "HBM budget exceeded");
+    ctx->used += bytes;
   }
+  auto* r = new hydro_run();
+  r->ctx = ctx;
+  r->spec = pr.spec;
+  r->v = pr.v;
+  r->dt_init = pr.h.dt_init;
+  RunView& v = r->v;
+  const HostInit& h = pr.h;
   cudaError_t e = cudaMalloc(&r->arena, bytes);
   if (e != cudaSuccess) {
+    {
+      std::lock_guard<std::mutex> lk(ctx->mu);
+      ctx->used -= bytes;
+    }
     delete r;
     return fail(-31, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   }
   r->arena_bytes = bytes;
-  ctx->used += bytes;
   layout(v, (char*)r->arena);
   r->d_ctrl = v.ctrl;
   cudaStream_t s = ctx->stream;
@@ -257,7 +296,8 @@ int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out) {
                                      cudaMemcpyHostToDevice, s);
     if (ee != cudaSuccess) rc = fail(-32, cudaGetErrorString(ee));
   };
-  CUDA_TRY(cudaMemsetAsync(r->arena, 0, bytes, s));
+  if (cudaMemsetAsync(r->arena, 0, bytes, s) != cudaSuccess)
+    rc = fail(-32, "arena clear");
   const long long nc = h.nc, nn = h.nn, P = v.pitch, NP = v.npitch;
   const int nb = v.nbmat;
   rc = rc ? rc : upload(v.rho, P, h.rho, nc, 1, nc, s);
@@ -287,12 +327,12 @@ int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out) {
   cp(v.flh, h.flh);
   cp(v.rho0_left, h.rho0_left);
   cp(v.node_mass, h.node_mass);
-  if (!rc) {
-    CUDA_TRY(cudaMemcpyAsync(v.mixte, h.mixte.data(), nc * sizeof(int),
-                             cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(v.pure, h.pure.data(), nc * sizeof(int),
-                             cudaMemcpyHostToDevice, s));
-  }
+  if (!rc &&
+      (cudaMemcpyAsync(v.mixte, h.mixte.data(), nc * sizeof(int),
+                       cudaMemcpyHostToDevice, s) != cudaSuccess ||
+       cudaMemcpyAsync(v.pure, h.pure.data(), nc * sizeof(int),
+                       cudaMemcpyHostToDevice, s) != cudaSuccess))
+    rc = fail(-32, "flag upload");
   Ctrl c0{};
   c0.t_n = 0.0;
   c0.dt_n = h.dt_init;
@@ -305,23 +345,38 @@ int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out) {
   c0.dt_min_bits = 0xFFEFFFFFFFFFFFFFull;  // ordered encoding of +DBL_MAX
   c0.pmax_bits = 0x0010000000000000ull;    // ordered encoding of -DBL_MAX
   r->h_ctrl = c0;
-  if (!rc)
-    rc = cudaMemcpyAsync(r->d_ctrl, &c0, sizeof(Ctrl), cudaMemcpyHostToDevice,
-                         s) == cudaSuccess
-             ? 0
-             : fail(-33, "ctrl upload");
+  // the control block goes through the pageable path too (staged at once)
+  if (!rc && cudaMemcpyAsync(r->d_ctrl, &r->h_ctrl, sizeof(Ctrl),
+                             cudaMemcpyHostToDevice, s) != cudaSuccess)
+    rc = fail(-33, "ctrl upload");
   if (!rc) launch_prologue(v, s);
-  if (!rc && cudaStreamSynchronize(s) != cudaSuccess)
+  if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(-34, "prologue launch");
+  if (!rc && wait && cudaStreamSynchronize(s) != cudaSuccess)
     rc = fail(-34, std::string("initial upload: ") +
                        cudaGetErrorString(cudaGetLastError()));
   if (rc) {
+    cudaStreamSynchronize(s);
     cudaFree(r->arena);
-    ctx->used -= bytes;
+    {
+      std::lock_guard<std::mutex> lk(ctx->mu);
+      ctx->used -= bytes;
+    }
     delete r;
     return rc;
   }
   *out = r;
   return 0;
+}
+
+}  // namespace hydro
+
+extern "C" {
+
+int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out) {
+  if (!ctx || !spec || !out) return fail(-1, "hydro_run_create: null argument");
+  PreparedRun pr;
+  if (int rc = prepare_run(*spec, pr)) return rc;
+  return place_run(ctx, pr, out, true);
 }
 
 int hydro_run_destroy(hydro_run* r) {
@@ -330,7 +385,10 @@ int hydro_run_destroy(hydro_run* r) {
   plan_forget_run(r->ctx->plan, r);
   if (r->graph) cudaGraphExecDestroy(r->graph);
   if (r->arena) cudaFree(r->arena);
-  r->ctx->used -= r->arena_bytes;
+  {
+    std::lock_guard<std::mutex> lk(r->ctx->mu);
+    r->ctx->used -= r->arena_bytes;
+  }
   delete r;
   return 0;
 }

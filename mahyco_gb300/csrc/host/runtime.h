@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../internal.h"
+#include "init.h"
 
 namespace hydro {
 
@@ -27,6 +28,19 @@ int measure_fp64_peak(int device, double* tflops);
       return ::hydro::fail(-100, std::string(#expr) + ": " +                 \
                                      cudaGetErrorString(e_));                \
   } while (0)
+
+// A run whose initial state is built on the host but not yet placed on the
+// device (run creation split in two so that a serving loop can prepare runs
+// on worker threads while the GPU is busy).
+struct PreparedRun {
+  hydro_spec spec{};
+  HostInit h;
+  RunView v{};
+  size_t bytes = 0;
+};
+int prepare_run(const hydro_spec& spec, PreparedRun& out);
+int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait);
+size_t run_arena_bytes(const hydro_spec& spec);
 
 struct BatchPlan;
 struct ServeState;
