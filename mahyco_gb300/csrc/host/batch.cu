@@ -235,6 +235,8 @@ int get_plan(hydro_ctx* ctx, hydro_run* const* runs, int n, BatchPlan** out) {
   for (int r = 0; r < n; ++r) {
     if (!runs[r]) return fail(-1, "batch: null run");
     if (runs[r]->ctx != ctx) return fail(-2, "batch: run belongs to another context");
+    if (runs[r]->v.scheme != HYDRO_SCHEME_VNR)
+      return fail(-4, "batch: the batched form advances VNR runs");
   }
   if (!ctx->plan) {
     auto* p = new BatchPlan();

@@ -32,12 +32,24 @@ struct HostInit {
   // node state
   std::vector<double> u;             // 2 planes
   std::vector<double> node_mass;
+  // Eucclhyd: cell velocity, constant cell and corner geometry of the Euler
+  // mesh, per (cell, corner k = position of the node in the cell)
+  std::vector<double> uc;            // 2 planes
+  std::vector<double> xc;            // 2 planes: cell centroids
+  std::vector<double> perim, evol;   // cell perimeter, Euler volume
+  std::vector<double> lpc;           // 8 planes [2k + d]: l_pc n_pc
+  std::vector<double> cmat;          // 12 planes [3k + e]: corner matrix
+                                     // entries 00, 01 (= 10), 11
 };
 
 // Builds the initial state for spec (VNR test cases of vnr_remap/Init.cc and
 // the extensions selected by spec->init_variant).  Returns 0 or a negative
 // status with hydro_last_error() set.
 int build_initial_state(const hydro_spec& spec, HostInit& out);
+
+// Eucclhyd set-up (eucclhyd_remap/Init.cc, PhaseLagrange.cc:27-66) for the
+// Sod, bi-material Sod, triple-point and Sedov cases.
+int build_initial_state_euc(const hydro_spec& spec, HostInit& out);
 
 }  // namespace hydro
 #endif

@@ -88,10 +88,25 @@ size_t layout(RunView& v, char* base) {
   v.UD1 = a.take<double>(3 * NP);
   v.xs = a.take<double>(v.nx + 1);
   v.ys = a.take<double>(v.ny + 1);
-  v.cqs = a.take<double>(8 * P);
-  v.cflsq = a.take<double>(P);
-  v.s0 = a.take<double>(P);
-  v.sqs0 = a.take<double>(P);
+  if (v.scheme == HYDRO_SCHEME_EUCCLHYD) {
+    v.cqs = v.cflsq = v.s0 = v.sqs0 = nullptr;
+    v.uc = a.take<double>(2 * P);
+    v.vg = a.take<double>(4 * P);
+    v.Fs = a.take<double>(2 * nb * P);
+    v.pex = a.take<double>(4 * P);
+    v.uex = a.take<double>(8 * P);
+    v.peex = a.take<double>(4 * nb * P);
+    v.lpc = a.take<double>(8 * P);
+    v.cmat = a.take<double>(12 * P);
+    v.xcc = a.take<double>(2 * P);
+    v.perim = a.take<double>(P);
+    v.evol = a.take<double>(P);
+  } else {
+    v.cqs = a.take<double>(8 * P);
+    v.cflsq = a.take<double>(P);
+    v.s0 = a.take<double>(P);
+    v.sqs0 = a.take<double>(P);
+  }
   v.nout = a.take<double>(4 * P);
   v.flv = a.take<double>(v.ny);
   v.flh = a.take<double>(v.nx);
@@ -112,8 +127,8 @@ int upload(double* dst, long long ds, const std::vector<double>& src,
 }
 
 int validate(const hydro_spec& s) {
-  if (s.scheme != HYDRO_SCHEME_VNR)
-    return fail(-20, "the GPU path currently implements the VNR scheme");
+  if (s.scheme != HYDRO_SCHEME_VNR && s.scheme != HYDRO_SCHEME_EUCCLHYD)
+    return fail(-20, "unknown Lagrange scheme");
   if (s.projection != 1)
     return fail(-21, "the GPU path requires the remap (AvecProjection = oui)");
   if (s.nbmat < 1 || s.nbmat > 3) return fail(-22, "nbmat must be 1..3");
@@ -126,8 +141,11 @@ int validate(const hydro_spec& s) {
                        "the reference (others only print)");
   if (s.dual_mass_flux < 0 || s.dual_mass_flux > 2)
     return fail(-26, "dual mass-flux method must be A1, A2 or PB");
-  if (s.dual_mass_flux == 2 && !(s.pb == 1 && s.projection_order > 1))
+  if (s.scheme == HYDRO_SCHEME_VNR && s.dual_mass_flux == 2 &&
+      !(s.pb == 1 && s.projection_order > 1))
     return fail(-27, "the PB dual mass flux needs PenteBorne and order > 1");
+  if (s.scheme == HYDRO_SCHEME_EUCCLHYD && s.space_order != 1 && s.space_order != 2)
+    return fail(-28, "the Eucclhyd space order must be 1 or 2");
   return 0;
 }
 
@@ -178,7 +196,10 @@ int prepare_run(const hydro_spec& spec_in, PreparedRun& pr) {
   if (int rc = validate(spec_in)) return rc;
   pr.spec = spec_in;
   const hydro_spec* spec = &pr.spec;
-  if (int rc = build_initial_state(*spec, pr.h)) return rc;
+  const bool euc = spec->scheme == HYDRO_SCHEME_EUCCLHYD;
+  if (int rc = euc ? build_initial_state_euc(*spec, pr.h)
+                   : build_initial_state(*spec, pr.h))
+    return rc;
   const HostInit& h = pr.h;
   RunView& v = pr.v;
   v = RunView{};
@@ -192,11 +213,19 @@ int prepare_run(const hydro_spec& spec_in, PreparedRun& pr) {
                                (long long)spec->nx * (spec->ny + 1)),
                       32);
   v.nbmat = spec->nbmat;
-  v.ncomp = 3 * spec->nbmat + 1;
-  for (int k = 0; k < kMaxComp; ++k) v.comp_ref[k] = -1;
-  for (int k = 0; k < 3 * spec->nbmat; ++k) v.comp_ref[k] = k;
-  v.comp_ref[3 * spec->nbmat] = 3 * spec->nbmat + 3;
   v.scheme = spec->scheme;
+  for (int k = 0; k < kMaxComp; ++k) v.comp_ref[k] = -1;
+  if (euc) {
+    // volumes, masses, energies, momentum x / y (+ kinetic energy)
+    v.ncomp = 3 * spec->nbmat + 2 + (spec->projection_conservative == 1 ? 1 : 0);
+    for (int k = 0; k < v.ncomp; ++k) v.comp_ref[k] = k;
+  } else {
+    v.ncomp = 3 * spec->nbmat + 1;
+    for (int k = 0; k < 3 * spec->nbmat; ++k) v.comp_ref[k] = k;
+    v.comp_ref[3 * spec->nbmat] = 3 * spec->nbmat + 3;
+  }
+  v.space_order = spec->space_order;
+  v.euc_cfl = spec->cfl;
   v.order = spec->projection_order;
   v.pb = spec->pb;
   v.pb_mixte = spec->pb_mixte;
@@ -250,7 +279,10 @@ size_t run_arena_bytes(const hydro_spec& spec) {
                                (long long)spec.nx * (spec.ny + 1)),
                       32);
   v.nbmat = spec.nbmat;
-  v.ncomp = 3 * spec.nbmat + 1;
+  v.scheme = spec.scheme;
+  v.ncomp = spec.scheme == HYDRO_SCHEME_EUCCLHYD
+                ? 3 * spec.nbmat + 2 + (spec.projection_conservative == 1 ? 1 : 0)
+                : 3 * spec.nbmat + 1;
   return layout(v, nullptr);
 }
 
@@ -316,11 +348,20 @@ int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait) {
   rc = rc ? rc : upload(v.mfm, P, h.mfm, nc, nb, nc, s);
   rc = rc ? rc : upload(v.cmassm, P, h.cmassm, nc, nb, nc, s);
   rc = rc ? rc : upload(v.u, NP, h.u, nn, 2, nn, s);
-  rc = rc ? rc : upload(const_cast<double*>(v.cqs), P, h.cqs, nc, 8, nc, s);
   rc = rc ? rc : upload(const_cast<double*>(v.nout), P, h.nout, nc, 4, nc, s);
-  cp(v.cflsq, h.cflsq);
-  cp(v.s0, h.s0);
-  cp(v.sqs0, h.sqs0);
+  if (v.scheme == HYDRO_SCHEME_EUCCLHYD) {
+    rc = rc ? rc : upload(v.uc, P, h.uc, nc, 2, nc, s);
+    rc = rc ? rc : upload(const_cast<double*>(v.lpc), P, h.lpc, nc, 8, nc, s);
+    rc = rc ? rc : upload(const_cast<double*>(v.cmat), P, h.cmat, nc, 12, nc, s);
+    rc = rc ? rc : upload(const_cast<double*>(v.xcc), P, h.xc, nc, 2, nc, s);
+    cp(v.perim, h.perim);
+    cp(v.evol, h.evol);
+  } else {
+    rc = rc ? rc : upload(const_cast<double*>(v.cqs), P, h.cqs, nc, 8, nc, s);
+    cp(v.cflsq, h.cflsq);
+    cp(v.s0, h.s0);
+    cp(v.sqs0, h.sqs0);
+  }
   cp(v.xs, h.xs);
   cp(v.ys, h.ys);
   cp(v.flv, h.flv);
@@ -349,7 +390,7 @@ int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait) {
   if (!rc && cudaMemcpyAsync(r->d_ctrl, &r->h_ctrl, sizeof(Ctrl),
                              cudaMemcpyHostToDevice, s) != cudaSuccess)
     rc = fail(-33, "ctrl upload");
-  if (!rc) launch_prologue(v, s);
+  if (!rc && v.scheme == HYDRO_SCHEME_VNR) launch_prologue(v, s);
   if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(-34, "prologue launch");
   if (!rc && wait && cudaStreamSynchronize(s) != cudaSuccess)
     rc = fail(-34, std::string("initial upload: ") +
@@ -501,6 +542,10 @@ size_t hydro_run_field_size(hydro_run* r, const char* f) {
   for (auto n : cell3)
     if (!strcmp(f, n)) return 3 * nc;
   if (!strcmp(f, "node_velocity")) return 2 * nn;
+  if (r->v.scheme == HYDRO_SCHEME_EUCCLHYD) {
+    if (!strcmp(f, "cell_velocity")) return 2 * nc;
+    return 0;
+  }
   if (!strcmp(f, "node_mass")) return nn;
   return 0;
 }
@@ -560,6 +605,15 @@ int hydro_run_fetch(hydro_run* r, const char* f, double* dst, size_t n) {
     for (long long p = 0; p < nn; ++p) {
       dst[2 * p] = tmp[p];
       dst[2 * p + 1] = tmp[v.npitch + p];
+    }
+    return 0;
+  }
+  if (!strcmp(f, "cell_velocity")) {
+    CUDA_TRY(get(v.uc, 2 * v.pitch, tmp));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    for (long long c = 0; c < nc; ++c) {
+      dst[2 * c] = tmp[c];
+      dst[2 * c + 1] = tmp[v.pitch + c];
     }
     return 0;
   }

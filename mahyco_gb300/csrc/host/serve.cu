@@ -324,6 +324,8 @@ int hydro_serve_config(hydro_ctx* ctx, size_t budget_bytes, int max_resident,
 int hydro_serve_submit(hydro_ctx* ctx, const hydro_spec* spec, int keep,
                        long* req_id) {
   if (!ctx || !spec) return fail(-1, "hydro_serve_submit: null argument");
+  if (spec->scheme != HYDRO_SCHEME_VNR)
+    return fail(-4, "hydro_serve_submit: the serving loop advances VNR runs");
   ServeState* S = get_serve(ctx);
   std::lock_guard<std::mutex> lk(S->mu);
   if (S->error) return fail(-2, "serving stopped: " + S->error_msg);

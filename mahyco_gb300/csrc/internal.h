@@ -92,6 +92,22 @@ struct RunView {
   double* gD;         // 2 node planes: limited nodal velocity gradient
   double* UD1;        // 3 node planes: m*u, m*v, m after sweep 1
 
+  // ---- Eucclhyd (cell-centred velocity; all null for VNR runs)
+  int space_order;
+  double* uc;         // 2 cell planes: cell velocity
+  double* vg;         // 4 cell planes: velocity gradient (row-major)
+  double* Fs;         // 2 + 2*nbmat cell planes: sums of the cell's corner
+                      // forces (total, then per material) of the last cycle
+  double* pex;        // 4 cell planes: extrapolated pressure per corner
+  double* uex;        // 8 cell planes [2k + d]: extrapolated velocity
+  double* peex;       // 4*nbmat cell planes [k*nbmat + m]: per material
+  const double* lpc;  // 8 cell planes [2k + d]: corner l_pc n_pc
+  const double* cmat; // 12 cell planes [3k + e]: corner matrix 00, 01, 11
+  const double* xcc;  // 2 cell planes: cell centroids
+  const double* perim;  // cell perimeter
+  const double* evol;   // Euler cell volume
+  double euc_cfl;
+
   // ---- control block (device)
   struct Ctrl* ctrl;
 };
@@ -114,7 +130,7 @@ struct Ctrl {
 
 // Per-kernel timing hook for launch_cycle.
 using LaunchHook = std::function<void(int)>;
-constexpr int kNumKernelKinds = 12;
+constexpr int kNumKernelKinds = 16;
 extern const char* const kKernelNames[kNumKernelKinds];
 
 // ---- batched execution: many independent runs advance in one launch per

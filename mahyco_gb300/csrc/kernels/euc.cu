@@ -1,0 +1,671 @@
+// FP64 CUDA kernels of one Eucclhyd Lagrange + remap cycle on GB300.
+//
+// Cycle structure (reference: Eucclhyd::executeTimeLoopN,
+// eucclhyd_remap/EucclhydRemap.cc:84-195):
+//   ke_begin     cycle start, reset of the dt reduction
+//   ke_cell_pre  computeEOS, computePressionMoyenne, computeGradients,
+//                computeMass, computem_cell_deltat (+ block min of dt)
+//   ke_nodes     extrapolateValue, computeG, computeNodeDissipationMatrixAndG,
+//                computeBoundaryNodeVelocities, computeNodeVelocity, the
+//                Lagrange node positions
+//   ke_cells     computeLagrangeVolumeAndCenterOfGravity, computeSubCellForce
+//                (recomputed per cell from the corner extrapolations),
+//                updateCellCenteredLagrangeVariables, the Lagrangian face
+//                lengths of the remap
+//   sweep x2     the shared directional remap (vnr.cu launch_sweep)
+//   ke_final     remapCellcenteredVariable (PhaseRemapFinal.cc:17-232)
+//   ke_end       computedeltat, updateTime, loop condition and time swap
+//
+// Corner quantities live per (cell, corner k); the reference keeps them per
+// (node, slot of the cell).  The sub-cell forces are not stored: the cell
+// kernel recomputes them from the corner extrapolations and the new node
+// velocities, and keeps only their per-material sums for the next cycle's
+// pressure gradients (computeGradients, PhaseLagrange.cc:225-244).  All
+// arithmetic keeps the reference's operation order (--fmad=false).
+#include <cuda_runtime.h>
+
+#include "../internal.h"
+#include "scheme_math.cuh"
+
+namespace hydro {
+
+int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* hook);
+
+namespace {
+
+constexpr int kBX = 32, kBY = 4;
+
+#define DV __device__ __forceinline__
+
+DV double ldg(const double* p, long long i) { return __ldg(p + i); }
+DV double gam(const RunView& v, int m) {
+  return m == 0 ? v.gamma[0] : (m == 1 ? v.gamma[1] : v.gamma[2]);
+}
+DV int eosm(const RunView& v, int m) {
+  return m == 0 ? v.eos[0] : (m == 1 ? v.eos[1] : v.eos[2]);
+}
+// dot product accumulated from 0.0 (includes/Freefunctions.h:15-20)
+DV double dot2(double a0, double a1, double b0, double b1) {
+  double r = 0.0;
+  r += a0 * b0;
+  r += a1 * b1;
+  return r;
+}
+DV double cross2(double a0, double a1, double b0, double b1) { return a0 * b1 - a1 * b0; }
+
+// block-wide min of ordered encodings, one atomic per block
+DV void block_min(unsigned long long dtv, Ctrl* C) {
+  __shared__ unsigned long long smin_s[32];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long a = __shfl_xor_sync(0xffffffffu, dtv, o);
+    dtv = a < dtv ? a : dtv;
+  }
+  if (lane == 0) smin_s[warp] = dtv;
+  __syncthreads();
+  if (warp == 0) {
+    dtv = lane < nw ? smin_s[lane] : ~0ull;
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long a = __shfl_xor_sync(0xffffffffu, dtv, o);
+      dtv = a < dtv ? a : dtv;
+    }
+    if (lane == 0 && dtv != ~0ull) atomicMin(&C->dt_min_bits, dtv);
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------- control
+__global__ void ke_begin(RunView v) {
+  Ctrl& C = *v.ctrl;
+  if (C.done || (C.err & ~HYDRO_ERR_NEGATIVE)) {
+    C.active = 0;
+    C.done = 1;
+    return;
+  }
+  C.active = 1;
+  C.n += 1;
+  C.dt_min_bits = ord_bits(1.7976931348623157e308);
+}
+
+// computedeltat (EucclhydRemap.cc:203-221): the cycle's cell dt minimum
+// gives dt_{n+1}; updateTime; the loop condition and the swap of t, dt.
+// The Lagrange positions and the remap of this cycle used dt_n.
+__global__ void ke_end(RunView v) {
+  Ctrl& C = *v.ctrl;
+  if (!C.active) return;
+  const double red = from_ord(C.dt_min_bits);
+  C.dt_np1 = smin(v.euc_cfl * red, C.dt_n * 1.05);
+  if (dlt(C.dt_np1, v.dt_min)) C.err |= HYDRO_ERR_DT_MIN;
+  C.t_np1 = C.t_n + C.dt_np1;
+  const bool cont = (C.n + 1 < v.max_iter) && dlt(C.t_np1, v.final_time);
+  C.t_n = C.t_np1;
+  C.dt_n = C.dt_np1;
+  if (cont)
+    C.x_then_y = !C.x_then_y;
+  else
+    C.done = 1;
+  if (C.err & ~HYDRO_ERR_NEGATIVE) C.done = 1;
+}
+
+// ------------------------------------------------- cell state of step n
+// computeEOS + computeEOSGP / computeEOSVoid (PhaseLagrange.cc:70-109),
+// computePressionMoyenne (:139-155), computeGradients (:160-246; the
+// fracvol-gradient part only feeds the particle scheme), computeMass
+// (:251-261), computem_cell_deltat (:302-316).
+struct EucCellPre {
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    unsigned long long dtb = ~0ull;
+    if (i < v.ny && j < v.nx) {
+      const long long P = v.pitch, NP = v.npitch;
+      const long long c = (long long)i * v.nx + j;
+      const int nb = v.nbmat;
+      double pm[3], cm[3];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        const double rm = v.rhom[m * P + c], em = v.em[m * P + c];
+        const double g = gam(v, m);
+        const int eos = eosm(v, m);
+        if (eos == HYDRO_EOS_PERFECT_GAS) {
+          pm[m] = (g - 1.0) * rm * em;
+          cm[m] = pos(rm) ? sqrt(g * pm[m] / rm) : 1.e-20;
+        } else if (eos == HYDRO_EOS_VOID) {
+          pm[m] = 0.;
+          cm[m] = 1.e-20;
+        } else {
+          pm[m] = v.pm[m * P + c];
+          cm[m] = v.cm[m * P + c];
+        }
+        v.pm[m * P + c] = pm[m];
+        v.cm[m * P + c] = cm[m];
+      }
+      double p = 0., snd = v.c[c];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        p += v.fm[m * P + c] * pm[m];
+        snd = smax(snd, cm[m]);
+      }
+      const double rho = v.rho[c];
+      if (pos(rho)) snd = sqrt(v.gamma[0] * p / rho);
+      v.p[c] = p;
+      v.c[c] = snd;
+      const double V = ldg(v.evol, c);
+      if (v.space_order == 2) {
+        const long long n0 = (long long)i * (v.nx + 1) + j;
+        const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
+        double r14[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const double u0 = v.u[nd[k]], u1 = v.u[NP + nd[k]];
+          const double l0 = ldg(v.lpc, (2 * k) * P + c), l1 = ldg(v.lpc, (2 * k + 1) * P + c);
+          r14[0] = r14[0] + u0 * l0;
+          r14[1] = r14[1] + u0 * l1;
+          r14[2] = r14[2] + u1 * l0;
+          r14[3] = r14[3] + u1 * l1;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v.vg[q * P + c] = qdiv(r14[q], V);
+        // per-material pressure gradients from last cycle's corner-force
+        // sums, in place
+        for (int q = 0; q < 2 * nb; ++q) v.Fs[q * P + c] = qdiv(v.Fs[q * P + c], V);
+      }
+      const double cmass = rho * V;
+      v.cell_mass[c] = cmass;
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        v.cmassm[m * P + c] = v.mfm[m * P + c] * cmass;
+      }
+      const double u0 = v.uc[c], u1 = v.uc[P + c];
+      const double un = sqrt(dot2(u0, u1, u0, u1));
+      const double cdt = (v.projection == 1) ? V / (ldg(v.perim, c) * (un + snd))
+                                             : V / (ldg(v.perim, c) * snd);
+      if (!is_nan(cdt)) dtb = ord_bits(cdt);
+    }
+    block_min(dtb, v.ctrl);
+  }
+};
+
+// Eucclhyd::nodeVelocityBoundaryCondition (ConditionsLimites.cc:109-123)
+DV void bc_velocity(int bc, double V0, double V1, const double* Mp, const double* G,
+                    double& o0, double& o1) {
+  if (bc == kBcSym) {
+    const double mv0 = dot2(Mp[0], Mp[1], V0, V1), mv1 = dot2(Mp[2], Mp[3], V0, V1);
+    const double s = dot2(G[0], G[1], V0, V1) / dot2(mv0, mv1, V0, V1);
+    o0 = V0 * s;
+    o1 = V1 * s;
+  } else if (bc == kBcImposed) {
+    o0 = V0;
+    o1 = V1;
+  } else if (bc == 202) {  // free: inverse(Mp) . G
+    const double alpha = 1.0 / (Mp[0] * Mp[3] - Mp[1] * Mp[2]);
+    const double i0 = Mp[3] * alpha, i1 = -Mp[1] * alpha, i2 = -Mp[2] * alpha,
+                 i3 = Mp[0] * alpha;
+    o0 = dot2(i0, i1, G[0], G[1]);
+    o1 = dot2(i2, i3, G[0], G[1]);
+  } else {
+    o0 = 0.0;
+    o1 = 0.0;
+  }
+}
+
+// ----------------------------------------------------------- node solve
+// extrapolateValue (:322-479), computeG (:484-505),
+// computeNodeDissipationMatrixAndG (:511-527), computeBoundaryNodeVelocities
+// (ConditionsLimites.cc:19-107), computeNodeVelocity (:532-543),
+// computeLagrangePosition nodes (:573-580).
+struct EucNodes {
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    if (i > v.ny || j > v.nx) return;
+    const Ctrl& C = *v.ctrl;
+    const long long P = v.pitch, NP = v.npitch;
+    const long long p = (long long)i * (v.nx + 1) + j;
+    const int nb = v.nbmat;
+    // cells of the node in getCellsOfNode order (CartesianMesh2D.cc:97-108)
+    // and the node's position in each
+    long long cells[4];
+    int loc[4], kc = 0;
+    if (i < v.ny && j < v.nx) { cells[kc] = (long long)i * v.nx + j; loc[kc++] = 0; }
+    if (i < v.ny && j > 0) { cells[kc] = (long long)i * v.nx + j - 1; loc[kc++] = 1; }
+    if (i > 0 && j < v.nx) { cells[kc] = (long long)(i - 1) * v.nx + j; loc[kc++] = 3; }
+    if (i > 0 && j > 0) { cells[kc] = (long long)(i - 1) * v.nx + j - 1; loc[kc++] = 2; }
+    const double X0 = ldg(v.xs, j), X1 = ldg(v.ys, i);
+    double pe_tot[4], ue0[4], ue1[4];
+    if (v.space_order == 2) {
+      double minP[3], maxP[3];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        minP[m] = 1.7976931348623157e308;
+        for (int t = 0; t < kc; ++t) minP[m] = smin(minP[m], v.pm[m * P + cells[t]]);
+        maxP[m] = 2.2250738585072014e-308;  // numeric_limits<double>::min()
+        for (int t = 0; t < kc; ++t) maxP[m] = smax(maxP[m], v.pm[m * P + cells[t]]);
+      }
+      double minVx = 1.7976931348623157e308, maxVx = 2.2250738585072014e-308;
+      double minVy = 1.7976931348623157e308, maxVy = 2.2250738585072014e-308;
+      for (int t = 0; t < kc; ++t) minVx = smin(minVx, v.uc[cells[t]]);
+      for (int t = 0; t < kc; ++t) maxVx = smax(maxVx, v.uc[cells[t]]);
+      for (int t = 0; t < kc; ++t) minVy = smin(minVy, v.uc[P + cells[t]]);
+      for (int t = 0; t < kc; ++t) maxVy = smax(maxVy, v.uc[P + cells[t]]);
+      for (int t = 0; t < kc; ++t) {
+        const long long c = cells[t];
+        const int k = loc[t];
+        const double d0 = X0 - ldg(v.xcc, c), d1 = X1 - ldg(v.xcc, P + c);
+        double pt = 0.;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          if (m >= nb) break;
+          const double pr = v.pm[m * P + c] +
+                            dot2(v.Fs[(2 * m) * P + c], v.Fs[(2 * m + 1) * P + c], d0, d1);
+          const double pe = smax(smin(maxP[m], pr), minP[m]);
+          v.peex[(k * nb + m) * P + c] = pe;
+          pt += v.fm[m * P + c] * pe;
+        }
+        pe_tot[t] = pt;
+        v.pex[k * P + c] = pt;
+        const double mv0 = dot2(v.vg[c], v.vg[P + c], d0, d1);
+        const double mv1 = dot2(v.vg[2 * P + c], v.vg[3 * P + c], d0, d1);
+        const double vt0 = v.uc[c] + mv0, vt1 = v.uc[P + c] + mv1;
+        ue0[t] = smax(smin(maxVx, vt0), minVx);
+        ue1[t] = smax(smin(maxVy, vt1), minVy);
+        v.uex[(2 * k) * P + c] = ue0[t];
+        v.uex[(2 * k + 1) * P + c] = ue1[t];
+      }
+    } else {
+      for (int t = 0; t < kc; ++t) {
+        const long long c = cells[t];
+        const int k = loc[t];
+        pe_tot[t] = v.p[c];
+        ue0[t] = v.uc[c];
+        ue1[t] = v.uc[P + c];
+        v.pex[k * P + c] = pe_tot[t];
+        v.uex[(2 * k) * P + c] = ue0[t];
+        v.uex[(2 * k + 1) * P + c] = ue1[t];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          if (m >= nb) break;
+          v.peex[(k * nb + m) * P + c] = v.pm[m * P + c];
+        }
+      }
+    }
+    // G and the node dissipation matrix
+    double G[2] = {0.0, 0.0};
+    double Mp[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int t = 0; t < kc; ++t) {
+      const long long c = cells[t];
+      const int k = loc[t];
+      const double s = v.rho[c] * v.c[c];
+      const double m00 = ldg(v.cmat, (3 * k) * P + c) * s;
+      const double m01 = ldg(v.cmat, (3 * k + 1) * P + c) * s;
+      const double m11 = ldg(v.cmat, (3 * k + 2) * P + c) * s;
+      const double mv0 = dot2(m00, m01, ue0[t], ue1[t]);
+      const double mv1 = dot2(m01, m11, ue0[t], ue1[t]);
+      const double l0 = ldg(v.lpc, (2 * k) * P + c), l1 = ldg(v.lpc, (2 * k + 1) * P + c);
+      G[0] = G[0] + (mv0 + l0 * pe_tot[t]);
+      G[1] = G[1] + (mv1 + l1 * pe_tot[t]);
+      Mp[0] = Mp[0] + m00;
+      Mp[1] = Mp[1] + m01;
+      Mp[2] = Mp[2] + m01;
+      Mp[3] = Mp[3] + m11;
+    }
+    // node velocity: the boundary rule of the last list holding the node
+    // (sides, then corners), inverse(Mp) . G inside
+    double u0, u1;
+    const bool top = (i == v.ny), bot = (i == 0), lft = (j == 0), rgt = (j == v.nx);
+    if ((top || bot) && (lft || rgt)) {
+      const int b1 = top ? v.bc_top : v.bc_bottom;
+      const double* V1 = top ? v.v_top : v.v_bottom;
+      const int b2 = lft ? v.bc_left : v.bc_right;
+      const double* V2 = lft ? v.v_left : v.v_right;
+      const double A0 = V1[0], A1 = V1[1], B0 = V2[0], B1 = V2[1];
+      u0 = 0.0;
+      u1 = 0.0;
+      if (b1 == kBcSym && b2 == kBcSym) {
+        const double na = sqrt(dot2(A0, A1, A0, A1)), nbb = sqrt(dot2(B0, B1, B0, B1));
+        if (fabs(fabs(dot2(A0, A1, B0, B1)) - na * nbb) < 1.0E-8)
+          bc_velocity(kBcSym, A0, A1, Mp, G, u0, u1);
+      } else if (b1 == kBcImposed && b2 == kBcImposed) {
+        u0 = 0.5 * (A0 + B0);
+        u1 = 0.5 * (A1 + B1);
+      } else if (b1 == 202 && b2 == 202) {
+        bc_velocity(202, A0, A1, Mp, G, u0, u1);
+      }
+    } else if (lft) {
+      bc_velocity(v.bc_left, v.v_left[0], v.v_left[1], Mp, G, u0, u1);
+    } else if (rgt) {
+      bc_velocity(v.bc_right, v.v_right[0], v.v_right[1], Mp, G, u0, u1);
+    } else if (top) {
+      bc_velocity(v.bc_top, v.v_top[0], v.v_top[1], Mp, G, u0, u1);
+    } else if (bot) {
+      bc_velocity(v.bc_bottom, v.v_bottom[0], v.v_bottom[1], Mp, G, u0, u1);
+    } else {
+      bc_velocity(202, 0.0, 0.0, Mp, G, u0, u1);
+    }
+    v.u[p] = u0;
+    v.u[NP + p] = u1;
+    v.XL[p] = X0 + u0 * C.dt_n;
+    v.XL[NP + p] = X1 + u1 * C.dt_n;
+  }
+};
+
+// ----------------------------------------------------- cell Lagrange step
+// computeLagrangeVolumeAndCenterOfGravity (:671-716), computeSubCellForce
+// (:625-666), updateCellCenteredLagrangeVariables (:746-1010), and the
+// Lagrangian face lengths that give HvLagrange (remap/PhaseRemap1.cc:57-71).
+struct EucCells {
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    if (i >= v.ny || j >= v.nx) return;
+    const Ctrl& C = *v.ctrl;
+    const long long P = v.pitch, NP = v.npitch;
+    const long long c = (long long)i * v.nx + j;
+    const int nb = v.nbmat;
+    const long long n0 = (long long)i * (v.nx + 1) + j;
+    const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
+    double X[4][2];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      X[k][0] = v.XL[nd[k]];
+      X[k][1] = v.XL[NP + nd[k]];
+    }
+    double r6 = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int kp = (k + 1) & 3;
+      r6 = r6 + cross2(X[k][0], X[k][1], X[kp][0], X[kp][1]);
+    }
+    const double vol = 0.5 * r6;
+    v.vL[c] = vol;
+    double r7a = 0.0, r7b = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int kp = (k + 1) & 3;
+      const double cr = cross2(X[k][0], X[k][1], X[kp][0], X[kp][1]);
+      r7a = r7a + (X[k][0] + X[kp][0]) * cr;
+      r7b = r7b + (X[k][1] + X[kp][1]) * cr;
+    }
+    const double sc = 1.0 / (6.0 * vol);
+    v.XcL[c] = r7a * sc;
+    v.XcL[P + c] = r7b * sc;
+    if (v.order > 1) {
+      auto len = [&](int a, int b) {
+        const double d0 = X[b][0] - X[a][0], d1 = X[b][1] - X[a][1];
+        return sqrt(dot2(d0, d1, d0, d1));
+      };
+      double hx = 0.;
+      hx += 0.5 * len(0, 1);
+      hx += 0.5 * len(3, 2);
+      double hy = 0.;
+      hy += 0.5 * len(1, 2);
+      hy += 0.5 * len(0, 3);
+      v.Hx[c] = hx;
+      v.Hy[c] = hy;
+    }
+    // sub-cell forces of the cell's corners with the new node velocities
+    const double rho = v.rho[c], snd = v.c[c];
+    const double s = rho * snd;
+    double se[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) se[m] = (m < nb) ? v.rhom[m * P + c] * snd : 0.0;
+    double r2 = 0.0, r3a = 0.0, r3b = 0.0;
+    double un0[4], un1[4], Fe0[4][3], Fe1[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const double u0 = v.u[nd[k]], u1 = v.u[NP + nd[k]];
+      un0[k] = u0;
+      un1[k] = u1;
+      const double l0 = ldg(v.lpc, (2 * k) * P + c), l1 = ldg(v.lpc, (2 * k + 1) * P + c);
+      r2 = r2 + dot2(l0, l1, u0, u1);
+      const double du0 = u0 - v.uex[(2 * k) * P + c];
+      const double du1 = u1 - v.uex[(2 * k + 1) * P + c];
+      const double c00 = ldg(v.cmat, (3 * k) * P + c), c01 = ldg(v.cmat, (3 * k + 1) * P + c),
+                   c11 = ldg(v.cmat, (3 * k + 2) * P + c);
+      {
+        const double m00 = c00 * s, m01 = c01 * s, m11 = c11 * s;
+        const double mp = -v.pex[k * P + c];
+        const double f0 = l0 * mp + dot2(m00, m01, du0, du1);
+        const double f1 = l1 * mp + dot2(m01, m11, du0, du1);
+        r3a = r3a + f0;
+        r3b = r3b + f1;
+      }
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        const double m00 = c00 * se[m], m01 = c01 * se[m], m11 = c11 * se[m];
+        const double mp = -v.peex[(k * nb + m) * P + c];
+        Fe0[k][m] = l0 * mp + dot2(m00, m01, du0, du1);
+        Fe1[k][m] = l1 * mp + dot2(m01, m11, du0, du1);
+      }
+    }
+    const double dt = C.dt_n;
+    const double cmass = v.cell_mass[c];
+    const double rhoL = 1 / (1 / rho + dt / cmass * r2);
+    const double uc0 = v.uc[c], uc1 = v.uc[P + c];
+    const double uL0 = uc0 + r3a * dt / cmass;
+    const double uL1 = uc1 + r3b * dt / cmass;
+    const double mid0 = (uc0 + uL0) * 0.5, mid1 = (uc1 + uL1) * 0.5;
+    double pr4[3] = {0.0, 0.0, 0.0}, fsa[3] = {0.0, 0.0, 0.0}, fsb[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const double d0 = un0[k] - mid0, d1 = un1[k] - mid1;
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        pr4[m] = pr4[m] + dot2(Fe0[k][m], Fe1[k][m], d0, d1);
+        fsa[m] = fsa[m] + Fe0[k][m];
+        fsb[m] = fsb[m] + Fe1[k][m];
+      }
+    }
+    // per-material corner-force sums for the next cycle's gradients
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      v.Fs[(2 * m) * P + c] = fsa[m];
+      v.Fs[(2 * m + 1) * P + c] = fsb[m];
+    }
+    double peL[3];
+    const double thr = v.threshold;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      peL[m] = 0.;
+      const double f = v.fm[m * P + c], cmm = v.cmassm[m * P + c];
+      if (dgt(f, thr) && nz(cmm)) peL[m] = v.em[m * P + c] + f * dt / cmm * pr4[m];
+    }
+    // ULagrange and Phi
+    const int ncomp = v.ncomp;
+    double U[kMaxComp];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      const double mf = v.mfm[m * P + c];
+      U[m] = v.fm[m * P + c] * vol;
+      U[nb + m] = mf * vol * rhoL;
+      U[2 * nb + m] = mf * vol * rhoL * peL[m];
+    }
+    U[3 * nb] = vol * rhoL * uL0;
+    U[3 * nb + 1] = vol * rhoL * uL1;
+    if (v.conservative == 1) U[3 * nb + 2] = 0.5 * vol * rhoL * (uL0 * uL0 + uL1 * uL1);
+    for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
+    if (v.pb == 1) {
+      double sv = 0.;
+      for (int m = 0; m < nb; ++m) sv += U[m];
+      double sm = 0.;
+      for (int m = 0; m < nb; ++m) {
+        v.Phi[m * P + c] = qdiv(U[m], sv);
+        v.Phi[(nb + m) * P + c] = nz(U[m]) ? qdiv(U[nb + m], U[m]) : 0.;
+        sm += U[nb + m];
+      }
+      v.Phi[3 * nb * P + c] = qdiv(U[3 * nb], sm);
+      v.Phi[(3 * nb + 1) * P + c] = qdiv(U[3 * nb + 1], sm);
+      for (int m = 0; m < nb; ++m)
+        v.Phi[(2 * nb + m) * P + c] = nz(U[nb + m]) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
+      if (v.conservative == 1) v.Phi[(3 * nb + 2) * P + c] = qdiv(U[3 * nb + 2], sm);
+    } else {
+      for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv(U[k], vol);
+    }
+  }
+};
+
+// --------------------------------------------------------- remap final
+// Eucclhyd::remapCellcenteredVariable (PhaseRemapFinal.cc:17-200)
+struct EucFinal {
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    if (i >= v.ny || j >= v.nx) return;
+    Ctrl& C = *v.ctrl;
+    const long long P = v.pitch;
+    const long long c = (long long)i * v.nx + j;
+    const int nb = v.nbmat;
+    const double thr = v.threshold;
+    const double* U = v.UL + c;  // second sweep output
+    const double vol = ldg(v.evol, c);
+    double volt = 0., masset = 0., vn[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      vn[m] = U[m * P];
+      volt += vn[m];
+      masset += U[(nb + m) * P];
+    }
+    double vnorm = 0.;
+    const double r = qdiv(vol, volt);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      vn[m] *= r;
+      vnorm += vn[m];
+    }
+    double f[3], mf[3], sf = 0.;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      f[m] = qdiv(vn[m], vnorm);
+      if (dlt(f[m], thr)) f[m] = 0.;
+      sf += f[m];
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      f[m] = qdiv(f[m], sf);
+    }
+    int matcell = 0, imatpure = -1;
+    for (int m = 0; m < nb; ++m)
+      if (pos(f[m])) {
+        matcell++;
+        imatpure = m;
+      }
+    v.mixte[c] = (matcell > 1) ? 1 : 0;
+    v.pure[c] = (matcell > 1) ? -1 : imatpure;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      mf[m] = qdiv(U[(nb + m) * P], masset);
+    }
+    double fmt = 0.;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      if (dlt(f[m], thr)) mf[m] = 0.;
+      fmt += mf[m];
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      mf[m] = qdiv(mf[m], fmt);
+    }
+    double dm[3] = {0., 0., 0.}, dens = 0.;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      if (dgt(f[m], thr)) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
+      dens += f[m] * dm[m];
+    }
+    const double mv = dens * vol;
+    const double un0 = qdiv(U[3 * nb * P], mv), un1 = qdiv(U[(3 * nb + 1) * P], mv);
+    double pe[3] = {0., 0., 0.};
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      if (dgt(f[m], thr) && nz(U[(nb + m) * P]))
+        pe[m] = qdiv(U[(2 * nb + m) * P], U[(nb + m) * P]);
+    }
+    double dec = 0.;
+    if (v.conservative == 1)
+      dec = qdiv(U[(3 * nb + 2) * P], masset) - 0.5 * (un0 * un0 + un1 * un1);
+    double e = 0.;
+    double rhom[3], em[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      rhom[m] = dm[m];
+      em[m] = pe[m];
+      em[m] += dec;
+      e += mf[m] * em[m];
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      if (neg(pe[m]) || neg(dm[m])) {
+        rhom[m] = 0.;
+        em[m] = 0.;
+        mf[m] = 0.;
+        f[m] = 0.;
+        atomicOr(&C.err, HYDRO_ERR_NEGATIVE);
+      }
+    }
+    if (is_nan(e) || is_nan(dens)) {
+      atomicOr(&C.err, HYDRO_ERR_NAN);
+      atomicMin((unsigned long long*)&C.err_cell, (unsigned long long)c);
+    }
+    v.rho[c] = dens;
+    v.uc[c] = un0;
+    v.uc[P + c] = un1;
+    v.e[c] = e;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      v.fm[m * P + c] = f[m];
+      v.mfm[m * P + c] = mf[m];
+      v.rhom[m * P + c] = rhom[m];
+      v.em[m * P + c] = em[m];
+    }
+  }
+};
+
+template <class F>
+__device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
+  if (!v.ctrl->active) return;
+  f(v, blockIdx.y * kBY + threadIdx.y, blockIdx.x * kBX + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kBX* kBY) ke_cell_pre(RunView v) { plain_items(v, EucCellPre{}); }
+__global__ void __launch_bounds__(kBX* kBY) ke_nodes(RunView v) { plain_items(v, EucNodes{}); }
+__global__ void __launch_bounds__(kBX* kBY) ke_cells(RunView v) { plain_items(v, EucCells{}); }
+__global__ void __launch_bounds__(kBX* kBY) ke_final(RunView v) { plain_items(v, EucFinal{}); }
+
+}  // namespace
+
+// One Eucclhyd cycle on stream s (kind ids: 0 begin, 12 cell_pre, 13 nodes,
+// 14 cells, sweeps, 15 final, 10 end).  Returns the number of kernels.
+int launch_cycle_euc(const RunView& v, cudaStream_t s, const LaunchHook* hook) {
+  const dim3 blk(kBX, kBY);
+  const dim3 cg((v.nx + kBX - 1) / kBX, (v.ny + kBY - 1) / kBY);
+  const dim3 ng((v.nx + 1 + kBX - 1) / kBX, (v.ny + 1 + kBY - 1) / kBY);
+  int nk = 0;
+  auto H = [&](int kind) {
+    if (hook) (*hook)(kind);
+  };
+  H(0); ke_begin<<<1, 1, 0, s>>>(v); ++nk;
+  H(12); ke_cell_pre<<<cg, blk, 0, s>>>(v); ++nk;
+  H(13); ke_nodes<<<ng, blk, 0, s>>>(v); ++nk;
+  H(14); ke_cells<<<cg, blk, 0, s>>>(v); ++nk;
+  for (int sweep = 1; sweep <= 2; ++sweep) nk += launch_sweep(v, sweep, s, hook);
+  H(15); ke_final<<<cg, blk, 0, s>>>(v); ++nk;
+  H(10); ke_end<<<1, 1, 0, s>>>(v); ++nk;
+  H(-1);
+  return nk;
+}
+
+}  // namespace hydro

@@ -571,12 +571,16 @@ struct SweepGrad {
       const double ppa = 0.5 * (Fa + fabs(Fa)) * dt;
       const double ppb = 0.5 * (Fb + fabs(Fb)) * dt;
       const double ppd = 0.5 * (fdual + fabs(fdual)) * dt;
-      const bool cfd = (v.dual_method == 2);
+      // Eucclhyd carries momentum (and kinetic energy) after the material
+      // components instead of the VNR pseudo-viscosity, and has no dual remap
+      const bool euc = (v.scheme == HYDRO_SCHEME_EUCCLHYD);
+      const bool cfd = !euc && (v.dual_method == 2);
       const int plim = vp ? v.limiter_pure : v.limiter;
       // which components are integrated: volumes always; masses for the pure
-      // variant; masses + energies for the "complet" variant; the dual flux
-      // needs the mass components (computeFluxPP, UtilesRemap-Impl.h:259-313)
-      const int nint = (v.pb_complet == 1) ? 3 * nb : (vp ? 2 * nb : nb);
+      // variant; masses + energies (+ momentum for Eucclhyd) for the
+      // "complet" variant; the dual flux needs the mass components
+      // (computeFluxPP, UtilesRemap-Impl.h:259-313)
+      const int nint = (v.pb_complet == 1) ? (euc ? ncomp : 3 * nb) : (vp ? 2 * nb : nb);
       const int nuse = (cfd && nint < 2 * nb) ? 2 * nb : nint;
       double Fr[kMaxComp], Fv[kMaxComp];
       const double hh = h0;
@@ -619,18 +623,25 @@ struct SweepGrad {
               F[2 * nb + m] = (F[2 * nb + m] / sfv) * F[nb + m];
               sfm += F[nb + m];
             }
-            F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
+            if (euc)
+              for (int k = 3 * nb; k < ncomp; ++k) F[k] = (F[k] / sfv) * sfm;
+            else
+              F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
           } else {
             for (int k = 0; k < ncomp; ++k) F[k] = 0.0;
           }
         } else {
-          double sfv = 0.;
+          double sfv = 0., sfm = 0.;
           for (int m = 0; m < nb; m++) {
             if (!vp) F[nb + m] = v.Phi[(nb + m) * P + c] * F[m];
             F[2 * nb + m] = v.Phi[(2 * nb + m) * P + c] * F[nb + m];
+            sfm += F[nb + m];
             sfv += F[m];
           }
-          F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
+          if (euc)
+            for (int k = 3 * nb; k < ncomp; ++k) F[k] = v.Phi[k * P + c] * sfm;
+          else
+            F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
         }
         for (int k = 0; k < ncomp; ++k) out[k * P] = iszero(ppv) ? 0.0 : F[k];
       };
@@ -788,7 +799,8 @@ struct SweepUpdate {
       }
       U[k] = Uin[k * P + c] - red;
       Uout[k * P + c] = U[k];
-      if (v.dual_method != 2 && k >= doff && k < doff + nb) {
+      if (v.scheme != HYDRO_SCHEME_EUCCLHYD && v.dual_method != 2 && k >= doff &&
+        k < doff + nb) {
         v.FFd[(k - doff) * P + c] = F0;
         v.FFd[(nb + k - doff) * P + c] = F1;
       }
@@ -806,7 +818,10 @@ struct SweepUpdate {
         }
         for (int m = 0; m < nb; m++)
           Phi[(2 * nb + m) * P + c] = nz(U[nb + m]) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
-        (void)sm;
+        // Eucclhyd momentum / kinetic energy per unit mass (the VNR
+        // pseudo-viscosity slot is not updated here in the reference)
+        if (v.scheme == HYDRO_SCHEME_EUCCLHYD)
+          for (int k = 3 * nb; k < ncomp; ++k) Phi[k * P + c] = qdiv(U[k], sm);
       } else {
         const double vl = v.vL[c];
         for (int k = 0; k < ncomp; ++k) Phi[k * P + c] = qdiv(U[k], vl);
@@ -1312,15 +1327,37 @@ void launch_node_mass(const RunView& v, cudaStream_t s) {
 const char* const kKernelNames[kNumKernelKinds] = {
     "k_begin",      "k_reset_reductions", "k_lag_nodes", "k_lag_cells",
     "k_sweep_grad", "k_sweep_face",       "k_sweep_update", "k_dual_grad",
-    "k_dual_update", "k_final",           "k_end",         "k_face_grad"};
+    "k_dual_update", "k_final",           "k_end",         "k_face_grad",
+    "ke_cell_pre",  "ke_nodes",           "ke_cells",      "ke_final"};
 
 // Enqueues one full cycle on stream s; hook(kind) is called before each
 // launch (and with kind = -1 after the last) when given.  Returns the number
 // of kernels.
+// One directional remap sweep (Remap::computeGradPhiFace, computeGradPhi,
+// computeUpwindFaceQuantitiesForProjection, computeUremap) on stream s,
+// shared by both Lagrange schemes.  Returns the number of kernels.
+int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* hook) {
+  const dim3 blk(kBX, kBY);
+  const dim3 cg = cell_grid(v), fg = node_grid(v);
+  int nk = 0;
+  auto H = [&](int kind) {
+    if (hook) (*hook)(kind);
+  };
+  if (v.order > 1) {
+    H(11); k_face_grad<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+    H(4); k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk;
+  }
+  H(5); k_sweep_face<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+  H(6); k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
+  return nk;
+}
+
+int launch_cycle_euc(const RunView& v, cudaStream_t s, const LaunchHook* hook);
+
 int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook) {
+  if (v.scheme == HYDRO_SCHEME_EUCCLHYD) return launch_cycle_euc(v, s, hook);
   const dim3 blk(kBX, kBY);
   const dim3 cg = cell_grid(v), ng = node_grid(v);
-  const dim3 fg = ng;
   int nk = 0;
   auto H = [&](int kind) {
     if (hook) (*hook)(kind);
@@ -1330,12 +1367,7 @@ int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook) {
   H(2); k_lag_nodes<<<ng, blk, 0, s>>>(v); ++nk;
   H(3); k_lag_cells<<<cg, blk, 0, s>>>(v); ++nk;
   for (int sweep = 1; sweep <= 2; ++sweep) {
-    if (v.order > 1) {
-      H(11); k_face_grad<<<fg, blk, 0, s>>>(v, sweep); ++nk;
-      H(4); k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk;
-    }
-    H(5); k_sweep_face<<<fg, blk, 0, s>>>(v, sweep); ++nk;
-    H(6); k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
+    nk += launch_sweep(v, sweep, s, hook);
     H(7); k_dual_grad<<<ng, blk, 0, s>>>(v, sweep); ++nk;
     H(8); k_dual_update<<<ng, blk, 0, s>>>(v, sweep); ++nk;
   }

@@ -195,8 +195,10 @@ static void sub_volumes(port_run* R, const double* X, const double* Xc,
   }
 }
 
-/* Vnr::initMeshGeometryForFaces (vnr_remap/Init.cc:517-554). */
-static void face_geometry(port_run* R) {
+/* Vnr::initMeshGeometryForFaces (vnr_remap/Init.cc:517-554); the same
+ * computation as Eucclhyd::initMeshGeometryForFaces (eucclhyd_remap/Init.cc
+ * :677-716) on that scheme's cell centres. */
+void port_face_geometry(port_run* R) {
   for (long f = 0; f < R->nf; ++f) {
     face_info F;
     port_face_decode(R, f, &F);
@@ -1208,7 +1210,7 @@ static int vnr_setup(port_run* R) {
   update_mixte(R);
   sub_volumes(R, R->X0, R->Xc0, R->Vpc0);
   for (long c = 0; c < R->nc; ++c) R->eulerV[c] = R->s.dx * R->s.dy;
-  face_geometry(R);
+  port_face_geometry(R);
   faces_of_node(R);
   vnr_cell_mass(R);
   if (R->s.sans_lagrange == 0) {

@@ -43,6 +43,16 @@ CELL_FIELDS = ["density", "pressure", "energy", "sound_speed", "pseudo", "divu",
                "cell_mass", "density_env", "energy_env", "pressure_env",
                "fracvol_env", "mass_fraction_env"]
 NODE_FIELDS = ["node_velocity"]
+EUC_FIELDS = ["density", "pressure", "energy", "sound_speed", "cell_velocity",
+              "density_env", "energy_env", "fracvol_env", "mass_fraction_env",
+              "node_velocity"]
+
+
+def fields_of(spec):
+    """Fields a fixture of this scheme holds (all compared bit for bit)."""
+    if spec.scheme == 2000:  # Eucclhyd
+        return EUC_FIELDS
+    return CELL_FIELDS + NODE_FIELDS + ["node_mass"]
 
 
 def get_field(run, name, nbmat):

@@ -8,9 +8,11 @@ precision final state next to the option set parsed from the deck:
                             pseudo divu cell_mass node_velocity node_mass
                             + *_env (nbmat columns), spec (JSON), meta
 
-Cases: every VNR deck of the reference's test suite that uses the remap
-(AvecProjection = oui), plus decks derived from them for the 200x10 Sod
-workload and a reduced bi-material Sod with the mixed interface row.
+Cases: every deck of the reference's test suite that uses the remap
+(AvecProjection = oui), VNR and Eucclhyd, plus decks derived from them: the
+200x10 Sod workload, a reduced bi-material Sod with the mixed interface row,
+and the three-material triple point with one exponent per material.
+Eucclhyd fixtures hold cell_velocity instead of the VNR-only fields.
 
 Needs the reference sources (default /root/reference); run from the repo root:
   make -f oracle/Makefile.ref REF=/root/reference -j8
@@ -36,6 +38,11 @@ DUMP = ROOT / "oracle" / "_ref" / "mahyco_dump"
 FIELDS = ["density", "pressure", "energy", "sound_speed", "pseudo", "divu",
           "cell_mass", "density_env", "energy_env", "pressure_env",
           "fracvol_env", "mass_fraction_env", "node_velocity", "node_mass"]
+# what the harness dumps for a Eucclhyd run (the cell-centred velocity, the
+# pressure and sound speed of the last cycle's start)
+FIELDS_EUC = ["density", "pressure", "energy", "sound_speed", "cell_velocity",
+              "density_env", "energy_env", "fracvol_env", "mass_fraction_env",
+              "node_velocity"]
 
 LIM_NAME = {v: k for k, v in M.LIMITERS.items()}
 
@@ -80,7 +87,7 @@ def write_deck(spec: M.HydroSpec, path: Path) -> None:
     path.write_text("\n".join(lines) + "\n")
 
 
-def run_reference(deck: Path, cycles: int = 0, extra=()) -> dict:
+def run_reference(deck: Path, cycles: int = 0, extra=(), fields=FIELDS) -> dict:
     with tempfile.TemporaryDirectory() as d:
         args = [str(DUMP), str(deck), d]
         if cycles:
@@ -88,7 +95,7 @@ def run_reference(deck: Path, cycles: int = 0, extra=()) -> dict:
         args += list(extra)
         subprocess.run(args, stdout=subprocess.DEVNULL, check=True)
         meta = dict(line.split() for line in open(f"{d}/meta.txt"))
-        out = {f: np.fromfile(f"{d}/{f}.f64") for f in FIELDS}
+        out = {f: np.fromfile(f"{d}/{f}.f64") for f in fields}
     return meta, out
 
 
@@ -118,7 +125,7 @@ def main() -> None:
         if not deck.exists():
             continue
         spec = M.parse_deck(deck)
-        if spec.scheme == M.SCHEME_VNR and spec.projection == 1:
+        if spec.projection == 1:
             cases.append((d.name, spec, deck, ()))
     tmp = Path(tempfile.mkdtemp())
     # 200x10 Sod X, VNR, order-2 remap, minmod, t = 0.2
@@ -133,10 +140,31 @@ def main() -> None:
     s.init_variant = 1
     cases.append(("BISOD_Y_64x64_superbee_pb_mixedrow", s, tmp / "bisod64.txt",
                   ("--ext-mixed-row",)))
+    # three-material triple point (Eucclhyd, superBee + PenteBorne mixte) with
+    # one adiabatic exponent per material
+    s = M.parse_deck(tests / "POINT_TRIPLE_SuperBee_PenteBorne_mixte" / "donnees.txt")
+    s.gamma[0], s.gamma[1], s.gamma[2] = 1.5, 1.4, 1.5
+    cases.append(("POINT_TRIPLE_gamma_1.5_1.4_1.5_pb_mixte", s,
+                  tests / "POINT_TRIPLE_SuperBee_PenteBorne_mixte" / "donnees.txt",
+                  ("--gamma", "1.5,1.4,1.5")))
+    # order-3 projection with PenteBorne (mixte): the reference takes the
+    # order-3 face value as an integrated flux and its state turns negative,
+    # then NaN in the second cycle (it exits); one cycle pins that arithmetic
+    src = (tests / "POINT_TRIPLE_SuperBee_PenteBorne_mixte" / "donnees.txt").read_text()
+    lines = src.splitlines()
+    for k, line in enumerate(lines):
+        if line.startswith("# Ordre de la projection"):
+            lines[k + 1] = "3"
+    (tmp / "tp_o3_pb.txt").write_text("\n".join(lines) + "\n")
+    s = M.parse_deck(tmp / "tp_o3_pb.txt")
+    s.max_cycles = 1
+    cases.append(("POINT_TRIPLE_o3_pb_mixte_1cycle", s, tmp / "tp_o3_pb.txt",
+                  ("--cycles", "1")))
     for name, spec, deck, extra in cases:
         if a.only and a.only not in name:
             continue
-        meta, fields = run_reference(deck, 0, extra)
+        euc = spec.scheme == M.SCHEME_EUCCLHYD
+        meta, fields = run_reference(deck, 0, extra, FIELDS_EUC if euc else FIELDS)
         save(name, spec, meta, fields)
 
 

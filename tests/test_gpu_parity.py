@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from conftest import (CELL_FIELDS, GOLDEN, NODE_FIELDS, assert_bitwise,
-                      get_field, golden_cases, load_golden)
+                      fields_of, get_field, golden_cases, load_golden)
 
 pytestmark = pytest.mark.gpu
 
@@ -36,7 +36,7 @@ def test_gpu_matches_reference(case, M, ctx):
     t, dt, n = run.time()
     assert n == int(meta["cycles"])
     assert t == float(meta["t"])
-    for f in CELL_FIELDS + NODE_FIELDS + ["node_mass"]:
+    for f in fields_of(spec):
         assert_bitwise(f"{case}:{f}", get_field(run, f, spec.nbmat), want[f])
     assert run.error()[0] & ~M.ERR_NEGATIVE == 0
 
@@ -102,3 +102,61 @@ def test_gpu_error_word_instead_of_abort(M, ctx):
     ok = M.Run(load_golden(GOLDEN / "SOD_X_Mono_mat_Minmod_vnr_o2.npz")[0], ctx)
     ok.step(3)
     assert ok.error()[0] == 0
+
+
+def triple_point(M, nx, ny, cycles, order=3):
+    """The three-material triple point on [0,7]x[0,3] (Eucclhyd, superBee
+    with PenteBorne mixte, arithmeticG in pure cells, CFL 0.4, exponents
+    1.5 / 1.4 / 1.5, regions x <= 1 and y <= 1.5 scaled to the domain)."""
+    s = M.default_spec()
+    s.scheme, s.test_case, s.nbmat = M.SCHEME_EUCCLHYD, 13, 3
+    s.nx, s.ny = nx, ny
+    s.dx, s.dy = 7.0 / nx, 3.0 / ny
+    for m, g in enumerate((1.5, 1.4, 1.5)):
+        s.eos[m] = 101
+        s.gamma[m] = g
+    s.gamma_scalar = 1.4
+    s.cfl = 0.4
+    s.final_time, s.dt_min, s.space_order = 100.0, 1e-12, 2
+    s.projection, s.projection_order = 1, order
+    s.limiter = M.LIMITERS["superBee"]
+    s.pb, s.pb_mixte, s.limiter_pure, s.pb_complet = 1, 1, M.LIMITERS["arithmeticG"], 0
+    s.init_variant = 3
+    s.max_cycles = cycles
+    return s
+
+
+@pytest.mark.parametrize("order,pb,complet", [(3, 0, 0), (2, 1, 0), (2, 1, 1), (3, 1, 0)])
+def test_gpu_triple_point_matches_port(order, pb, complet, M, ctx, port_lib):
+    """Order 3 with PenteBorne reproduces the reference's arithmetic, which
+    takes the order-3 face value as an integrated flux: the state turns
+    negative and the run stops with a NaN error in the second cycle, on the
+    GPU as in the reference."""
+    from conftest import EUC_FIELDS
+    spec = triple_point(M, 224, 96, 60, order)
+    spec.pb, spec.pb_mixte, spec.pb_complet = pb, pb, complet
+    g = M.Run(spec, ctx)
+    g.simulate()
+    c = port_lib.PortRun(spec)
+    c.simulate()
+    assert g.time() == c.time()
+    assert g.error() == c.error()
+    for f in EUC_FIELDS:
+        assert_bitwise(f, get_field(g, f, spec.nbmat), get_field(c, f, spec.nbmat))
+
+
+def test_gpu_triple_point_full_size_conserves_mass(M, ctx):
+    """1792x768 triple point (the Eucclhyd workload: order-3 projection,
+    superBee), 20 cycles: total mass is conserved to 1e-12 relative,
+    velocities and densities stay finite."""
+    spec = triple_point(M, 1792, 768, 20)
+    spec.pb = spec.pb_mixte = 0
+    run = M.Run(spec, ctx)
+    vol = 7.0 * 3.0 / (1792 * 768)
+    m0 = run.fetch("density").sum() * vol
+    run.simulate()
+    m1 = run.fetch("density").sum() * vol
+    assert abs(m1 - m0) <= 1e-12 * m0
+    assert np.all(np.isfinite(run.fetch("cell_velocity")))
+    assert run.error()[0] & ~M.ERR_NEGATIVE == 0
+    assert run.time()[2] == 20

@@ -5,7 +5,7 @@ from __future__ import annotations
 import pytest
 
 from conftest import (CELL_FIELDS, GOLDEN, NODE_FIELDS, assert_bitwise,
-                      get_field, golden_cases, load_golden)
+                      fields_of, get_field, golden_cases, load_golden)
 
 
 @pytest.mark.parametrize("case", golden_cases())
@@ -16,5 +16,5 @@ def test_port_matches_reference(case, port_lib):
     t, dt, n = run.time()
     assert n == int(meta["cycles"])
     assert t == float(meta["t"])
-    for f in CELL_FIELDS + NODE_FIELDS + ["node_mass"]:
+    for f in fields_of(spec):
         assert_bitwise(f"{case}:{f}", get_field(run, f, spec.nbmat), want[f])
