@@ -370,6 +370,88 @@ def bench_serve(M, args, local: int) -> dict:
             "value": max((o["value"] or 0) for o in out) if out else None, "unit": UNIT}
 
 
+def triple_point_spec(M, nx: int = 1792, ny: int = 768, cycles: int = 300,
+                      order: int = 3, pb: int = 0):
+    """Three-material triple point on [0,7]x[0,3]: Eucclhyd, superBee,
+    CFL 0.4, exponents 1.5 / 1.4 / 1.5, regions x <= 1 and y <= 1.5."""
+    s = M.default_spec()
+    s.scheme, s.test_case, s.nbmat = M.SCHEME_EUCCLHYD, 13, 3
+    s.nx, s.ny = nx, ny
+    s.dx, s.dy = 7.0 / nx, 3.0 / ny
+    for m, g in enumerate((1.5, 1.4, 1.5)):
+        s.eos[m] = 101
+        s.gamma[m] = g
+    s.gamma_scalar, s.cfl = 1.4, 0.4
+    s.final_time, s.dt_min, s.space_order = 100.0, 1e-12, 2
+    s.projection, s.projection_order = 1, order
+    s.limiter = M.LIMITERS["superBee"]
+    s.pb, s.pb_mixte, s.limiter_pure, s.pb_complet = pb, pb, M.LIMITERS["arithmeticG"], 0
+    s.init_variant = 3
+    s.max_cycles = cycles
+    return s
+
+
+EUC_WORKLOAD = {
+    "workload": "triple point, 3 materials, 1792x768 cells on [0,7]x[0,3], "
+                "Eucclhyd + order-3 remap, superBee, CFL 0.4, gamma 1.5/1.4/1.5",
+    "mesh": [1792, 768], "nbmat": 3, "scheme": "Eucclhyd", "projection_order": 3,
+    "limiter": "superBee", "pente_borne": "non",
+    "note": "with PenteBorne mixte and order 3 the reference itself stops in "
+            "cycle 2 (negative, then NaN densities: it takes the order-3 face "
+            "value as an integrated flux); this path reproduces that and stops "
+            "the same way (see configured_variant), so the throughput is "
+            "measured on the same case without PenteBorne",
+}
+
+
+def bench_euc(M, ctx, args, local: int) -> dict:
+    """Eucclhyd on the triple point: device time of K cycles (state resident),
+    per-kernel times, the configured PenteBorne variant's outcome, and the
+    C restatement on a bounded sample."""
+    K = args.euc_steps
+    w = M.Run(triple_point_spec(M, cycles=args.warmup + 1), ctx)
+    w.timed(args.warmup)
+    w.close()
+    run = M.Run(triple_point_spec(M, cycles=K + 8), ctx)
+    cells = 1792 * 768
+    l0 = run.kernel_launches
+    with Clocks(local) as clk:
+        ms = run.timed(K)
+    launches = run.kernel_launches - l0
+    prof = run.profile(4)
+    err = run.error()[0]
+    run.close()
+    kinds = {k: v for k, v in prof.items() if v[1] > 0}
+    cfg_run = M.Run(triple_point_spec(M, cycles=10, pb=1), ctx)
+    cfg_run.simulate()
+    code, cell = cfg_run.error()
+    configured = {"pente_borne": "mixte", "cycles_done": cfg_run.time()[2],
+                  "error_word": code, "error_cell": cell,
+                  "reference_behaviour": "cell--Nan 2, exit(1) in cycle 2"}
+    cfg_run.close()
+    out = {"value": cells * K / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / K,
+           "steps": K, "gpu_launches": launches, "error_word": err,
+           "clocks": clk.summary(), "config": EUC_WORKLOAD,
+           "configured_variant": configured,
+           "kernel_ms": {k: [round(v[0], 4), v[1]] for k, v in kinds.items()}}
+    if not args.no_cpu:
+        from oracle import port
+        pr = port.PortRun(triple_point_spec(M, cycles=1000))
+        pr.step(1)
+        n, t0 = 0, time.perf_counter()
+        while n < 20 and time.perf_counter() - t0 < 15.0:
+            pr.step(1)
+            n += 1
+        el = time.perf_counter() - t0
+        pr.close()
+        out["cpu_baseline"] = {"value": cells * n / el, "unit": UNIT,
+                               "cores": port.num_threads(), "kind": "port",
+                               "sample": f"{n} cycles of the 1792x768 triple point "
+                                         f"on {port.num_threads()} OpenMP threads, "
+                                         f"{el:.1f} s"}
+    return out
+
+
 def run_ours(args) -> None:
     rank, world, local = dist_env()
     if world > 1:
@@ -456,6 +538,7 @@ def run_ours(args) -> None:
         cfg["workload"] = cfg["workload"].replace("2048x2048", f"{n}x{n}")
     batched = None if args.no_batch else bench_batch(M, ctx, args, local)
     served = None if args.no_serve else bench_serve(M, args, local)
+    eucclhyd = None if args.no_euc else bench_euc(M, ctx, args, local)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
@@ -466,6 +549,7 @@ def run_ours(args) -> None:
         "kernel_ms": {k: [round(v[0], 4), v[1]] for k, v in kinds.items()},
         "batched": batched,
         "served": served,
+        "eucclhyd": eucclhyd,
     }
     print(json.dumps(line))
 
@@ -482,6 +566,8 @@ def main() -> None:
     ap.add_argument("--batch-n", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=40)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-euc", action="store_true")
+    ap.add_argument("--euc-steps", type=int, default=60)
     ap.add_argument("--serve-rates", default="50,200,1000,2000")
     ap.add_argument("--serve-n", type=int, default=24)
     ap.add_argument("--serve-timeout", type=float, default=120.0)

@@ -469,7 +469,9 @@ DV double fnv_horizontal(const RunView& v, long long na, long long nb) {
 struct FaceGrad {
   int sweep;
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
-    if (v.order <= 1) return;  // no slopes at order 1 (batched launches)
+    // no slopes at order 1, nor at order 3 without PenteBorne (batched
+    // launches; the plain cycle does not launch these then)
+    if (v.order <= 1 || (v.order == 3 && v.pb == 0)) return;
     const Ctrl& C = *v.ctrl;
     const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
     const long long P = v.pitch, FP = v.fpitch;
@@ -500,7 +502,9 @@ struct FaceGrad {
 struct SweepGrad {
   int sweep;
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
-    if (v.order <= 1) return;  // no slopes at order 1 (batched launches)
+    // no slopes at order 1, nor at order 3 without PenteBorne (batched
+    // launches; the plain cycle does not launch these then)
+    if (v.order <= 1 || (v.order == 3 && v.pb == 0)) return;
     const Ctrl& C = *v.ctrl;
     if (i >= v.ny || j >= v.nx) return;
     const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
@@ -719,11 +723,17 @@ struct SweepFace {
       const double vdt = fnv * C.dt_n;
       double h[6];
       for (int t = 0; t < 6; ++t) h[t] = H[cs[t]];
+      // every division of the order-3 value depends on the face only
+      const O3Face F = o3_face(h, vdt);
       for (int k = 0; k < ncomp; ++k) {
         double y[6];
-        for (int t = 0; t < 6; ++t) y[t] = Uin[k * P + cs[t]] / v.vL[cs[t]];
-        out[k * FP] = flux_ordre3(y[0], y[1], y[2], y[3], y[4], y[5], h[0], h[1],
-                                  h[2], h[3], h[4], h[5], vdt);
+        if (v.pb == 0) {
+          // U / vLagrange is what Phi holds without PenteBorne (same division)
+          for (int t = 0; t < 6; ++t) y[t] = v.Phi[k * P + cs[t]];
+        } else {
+          for (int t = 0; t < 6; ++t) y[t] = qdiv(Uin[k * P + cs[t]], v.vL[cs[t]]);
+        }
+        out[k * FP] = flux_ordre3_c(F, y);
       }
     }
   }
@@ -1343,7 +1353,8 @@ int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* 
   auto H = [&](int kind) {
     if (hook) (*hook)(kind);
   };
-  if (v.order > 1) {
+  // limited slopes feed the order-2 face values and PenteBorne only
+  if (v.order == 2 || (v.order == 3 && v.pb == 1)) {
     H(11); k_face_grad<<<fg, blk, 0, s>>>(v, sweep); ++nk;
     H(4); k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk;
   }

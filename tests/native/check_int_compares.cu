@@ -105,7 +105,28 @@ int main() {
         ++lbad;
       }
     }
-  printf("compares: %ld value pairs, %ld mismatches; limiter: %zu pairs, %ld mismatches\n",
-         n, bad, pairs.size(), lbad);
-  return (bad || lbad) ? 1 : 0;
+  // order-3 face value with hoisted face constants vs the direct form
+  long obad = 0, on = 0;
+  for (int it = 0; it < 200000; ++it) {
+    double h[6], y[6];
+    for (int t = 0; t < 6; ++t) {
+      h[t] = std::ldexp(1.0 + (double)(g() % 1000000) * 1e-6, -(int)(g() % 12));
+      y[t] = (g() % 7 == 0) ? 0.0 : ((double)(g() % 2000000) - 1e6) * 1e-6;
+    }
+    if (g() % 5 == 0) y[2] = y[3];
+    const double vdt = ((double)(g() % 2000001) - 1e6) * 1e-9 * (it % 3 ? 1.0 : 1e3);
+    const double want = flux_ordre3(y[0], y[1], y[2], y[3], y[4], y[5], h[0], h[1],
+                                    h[2], h[3], h[4], h[5], vdt);
+    const O3Face F = o3_face(h, vdt);
+    const double got = flux_ordre3_c(F, y);
+    ++on;
+    if (!same(got, want)) {
+      if (obad < 5) printf("order3 mismatch: got %.17g want %.17g\n", got, want);
+      ++obad;
+    }
+  }
+  printf("compares: %ld value pairs, %ld mismatches; limiter: %zu pairs, %ld mismatches; "
+         "order3: %ld faces, %ld mismatches\n",
+         n, bad, pairs.size(), lbad, on, obad);
+  return (bad || lbad || obad) ? 1 : 0;
 }

@@ -145,18 +145,24 @@ def test_gpu_triple_point_matches_port(order, pb, complet, M, ctx, port_lib):
         assert_bitwise(f, get_field(g, f, spec.nbmat), get_field(c, f, spec.nbmat))
 
 
-def test_gpu_triple_point_full_size_conserves_mass(M, ctx):
+def test_gpu_triple_point_full_size_matches_port(M, ctx, port_lib):
     """1792x768 triple point (the Eucclhyd workload: order-3 projection,
-    superBee), 20 cycles: total mass is conserved to 1e-12 relative,
-    velocities and densities stay finite."""
-    spec = triple_point(M, 1792, 768, 20)
+    superBee), 8 cycles: bit-identical to the C restatement at full size;
+    total mass moves by less than 1e-11 relative (the remap's volume
+    normalisation is not exactly conservative in the reference either)."""
+    from conftest import EUC_FIELDS
+    spec = triple_point(M, 1792, 768, 8)
     spec.pb = spec.pb_mixte = 0
     run = M.Run(spec, ctx)
     vol = 7.0 * 3.0 / (1792 * 768)
     m0 = run.fetch("density").sum() * vol
     run.simulate()
+    ref = port_lib.PortRun(spec)
+    ref.simulate()
+    assert run.time() == ref.time()
+    for f in EUC_FIELDS:
+        assert_bitwise(f, get_field(run, f, spec.nbmat), get_field(ref, f, spec.nbmat))
     m1 = run.fetch("density").sum() * vol
-    assert abs(m1 - m0) <= 1e-12 * m0
-    assert np.all(np.isfinite(run.fetch("cell_velocity")))
+    assert abs(m1 - m0) <= 1e-11 * m0
     assert run.error()[0] & ~M.ERR_NEGATIVE == 0
-    assert run.time()[2] == 20
+    assert run.time()[2] == 8

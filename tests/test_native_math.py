@@ -27,4 +27,5 @@ def test_integer_pipe_compares_and_limiter(tmp_path):
                     "-o", str(exe)], check=True, capture_output=True)
     res = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stdout + res.stderr
-    assert " 0 mismatches; limiter" in res.stdout and res.stdout.rstrip().endswith(" 0 mismatches")
+    assert " 0 mismatches; limiter" in res.stdout and " 0 mismatches; order3" in res.stdout
+    assert res.stdout.rstrip().endswith(" 0 mismatches")
