@@ -115,13 +115,30 @@ int hydro_run_create(hydro_ctx* ctx, const hydro_spec* spec, hydro_run** out);
 /* Advance at most ncycles cycles (stops early at final_time / max_cycles);
  * *done is set to 1 once the reference loop condition ends the run. */
 int hydro_run_step(hydro_run* run, int ncycles, int* done);
-/* Copy a named field (see hydro_run_field_size) into host memory. */
+/* Copy a named field (see hydro_run_field_size) into host memory.  Besides
+ * the full-state fields, the names the reference's dumpVariables gives its
+ * output variables fetch exactly what it writes at the start of the next
+ * cycle: "Pressure", "Density", "Energy", VNR "fracvol1", "fracvol2" (cell)
+ * and "VitesseX", "VitesseY" (node), Eucclhyd "F1".."F3", "VelocityX",
+ * "VelocityY" (vnr_remap/VnrRemap.cc:264-278, eucclhyd_remap/EucclhydRemap.cc
+ * :43-50). */
 int hydro_run_fetch(hydro_run* run, const char* field, double* host_dst,
                     size_t n);
 size_t hydro_run_field_size(hydro_run* run, const char* field);
 int hydro_run_time(hydro_run* run, double* t, double* dt, long* cycle);
 int hydro_run_error(hydro_run* run, unsigned* code, long* cell);
 int hydro_run_destroy(hydro_run* run);
+
+/* Output-driven stepping (the caller side of Vnr::dumpVariables,
+ * vnr_remap/VnrRemap.cc:255-287, and Eucclhyd::dumpVariables,
+ * eucclhyd_remap/EucclhydRemap.cc:24-64): advances at least one and at most
+ * ncycles cycles and stops before the first later cycle whose start time
+ * t_n satisfies t_n >= t_out || t_n == 0, the reference's dump condition with
+ * t_out = lastDump + output_time.  *paused = 1 when it stopped there (the
+ * caller writes its output, then calls again), *done = 1 when the run
+ * ended.  The test runs on the device, so no cycle waits for the host. */
+int hydro_run_step_to_output(hydro_run* run, int ncycles, double t_out,
+                             int* done, int* paused);
 
 /* Asynchronous form of hydro_run_step: enqueue cycles on the context's
  * stream; hydro_run_sync waits and reports whether the run has ended. */

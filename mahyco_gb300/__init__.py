@@ -102,6 +102,8 @@ def lib() -> C.CDLL:
         L.hydro_run_create.argtypes = [vp, C.POINTER(HydroSpec), C.POINTER(vp)]
         L.hydro_run_step.argtypes = [vp, i, C.POINTER(i)]
         L.hydro_run_enqueue.argtypes = [vp, i]
+        L.hydro_run_step_to_output.argtypes = [vp, i, C.c_double, C.POINTER(i),
+                                               C.POINTER(i)]
         L.hydro_run_sync.argtypes = [vp, C.POINTER(i)]
         L.hydro_run_fetch.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), sz]
         L.hydro_run_field_size.argtypes = [vp, C.c_char_p]
@@ -168,6 +170,63 @@ def parse_deck(path: str | os.PathLike) -> HydroSpec:
     _check(lib().hydro_spec_parse_deck(str(path).encode(), C.byref(s)),
            "hydro_spec_parse_deck")
     return s
+
+
+_CASE_NAMES = {0: "UnitTestCase", 1: "SedovTestCase", 2: "TriplePoint",
+               4: "SodCaseX", 5: "SodCaseY", 6: "NohTestCase", 7: "AdvectionX",
+               8: "AdvectionY", 9: "AdvectionVitX", 10: "AdvectionVitY",
+               11: "BiUnitTestCase", 12: "BiSedovTestCase", 13: "BiTriplePoint",
+               14: "BiShockBubble", 15: "BiSodCaseX", 16: "BiSodCaseY",
+               17: "BiNohTestCase", 18: "BiAdvectionX", 19: "BiAdvectionY",
+               20: "BiAdvectionVitX", 21: "BiAdvectionVitY"}
+
+
+def deck_text(spec: HydroSpec) -> str:
+    """The positional deck (key order of lecture_donnees/LectureDonnees.cc)
+    that parse_deck reads back into the same options: test case, mesh, times,
+    one EOS per material, scheme, orders, projection and limiter keys.  Only
+    what the deck format carries is written (no cycle cap, exponents, CFL or
+    init variant)."""
+    lim_name = {v: k for k, v in LIMITERS.items()}
+    on = lambda b: "oui" if b else "non"  # noqa: E731
+    lines = ["# Cas test", _CASE_NAMES[spec.test_case],
+             "# Nombre de Mailles en X", str(spec.nx),
+             "# Nombre de Mailles en Y", str(spec.ny),
+             "# DELTA_X", repr(spec.dx), "# DELTA_Y", repr(spec.dy),
+             "# temps final", repr(spec.final_time),
+             "# Temps entre deux sorties", repr(spec.output_time),
+             "# Pas de temps initial", repr(spec.dt_init),
+             "# Pas de temps minimal", repr(spec.dt_min)]
+    for m in range(spec.nbmat):
+        lines += ["# equation d'etat", "PerfectGas" if spec.eos[m] == 101 else "Void"]
+    lines += ["# schema Lagrange", "VNR" if spec.scheme == SCHEME_VNR else "Eucclhyd",
+              "# ordre en espace", str(spec.space_order),
+              "# avec projection", on(spec.projection),
+              "# projection conservative", on(spec.projection_conservative),
+              "# Limite fraction volumique", repr(spec.threshold),
+              "# Ordre de la projection", str(spec.projection_order),
+              "# Limiteurs", lim_name[spec.limiter],
+              "# option Pente Borne", on(spec.pb)]
+    if spec.pb:
+        lines += ["# Pente Borne mixte", on(spec.pb_mixte),
+                  "# limiteur mailles pures", lim_name.get(spec.limiter_pure, "minmod"),
+                  "# Pente Borne complet", on(spec.pb_complet)]
+    if spec.scheme == SCHEME_VNR:
+        lines += ["# pseudo_centree", on(spec.pseudo_centree)]
+        if spec.projection:
+            lines += ["# methode flux masse", ["A1", "A2", "PB"][spec.dual_mass_flux]]
+    return "\n".join(lines) + "\n"
+
+
+def write_deck(spec: HydroSpec, path: str | os.PathLike) -> None:
+    with open(path, "w") as f:
+        f.write(deck_text(spec))
+
+
+def driver_path() -> str:
+    """The drop-in command-line driver (mahyco_gb300_run <deck>)."""
+    from . import build as _b
+    return str(_b.OUT / "mahyco_gb300_run")
 
 
 class Context:
@@ -239,6 +298,16 @@ class Run:
         done = C.c_int(0)
         _check(lib().hydro_run_step(self.h, ncycles, C.byref(done)), "hydro_run_step")
         return bool(done.value)
+
+    def step_to_output(self, ncycles: int, t_out: float):
+        """Runs at least one and up to ncycles cycles, stopping before a
+        cycle whose start time t satisfies t >= t_out or t == 0 (the
+        reference's dump condition).  Returns (done, paused)."""
+        done, paused = C.c_int(0), C.c_int(0)
+        _check(lib().hydro_run_step_to_output(self.h, ncycles, t_out, C.byref(done),
+                                              C.byref(paused)),
+               "hydro_run_step_to_output")
+        return bool(done.value), bool(paused.value)
 
     def enqueue(self, ncycles: int) -> None:
         _check(lib().hydro_run_enqueue(self.h, ncycles), "hydro_run_enqueue")

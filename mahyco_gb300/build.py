@@ -2,7 +2,8 @@
 
   libmahyco_gb300.so  - the product: host runtime (C++) + sm_103a CUDA kernels,
                         exporting the C ABI of include/hydro_gb300.h
-  mahyco_gb300_run    - drop-in command-line driver (deck in, VTK out)
+  mahyco_gb300_run    - drop-in command-line driver (deck in, VTK out;
+                        tools_src/: driver.cc + the asynchronous VTK writer)
 
 Kernels are compiled for sm_103a only, with --fmad=false and IEEE division /
 square root so that FP64 results are bit-identical to the reference's
@@ -95,12 +96,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if force or jobs or not LIB.exists():
         _compile([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs),
                   "-lcudart"], OUT / "link.log")
-    drv_src = PKG / "tools_src" / "driver.cc"
-    if drv_src.exists():
+    tools = PKG / "tools_src"
+    drv_srcs = sorted(tools.glob("*.cc"))
+    if drv_srcs:
         drv = OUT / "mahyco_gb300_run"
-        if force or _newer(drv, [drv_src, LIB]):
-            _compile([os.environ.get("CXX", "g++"), *CXX_FLAGS, *_includes(),
-                      str(drv_src), "-o", str(drv), "-L", str(OUT),
+        if force or _newer(drv, [*drv_srcs, *tools.glob("*.h"), LIB]):
+            _compile([os.environ.get("CXX", "g++"), *CXX_FLAGS, "-pthread", *_includes(),
+                      "-I", str(tools), *map(str, drv_srcs), "-o", str(drv), "-L", str(OUT),
                       "-lmahyco_gb300", f"-Wl,-rpath,{OUT}"], OUT / "driver.log")
     if verbose:
         print(f"built {LIB}")

@@ -3,7 +3,9 @@
 // include/hydro_gb300.h.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -91,6 +93,7 @@ size_t layout(RunView& v, char* base) {
   if (v.scheme == HYDRO_SCHEME_EUCCLHYD) {
     v.cqs = v.cflsq = v.s0 = v.sqs0 = nullptr;
     v.uc = a.take<double>(2 * P);
+    v.uco = a.take<double>(2 * P);
     v.vg = a.take<double>(4 * P);
     v.Fs = a.take<double>(2 * nb * P);
     v.pex = a.take<double>(4 * P);
@@ -351,6 +354,7 @@ int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait) {
   rc = rc ? rc : upload(const_cast<double*>(v.nout), P, h.nout, nc, 4, nc, s);
   if (v.scheme == HYDRO_SCHEME_EUCCLHYD) {
     rc = rc ? rc : upload(v.uc, P, h.uc, nc, 2, nc, s);
+    rc = rc ? rc : upload(v.uco, P, h.uc, nc, 2, nc, s);
     rc = rc ? rc : upload(const_cast<double*>(v.lpc), P, h.lpc, nc, 8, nc, s);
     rc = rc ? rc : upload(const_cast<double*>(v.cmat), P, h.cmat, nc, 12, nc, s);
     rc = rc ? rc : upload(const_cast<double*>(v.xcc), P, h.xc, nc, 2, nc, s);
@@ -502,6 +506,57 @@ int hydro_run_step(hydro_run* r, int ncycles, int* done) {
   return 0;
 }
 
+// Arms or disarms the output pause in the device control block (stream
+// ordered, so it takes effect between cycles).
+static int set_pause(hydro_run* r, int on, double t_out) {
+  Ctrl& h = r->h_ctrl;
+  h.t_out = t_out;
+  h.pause = on;
+  h.pause_skip = on;
+  h.paused = 0;
+  static_assert(offsetof(Ctrl, pad3) == offsetof(Ctrl, t_out) + sizeof(double) + 3 * sizeof(int),
+                "pause fields are contiguous");
+  CUDA_TRY(cudaMemcpyAsync(&r->d_ctrl->t_out, &h.t_out,
+                           sizeof(double) + 3 * sizeof(int), cudaMemcpyHostToDevice,
+                           r->ctx->stream));
+  return 0;
+}
+
+int hydro_run_step_to_output(hydro_run* r, int ncycles, double t_out, int* done,
+                             int* paused) {
+  if (!r) return fail(-1, "null run");
+  if (ncycles < 1) return fail(-1, "hydro_run_step_to_output: ncycles < 1");
+  CUDA_TRY(cudaSetDevice(r->ctx->device));
+  if (int rc = sync_ctrl(r)) return rc;
+  if (done) *done = r->h_ctrl.done;
+  if (paused) *paused = 0;
+  if (r->h_ctrl.done) return 0;
+  if (int rc = set_pause(r, 1, t_out)) return rc;
+  int left = ncycles, rc = 0;
+  while (left > 0 && !rc) {
+    // cycles to the next output at the current time step (the step grows by
+    // at most 5% a cycle), so that few cycles are enqueued past the pause
+    const Ctrl& c = r->h_ctrl;
+    double est = 64.0;
+    if (c.dt_n > 0.0 && t_out > c.t_n) {
+      const double e = (t_out - c.t_n) / c.dt_n + 1.0;
+      if (e < est) est = e;
+    }
+    const int chunk = std::min(left, std::max(1, (int)est));
+    rc = hydro_run_enqueue(r, chunk);
+    if (!rc) rc = sync_ctrl(r);
+    left -= chunk;
+    if (!rc && (r->h_ctrl.done || r->h_ctrl.paused)) break;
+  }
+  const int was_paused = rc ? 0 : r->h_ctrl.paused;
+  const int rc2 = set_pause(r, 0, 0.0);
+  if (rc) return rc;
+  if (rc2) return rc2;
+  if (done) *done = r->h_ctrl.done;
+  if (paused) *paused = was_paused;
+  return 0;
+}
+
 int hydro_run_sync(hydro_run* r, int* done) {
   if (!r) return fail(-1, "null run");
   if (int rc = sync_ctrl(r)) return rc;
@@ -530,6 +585,76 @@ long long hydro_run_kernel_launches(hydro_run* r) {
   return r ? r->kernels_launched : 0;
 }
 
+// The variables the reference's dumpVariables hands to its VTK writer, by
+// the names it gives them (vnr_remap/VnrRemap.cc:264-278,
+// eucclhyd_remap/EucclhydRemap.cc:43-50).  Returns the material / component
+// index the name selects, -1 for other names.
+static int dump_plane(hydro_run* r, const char* f) {
+  static const char* common[] = {"Pressure", "Density", "Energy"};
+  for (auto n : common)
+    if (!strcmp(f, n)) return 0;
+  if (r->v.scheme == HYDRO_SCHEME_EUCCLHYD) {
+    static const char* euc[] = {"F1", "F2", "F3"};
+    for (int m = 0; m < 3; ++m)
+      if (!strcmp(f, euc[m])) return m;
+    if (!strcmp(f, "VelocityX")) return 0;
+    if (!strcmp(f, "VelocityY")) return 1;
+    return -1;
+  }
+  if (!strcmp(f, "fracvol1")) return 0;
+  if (!strcmp(f, "fracvol2")) return 1;
+  if (!strcmp(f, "VitesseX")) return 0;
+  if (!strcmp(f, "VitesseY")) return 1;
+  return -1;
+}
+static bool dump_on_nodes(hydro_run* r, const char* f) {
+  return r->v.scheme == HYDRO_SCHEME_VNR && (!strcmp(f, "VitesseX") || !strcmp(f, "VitesseY"));
+}
+
+// Copies one dump variable (see dump_plane) into dst.  Eucclhyd's Pressure
+// is the mean pressure of the current state as computeEOS +
+// computePressionMoyenne give it at the start of the next cycle, where the
+// reference dumps it; its VelocityX/Y are the clamped output velocities the
+// final remap kernel keeps.  Material slots beyond nbmat read as zero.
+static int fetch_dump(hydro_run* r, const char* f, int k, double* dst, size_t n) {
+  const RunView& v = r->v;
+  cudaStream_t s = r->ctx->stream;
+  const double* plane = nullptr;
+  double* scratch = nullptr;
+  const bool euc = v.scheme == HYDRO_SCHEME_EUCCLHYD;
+  if (!strcmp(f, "Density")) plane = v.rho;
+  else if (!strcmp(f, "Energy")) plane = v.e;
+  else if (!strcmp(f, "Pressure")) {
+    if (euc) {
+      CUDA_TRY(cudaMalloc(&scratch, v.nc * sizeof(double)));
+      launch_euc_out_pressure(v, scratch, s);
+      r->kernels_launched += 1;
+      plane = scratch;
+    } else {
+      plane = v.p;
+    }
+  } else if (!strcmp(f, "VelocityX") || !strcmp(f, "VelocityY")) {
+    plane = v.uco + k * v.pitch;
+  } else if (!strcmp(f, "VitesseX") || !strcmp(f, "VitesseY")) {
+    plane = v.u + k * v.npitch;
+  } else if (k < v.nbmat) {
+    plane = v.fm + k * v.pitch;
+  }
+  if (!plane) {
+    for (size_t i = 0; i < n; ++i) dst[i] = 0.0;
+    return 0;
+  }
+  cudaError_t e = cudaMemcpyAsync(dst, plane, n * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (scratch) {
+    const cudaError_t e2 = cudaFree(scratch);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e != cudaSuccess)
+    return fail(-100, std::string("fetch ") + f + ": " + cudaGetErrorString(e));
+  return 0;
+}
+
 size_t hydro_run_field_size(hydro_run* r, const char* f) {
   if (!r || !f) return 0;
   const size_t nc = (size_t)r->v.nc, nn = (size_t)r->v.nn;
@@ -542,6 +667,7 @@ size_t hydro_run_field_size(hydro_run* r, const char* f) {
   for (auto n : cell3)
     if (!strcmp(f, n)) return 3 * nc;
   if (!strcmp(f, "node_velocity")) return 2 * nn;
+  if (dump_plane(r, f) >= 0) return dump_on_nodes(r, f) ? nn : nc;
   if (r->v.scheme == HYDRO_SCHEME_EUCCLHYD) {
     if (!strcmp(f, "cell_velocity")) return 2 * nc;
     return 0;
@@ -567,6 +693,7 @@ int hydro_run_fetch(hydro_run* r, const char* f, double* dst, size_t n) {
     return cudaMemcpyAsync(out.data(), src, cnt * sizeof(double),
                            cudaMemcpyDeviceToHost, s);
   };
+  if (const int k = dump_plane(r, f); k >= 0) return fetch_dump(r, f, k, dst, n);
   std::vector<double> tmp;
   const double* one = nullptr;
   if (!strcmp(f, "density")) one = v.rho;

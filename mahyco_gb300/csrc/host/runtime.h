@@ -17,6 +17,7 @@ namespace hydro {
 void launch_prologue(const RunView& v, cudaStream_t s);
 int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook);
 void launch_node_mass(const RunView& v, cudaStream_t s);
+int launch_euc_out_pressure(const RunView& v, double* out, cudaStream_t s);
 int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s, const LaunchHook* hook);
 int batch_occupancy(int* blocks_per_sm);
 int measure_fp64_peak(int device, double* tflops);

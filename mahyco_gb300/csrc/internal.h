@@ -95,6 +95,9 @@ struct RunView {
   // ---- Eucclhyd (cell-centred velocity; all null for VNR runs)
   int space_order;
   double* uc;         // 2 cell planes: cell velocity
+  double* uco;        // 2 cell planes: the dumped cell velocity
+                      // (m_x/y_cell_velocity: clamped away from zero by the
+                      // threshold, kept when the velocity is exactly zero)
   double* vg;         // 4 cell planes: velocity gradient (row-major)
   double* Fs;         // 2 + 2*nbmat cell planes: sums of the cell's corner
                       // forces (total, then per material) of the last cycle
@@ -126,7 +129,33 @@ struct Ctrl {
   unsigned err;
   int pad2;
   long long err_cell;
+  // output pause (hydro_run_step_to_output): while `pause` is set, a cycle
+  // whose start time satisfies the dump condition does not run and `paused`
+  // is set; `pause_skip` lets the first cycle after arming run regardless
+  double t_out;
+  int pause, pause_skip, paused, pad3;
 };
+
+#ifdef __CUDACC__
+// The dump condition of Vnr::dumpVariables / Eucclhyd::dumpVariables
+// (vnr_remap/VnrRemap.cc:257-258, eucclhyd_remap/EucclhydRemap.cc:36-37),
+// t_n >= lastDump + output_time || t_n == 0, with t_out = lastDump +
+// output_time computed by the host.  Called by the cycle-start kernels;
+// true when this cycle must not run because the caller wants to write an
+// output at its start first.
+__device__ __forceinline__ bool output_pause_here(Ctrl& C) {
+  if (!C.pause) return false;
+  if (C.pause_skip) {
+    C.pause_skip = 0;
+    return false;
+  }
+  if (C.t_n >= C.t_out || C.t_n == 0.) {
+    C.paused = 1;
+    return true;
+  }
+  return false;
+}
+#endif
 
 // Per-kernel timing hook for launch_cycle.
 using LaunchHook = std::function<void(int)>;

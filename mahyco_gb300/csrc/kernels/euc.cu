@@ -84,6 +84,10 @@ __global__ void ke_begin(RunView v) {
     C.done = 1;
     return;
   }
+  if (output_pause_here(C)) {
+    C.active = 0;
+    return;
+  }
   C.active = 1;
   C.n += 1;
   C.dt_min_bits = ord_bits(1.7976931348623157e308);
@@ -109,6 +113,26 @@ __global__ void ke_end(RunView v) {
   if (C.err & ~HYDRO_ERR_NEGATIVE) C.done = 1;
 }
 
+// computeEOSGP / computeEOSVoid for material m of cell c (PhaseLagrange.cc
+// :70-109); the other EOS ids keep the stored values (their reference
+// routines only print).
+DV void cell_eos(const RunView& v, int m, long long c, double& pm, double& cm) {
+  const long long P = v.pitch;
+  const double rm = v.rhom[m * P + c], em = v.em[m * P + c];
+  const double g = gam(v, m);
+  const int eos = eosm(v, m);
+  if (eos == HYDRO_EOS_PERFECT_GAS) {
+    pm = (g - 1.0) * rm * em;
+    cm = pos(rm) ? sqrt(g * pm / rm) : 1.e-20;
+  } else if (eos == HYDRO_EOS_VOID) {
+    pm = 0.;
+    cm = 1.e-20;
+  } else {
+    pm = v.pm[m * P + c];
+    cm = v.cm[m * P + c];
+  }
+}
+
 // ------------------------------------------------- cell state of step n
 // computeEOS + computeEOSGP / computeEOSVoid (PhaseLagrange.cc:70-109),
 // computePressionMoyenne (:139-155), computeGradients (:160-246; the
@@ -125,19 +149,7 @@ struct EucCellPre {
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
-        const double rm = v.rhom[m * P + c], em = v.em[m * P + c];
-        const double g = gam(v, m);
-        const int eos = eosm(v, m);
-        if (eos == HYDRO_EOS_PERFECT_GAS) {
-          pm[m] = (g - 1.0) * rm * em;
-          cm[m] = pos(rm) ? sqrt(g * pm[m] / rm) : 1.e-20;
-        } else if (eos == HYDRO_EOS_VOID) {
-          pm[m] = 0.;
-          cm[m] = 1.e-20;
-        } else {
-          pm[m] = v.pm[m * P + c];
-          cm[m] = v.cm[m * P + c];
-        }
+        cell_eos(v, m, c, pm[m], cm[m]);
         v.pm[m * P + c] = pm[m];
         v.cm[m * P + c] = cm[m];
       }
@@ -623,6 +635,12 @@ struct EucFinal {
     v.uc[c] = un0;
     v.uc[P + c] = un1;
     v.e[c] = e;
+    // velocities for the outputs (PhaseRemapFinal.cc:200-213): kept where
+    // the velocity is zero, else pushed away from zero to the threshold
+    if (pos(un0)) v.uco[c] = smax(un0, thr);
+    else if (neg(un0)) v.uco[c] = smin(un0, -thr);
+    if (pos(un1)) v.uco[P + c] = smax(un1, thr);
+    else if (neg(un1)) v.uco[P + c] = smin(un1, -thr);
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
@@ -633,6 +651,22 @@ struct EucFinal {
     }
   }
 };
+
+// The mean pressure that Eucclhyd::dumpVariables writes: computeEOS +
+// computePressionMoyenne (PhaseLagrange.cc:70-155) on the current state,
+// i.e. what the next cycle's first kernel computes, into out[c].
+__global__ void __launch_bounds__(kBX* kBY) ke_out_pressure(RunView v, double* out) {
+  const int i = blockIdx.y * kBY + threadIdx.y, j = blockIdx.x * kBX + threadIdx.x;
+  if (i >= v.ny || j >= v.nx) return;
+  const long long c = (long long)i * v.nx + j;
+  double p = 0.;
+  for (int m = 0; m < v.nbmat; ++m) {
+    double pm, cm;
+    cell_eos(v, m, c, pm, cm);
+    p += v.fm[m * v.pitch + c] * pm;
+  }
+  out[c] = p;
+}
 
 template <class F>
 __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
@@ -646,6 +680,12 @@ __global__ void __launch_bounds__(kBX* kBY) ke_cells(RunView v) { plain_items(v,
 __global__ void __launch_bounds__(kBX* kBY) ke_final(RunView v) { plain_items(v, EucFinal{}); }
 
 }  // namespace
+
+int launch_euc_out_pressure(const RunView& v, double* out, cudaStream_t s) {
+  const dim3 cg((v.nx + kBX - 1) / kBX, (v.ny + kBY - 1) / kBY);
+  ke_out_pressure<<<cg, dim3(kBX, kBY), 0, s>>>(v, out);
+  return 1;
+}
 
 // One Eucclhyd cycle on stream s (kind ids: 0 begin, 12 cell_pre, 13 nodes,
 // 14 cells, sweeps, 15 final, 10 end).  Returns the number of kernels.

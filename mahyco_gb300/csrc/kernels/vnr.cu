@@ -54,6 +54,10 @@ __device__ __forceinline__ void begin_at(const RunView& v) {
     C.done = 1;
     return;
   }
+  if (output_pause_here(C)) {
+    C.active = 0;
+    return;
+  }
   C.active = 1;
   C.n += 1;
   if (v.sans_lagrange == 0) {

@@ -44,47 +44,7 @@ FIELDS_EUC = ["density", "pressure", "energy", "sound_speed", "cell_velocity",
               "density_env", "energy_env", "fracvol_env", "mass_fraction_env",
               "node_velocity"]
 
-LIM_NAME = {v: k for k, v in M.LIMITERS.items()}
-
-
-def write_deck(spec: M.HydroSpec, path: Path) -> None:
-    """Writes a positional deck (lecture_donnees/LectureDonnees.cc order)."""
-    case_names = {0: "UnitTestCase", 1: "SedovTestCase", 2: "TriplePoint",
-                  4: "SodCaseX", 5: "SodCaseY", 6: "NohTestCase",
-                  7: "AdvectionX", 8: "AdvectionY", 9: "AdvectionVitX",
-                  10: "AdvectionVitY", 11: "BiUnitTestCase",
-                  12: "BiSedovTestCase", 13: "BiTriplePoint",
-                  14: "BiShockBubble", 15: "BiSodCaseX", 16: "BiSodCaseY",
-                  17: "BiNohTestCase", 18: "BiAdvectionX", 19: "BiAdvectionY",
-                  20: "BiAdvectionVitX", 21: "BiAdvectionVitY"}
-    on = lambda b: "oui" if b else "non"  # noqa: E731
-    lines = ["# Cas test", case_names[spec.test_case],
-             "# Nombre de Mailles en X", str(spec.nx),
-             "# Nombre de Mailles en Y", str(spec.ny),
-             "# DELTA_X", repr(spec.dx), "# DELTA_Y", repr(spec.dy),
-             "# temps final", repr(spec.final_time),
-             "# Temps entre deux sorties", repr(spec.output_time),
-             "# Pas de temps initial", repr(spec.dt_init),
-             "# Pas de temps minimal", repr(spec.dt_min)]
-    for m in range(spec.nbmat):
-        lines += ["# equation d'etat", "PerfectGas" if spec.eos[m] == 101 else "Void"]
-    lines += ["# schema Lagrange", "VNR" if spec.scheme == 2001 else "Eucclhyd",
-              "# ordre en espace", str(spec.space_order),
-              "# avec projection", on(spec.projection),
-              "# projection conservative", on(spec.projection_conservative),
-              "# Limite fraction volumique", repr(spec.threshold),
-              "# Ordre de la projection", str(spec.projection_order),
-              "# Limiteurs", LIM_NAME[spec.limiter],
-              "# option Pente Borne", on(spec.pb)]
-    if spec.pb:
-        lines += ["# Pente Borne mixte", on(spec.pb_mixte),
-                  "# limiteur mailles pures", LIM_NAME.get(spec.limiter_pure, "minmod"),
-                  "# Pente Borne complet", on(spec.pb_complet)]
-    if spec.scheme == 2001:
-        lines += ["# pseudo_centree", on(spec.pseudo_centree)]
-        if spec.projection:
-            lines += ["# methode flux masse", ["A1", "A2", "PB"][spec.dual_mass_flux]]
-    path.write_text("\n".join(lines) + "\n")
+write_deck = M.write_deck
 
 
 def run_reference(deck: Path, cycles: int = 0, extra=(), fields=FIELDS) -> dict:
