@@ -118,17 +118,6 @@ size_t layout(RunView& v, char* base) {
   return a.off + 256;
 }
 
-// Copies nplanes host planes of n values (host stride hs) into device planes
-// of stride ds.
-int upload(double* dst, long long ds, const std::vector<double>& src,
-           long long hs, int nplanes, long long n, cudaStream_t s) {
-  for (int k = 0; k < nplanes; ++k)
-    CUDA_TRY(cudaMemcpyAsync(dst + k * ds, src.data() + k * hs,
-                             (size_t)n * sizeof(double),
-                             cudaMemcpyHostToDevice, s));
-  return 0;
-}
-
 int validate(const hydro_spec& s) {
   if (s.scheme != HYDRO_SCHEME_VNR && s.scheme != HYDRO_SCHEME_EUCCLHYD)
     return fail(-20, "unknown Lagrange scheme");
@@ -200,9 +189,7 @@ int prepare_run(const hydro_spec& spec_in, PreparedRun& pr) {
   pr.spec = spec_in;
   const hydro_spec* spec = &pr.spec;
   const bool euc = spec->scheme == HYDRO_SCHEME_EUCCLHYD;
-  if (int rc = euc ? build_initial_state_euc(*spec, pr.h)
-                   : build_initial_state(*spec, pr.h))
-    return rc;
+  if (int rc = euc ? init_options_euc(*spec, pr.h) : init_options(*spec, pr.h)) return rc;
   const HostInit& h = pr.h;
   RunView& v = pr.v;
   v = RunView{};
@@ -289,11 +276,12 @@ size_t run_arena_bytes(const hydro_spec& spec) {
   return layout(v, nullptr);
 }
 
-// Device part: allocates the run's arena, uploads the prepared state on the
-// context's stream and queues the prologue.  With wait, returns after the
-// upload has finished; without, the caller orders later work on the same
-// stream (the host copies are staged before this returns, so `pr` may be
-// released at once).
+// Device part: allocates the run's arena and queues, on the context's
+// stream, its clearing, the control block's upload, the device kernels that
+// build the initial state and geometry, and the prologue.  With wait,
+// returns once they have run; without, the caller orders later work on the
+// same stream (the control block is staged before this returns, so `pr` may
+// be released at once).
 int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait) {
   CUDA_TRY(cudaSetDevice(ctx->device));
   const size_t bytes = pr.bytes;
@@ -324,60 +312,8 @@ int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait) {
   r->d_ctrl = v.ctrl;
   cudaStream_t s = ctx->stream;
   int rc = 0;
-  auto cp = [&](const double* dst, const std::vector<double>& src) {
-    if (rc) return;
-    cudaError_t ee = cudaMemcpyAsync((void*)dst, src.data(),
-                                     src.size() * sizeof(double),
-                                     cudaMemcpyHostToDevice, s);
-    if (ee != cudaSuccess) rc = fail(-32, cudaGetErrorString(ee));
-  };
   if (cudaMemsetAsync(r->arena, 0, bytes, s) != cudaSuccess)
     rc = fail(-32, "arena clear");
-  const long long nc = h.nc, nn = h.nn, P = v.pitch, NP = v.npitch;
-  const int nb = v.nbmat;
-  rc = rc ? rc : upload(v.rho, P, h.rho, nc, 1, nc, s);
-  rc = rc ? rc : upload(v.p, P, h.p, nc, 1, nc, s);
-  rc = rc ? rc : upload(v.c, P, h.c, nc, 1, nc, s);
-  rc = rc ? rc : upload(v.e, P, h.e, nc, 1, nc, s);
-  rc = rc ? rc : upload(v.q, P, h.q, nc, 1, nc, s);
-  rc = rc ? rc : upload(v.divu, P, h.divu, nc, 1, nc, s);
-  rc = rc ? rc : upload(v.cell_mass, P, h.cell_mass, nc, 1, nc, s);
-  rc = rc ? rc : upload(v.rhom, P, h.rhom, nc, nb, nc, s);
-  rc = rc ? rc : upload(v.pm, P, h.pm, nc, nb, nc, s);
-  rc = rc ? rc : upload(v.cm, P, h.cm, nc, nb, nc, s);
-  rc = rc ? rc : upload(v.em, P, h.em, nc, nb, nc, s);
-  rc = rc ? rc : upload(v.qm, P, h.qm, nc, nb, nc, s);
-  rc = rc ? rc : upload(v.fm, P, h.fm, nc, nb, nc, s);
-  rc = rc ? rc : upload(v.mfm, P, h.mfm, nc, nb, nc, s);
-  rc = rc ? rc : upload(v.cmassm, P, h.cmassm, nc, nb, nc, s);
-  rc = rc ? rc : upload(v.u, NP, h.u, nn, 2, nn, s);
-  rc = rc ? rc : upload(const_cast<double*>(v.nout), P, h.nout, nc, 4, nc, s);
-  if (v.scheme == HYDRO_SCHEME_EUCCLHYD) {
-    rc = rc ? rc : upload(v.uc, P, h.uc, nc, 2, nc, s);
-    rc = rc ? rc : upload(v.uco, P, h.uc, nc, 2, nc, s);
-    rc = rc ? rc : upload(const_cast<double*>(v.lpc), P, h.lpc, nc, 8, nc, s);
-    rc = rc ? rc : upload(const_cast<double*>(v.cmat), P, h.cmat, nc, 12, nc, s);
-    rc = rc ? rc : upload(const_cast<double*>(v.xcc), P, h.xc, nc, 2, nc, s);
-    cp(v.perim, h.perim);
-    cp(v.evol, h.evol);
-  } else {
-    rc = rc ? rc : upload(const_cast<double*>(v.cqs), P, h.cqs, nc, 8, nc, s);
-    cp(v.cflsq, h.cflsq);
-    cp(v.s0, h.s0);
-    cp(v.sqs0, h.sqs0);
-  }
-  cp(v.xs, h.xs);
-  cp(v.ys, h.ys);
-  cp(v.flv, h.flv);
-  cp(v.flh, h.flh);
-  cp(v.rho0_left, h.rho0_left);
-  cp(v.node_mass, h.node_mass);
-  if (!rc &&
-      (cudaMemcpyAsync(v.mixte, h.mixte.data(), nc * sizeof(int),
-                       cudaMemcpyHostToDevice, s) != cudaSuccess ||
-       cudaMemcpyAsync(v.pure, h.pure.data(), nc * sizeof(int),
-                       cudaMemcpyHostToDevice, s) != cudaSuccess))
-    rc = fail(-32, "flag upload");
   Ctrl c0{};
   c0.t_n = 0.0;
   c0.dt_n = h.dt_init;
@@ -390,10 +326,12 @@ int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait) {
   c0.dt_min_bits = 0xFFEFFFFFFFFFFFFFull;  // ordered encoding of +DBL_MAX
   c0.pmax_bits = 0x0010000000000000ull;    // ordered encoding of -DBL_MAX
   r->h_ctrl = c0;
-  // the control block goes through the pageable path too (staged at once)
+  // the control block is the only host -> device copy (pageable, staged at
+  // once); the initial state is built in place by the device
   if (!rc && cudaMemcpyAsync(r->d_ctrl, &r->h_ctrl, sizeof(Ctrl),
                              cudaMemcpyHostToDevice, s) != cudaSuccess)
     rc = fail(-33, "ctrl upload");
+  if (!rc) launch_device_init(v, pr.spec.test_case, pr.spec.init_variant, s);
   if (!rc && v.scheme == HYDRO_SCHEME_VNR) launch_prologue(v, s);
   if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(-34, "prologue launch");
   if (!rc && wait && cudaStreamSynchronize(s) != cudaSuccess)

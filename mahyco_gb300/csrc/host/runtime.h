@@ -15,6 +15,7 @@
 namespace hydro {
 
 void launch_prologue(const RunView& v, cudaStream_t s);
+int launch_device_init(const RunView& v, int test_case, int init_variant, cudaStream_t s);
 int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook);
 void launch_node_mass(const RunView& v, cudaStream_t s);
 int launch_euc_out_pressure(const RunView& v, double* out, cudaStream_t s);
