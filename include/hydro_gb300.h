@@ -140,6 +140,15 @@ int hydro_run_destroy(hydro_run* run);
 int hydro_run_step_to_output(hydro_run* run, int ncycles, double t_out,
                              int* done, int* paused);
 
+/* Checkpoint / restart (no counterpart in the reference).  A checkpoint,
+ * taken between cycles, holds the run's options and its whole device state
+ * (fields, control block with time, dt, cycle count and error word); a
+ * restored run continues bit for bit as the original.  Files are tied to the
+ * library's memory layout (rejected otherwise) and carry a content hash
+ * (truncated or corrupted files are rejected). */
+int hydro_run_checkpoint(hydro_run* run, const char* path);
+int hydro_run_restore(hydro_ctx* ctx, const char* path, hydro_run** out);
+
 /* Asynchronous form of hydro_run_step: enqueue cycles on the context's
  * stream; hydro_run_sync waits and reports whether the run has ended. */
 int hydro_run_enqueue(hydro_run* run, int ncycles);

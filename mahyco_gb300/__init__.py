@@ -102,6 +102,8 @@ def lib() -> C.CDLL:
         L.hydro_run_create.argtypes = [vp, C.POINTER(HydroSpec), C.POINTER(vp)]
         L.hydro_run_step.argtypes = [vp, i, C.POINTER(i)]
         L.hydro_run_enqueue.argtypes = [vp, i]
+        L.hydro_run_checkpoint.argtypes = [vp, C.c_char_p]
+        L.hydro_run_restore.argtypes = [vp, C.c_char_p, C.POINTER(vp)]
         L.hydro_run_step_to_output.argtypes = [vp, i, C.c_double, C.POINTER(i),
                                                C.POINTER(i)]
         L.hydro_run_sync.argtypes = [vp, C.POINTER(i)]
@@ -298,6 +300,25 @@ class Run:
         done = C.c_int(0)
         _check(lib().hydro_run_step(self.h, ncycles, C.byref(done)), "hydro_run_step")
         return bool(done.value)
+
+    def checkpoint(self, path: str | os.PathLike) -> None:
+        """Writes the run's options and device state to path (between
+        cycles); Run.restore continues it bit for bit."""
+        _check(lib().hydro_run_checkpoint(self.h, os.fspath(path).encode()),
+               "hydro_run_checkpoint")
+
+    @classmethod
+    def restore(cls, path: str | os.PathLike, ctx: "Context | None" = None) -> "Run":
+        ctx = ctx or default_context()
+        h = C.c_void_p()
+        _check(lib().hydro_run_restore(ctx.h, os.fspath(path).encode(), C.byref(h)),
+               "hydro_run_restore")
+        with open(path, "rb") as f:  # the options follow the 64-byte header
+            f.seek(64)
+            spec = HydroSpec.from_buffer_copy(f.read(C.sizeof(HydroSpec)))
+        r = cls.borrowed(h.value, spec, ctx)
+        r.owner = True
+        return r
 
     def step_to_output(self, ncycles: int, t_out: float):
         """Runs at least one and up to ncycles cycles, stopping before a

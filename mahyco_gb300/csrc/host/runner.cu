@@ -282,7 +282,7 @@ size_t run_arena_bytes(const hydro_spec& spec) {
 // returns once they have run; without, the caller orders later work on the
 // same stream (the control block is staged before this returns, so `pr` may
 // be released at once).
-int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait) {
+int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait, bool build_state) {
   CUDA_TRY(cudaSetDevice(ctx->device));
   const size_t bytes = pr.bytes;
   {
@@ -328,11 +328,12 @@ int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait) {
   r->h_ctrl = c0;
   // the control block is the only host -> device copy (pageable, staged at
   // once); the initial state is built in place by the device
-  if (!rc && cudaMemcpyAsync(r->d_ctrl, &r->h_ctrl, sizeof(Ctrl),
-                             cudaMemcpyHostToDevice, s) != cudaSuccess)
+  if (!rc && build_state &&
+      cudaMemcpyAsync(r->d_ctrl, &r->h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess)
     rc = fail(-33, "ctrl upload");
-  if (!rc) launch_device_init(v, pr.spec.test_case, pr.spec.init_variant, s);
-  if (!rc && v.scheme == HYDRO_SCHEME_VNR) launch_prologue(v, s);
+  if (!rc && build_state) launch_device_init(v, pr.spec.test_case, pr.spec.init_variant, s);
+  if (!rc && build_state && v.scheme == HYDRO_SCHEME_VNR) launch_prologue(v, s);
   if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(-34, "prologue launch");
   if (!rc && wait && cudaStreamSynchronize(s) != cudaSuccess)
     rc = fail(-34, std::string("initial upload: ") +

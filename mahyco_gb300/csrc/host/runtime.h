@@ -41,7 +41,10 @@ struct PreparedRun {
   size_t bytes = 0;
 };
 int prepare_run(const hydro_spec& spec, PreparedRun& out);
-int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait);
+// build_state = false leaves the cleared arena for the caller to fill (a
+// restart from a checkpoint)
+int place_run(hydro_ctx* ctx, PreparedRun& pr, hydro_run** out, bool wait,
+              bool build_state = true);
 size_t run_arena_bytes(const hydro_spec& spec);
 
 struct BatchPlan;
