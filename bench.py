@@ -13,7 +13,7 @@ cycle streams it from HBM.
              state resident in HBM
   e2e        the same work through the C ABI with host buffers: run
              creation from the options (the initial state is built on the
-             device; the host uploads the 120-byte control block), K cycles,
+             device; the host uploads the 128-byte control block), K cycles,
              fetch of the final fields (device->host)
   roofline   the dominant kernel's algorithmic bytes / measured launch time
              against the measured HBM copy bandwidth, plus its FP64 rate
@@ -39,7 +39,7 @@ import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
-CTRL_BYTES = 120  # the run's control block, the one host->device copy of creation
+CTRL_BYTES = 128  # the run's control block, the one host->device copy of creation
 sys.path.insert(0, str(ROOT))
 
 METRIC = "FP64 cell-updates/s on 1 GB300 batched/served vs plain GPU vs CPU; p50/p99"

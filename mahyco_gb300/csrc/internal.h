@@ -134,6 +134,7 @@ struct Ctrl {
   // is set; `pause_skip` lets the first cycle after arming run regardless
   double t_out;
   int pause, pause_skip, paused, pad3;
+  double rdt_np1;  // 1.0 / dt_np1, formed once per cycle (VNR divergence)
 };
 
 #ifdef __CUDACC__

@@ -67,6 +67,7 @@ __device__ __forceinline__ void begin_at(const RunView& v) {
     C.dt_np1 = C.dt_n;
   }
   C.t_np1 = C.t_n + C.dt_np1;
+  C.rdt_np1 = 1.0 / C.dt_np1;
 }
 
 __device__ __forceinline__ void reset_at(const RunView& v) {
@@ -322,7 +323,7 @@ struct LagCells {
     if (v.sans_lagrange == 0) {
       const double rho_old = v.rho[c];
       const double tau = 0.5 * (1.0 / rho_new + 1.0 / rho_old);
-      const double divu_new = 1.0 / C.dt_np1 * (1.0 / rho_new - 1.0 / rho_old) / tau;
+      const double divu_new = C.rdt_np1 * (1.0 / rho_new - 1.0 / rho_old) / tau;
       const double c_old = v.c[c];
       if (neg(v.divu[c])) {
         const double s0 = ld(v.s0, c);
@@ -495,7 +496,16 @@ struct FaceGrad {
       ax = 1;
     }
     const double dx = (v.XcL[ax * P + front] - v.XcL[ax * P + back]) + 0.0;
-    for (int k = 0; k < v.ncomp; ++k)
+    // with PenteBorne only the integrated components' slopes are read (see
+    // SweepGrad): the most any cell integrates
+    int nk = v.ncomp;
+    if (v.pb == 1) {
+      const int nb = v.nbmat;
+      const bool euc = (v.scheme == HYDRO_SCHEME_EUCCLHYD);
+      nk = (v.pb_complet == 1) ? (euc ? v.ncomp : 3 * nb) : (v.pb_mixte == 1 ? 2 * nb : nb);
+      if (!euc && v.dual_method == 2 && nk < 2 * nb) nk = 2 * nb;
+    }
+    for (int k = 0; k < nk; ++k)
       v.phiF[k * FP + fidx] = qdiv(v.Phi[k * P + front] - v.Phi[k * P + back], dx);
   }
 };
@@ -548,8 +558,20 @@ struct SweepGrad {
     const long long cp = dirx ? cf : cb, cm = dirx ? cb : cf;
     const double h0 = H[c], hp = H[cp], hm = H[cm];
     const int ncomp = v.ncomp, nb = v.nbmat;
+    // Eucclhyd carries momentum (and kinetic energy) after the material
+    // components instead of the VNR pseudo-viscosity, and has no dual remap
+    const bool euc = (v.scheme == HYDRO_SCHEME_EUCCLHYD);
+    const bool cfd = !euc && (v.dual_method == 2);
+    // which components are integrated with PenteBorne: volumes always;
+    // masses for the pure variant; masses + energies (+ momentum for
+    // Eucclhyd) for the "complet" variant; the dual flux needs the mass
+    // components (computeFluxPP, UtilesRemap-Impl.h:259-313).  Only their
+    // limited slopes are read; without PenteBorne every slope is stored.
+    const int nint = (v.pb_complet == 1) ? (euc ? ncomp : 3 * nb) : (vp ? 2 * nb : nb);
+    const int nuse = (cfd && nint < 2 * nb) ? 2 * nb : nint;
+    const int ngrad = (v.pb == 1) ? nuse : ncomp;
     double grad[kMaxComp];
-    for (int k = 0; k < ncomp; ++k) {
+    for (int k = 0; k < ngrad; ++k) {
       const double y0 = v.Phi[k * P + c];
       const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
       const double gp = has_gp ? v.phiF[k * FP + fp_idx] : 0.;
@@ -579,17 +601,7 @@ struct SweepGrad {
       const double ppa = 0.5 * (Fa + fabs(Fa)) * dt;
       const double ppb = 0.5 * (Fb + fabs(Fb)) * dt;
       const double ppd = 0.5 * (fdual + fabs(fdual)) * dt;
-      // Eucclhyd carries momentum (and kinetic energy) after the material
-      // components instead of the VNR pseudo-viscosity, and has no dual remap
-      const bool euc = (v.scheme == HYDRO_SCHEME_EUCCLHYD);
-      const bool cfd = !euc && (v.dual_method == 2);
       const int plim = vp ? v.limiter_pure : v.limiter;
-      // which components are integrated: volumes always; masses for the pure
-      // variant; masses + energies (+ momentum for Eucclhyd) for the
-      // "complet" variant; the dual flux needs the mass components
-      // (computeFluxPP, UtilesRemap-Impl.h:259-313)
-      const int nint = (v.pb_complet == 1) ? (euc ? ncomp : 3 * nb) : (vp ? 2 * nb : nb);
-      const int nuse = (cfd && nint < 2 * nb) ? 2 * nb : nint;
       double Fr[kMaxComp], Fv[kMaxComp];
       const double hh = h0;
       for (int k = 0; k < nuse; ++k) {
