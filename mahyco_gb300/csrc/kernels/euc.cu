@@ -340,8 +340,8 @@ struct EucNodes {
         if (fabs(fabs(dot2(A0, A1, B0, B1)) - na * nbb) < 1.0E-8)
           bc_velocity(kBcSym, A0, A1, Mp, G, u0, u1);
       } else if (b1 == kBcImposed && b2 == kBcImposed) {
-        u0 = 0.5 * (A0 + B0);
-        u1 = 0.5 * (A1 + B1);
+        u0 = half(A0 + B0);
+        u1 = half(A1 + B1);
       } else if (b1 == 202 && b2 == 202) {
         bc_velocity(202, A0, A1, Mp, G, u0, u1);
       }
@@ -388,7 +388,7 @@ struct EucCells {
       const int kp = (k + 1) & 3;
       r6 = r6 + cross2(X[k][0], X[k][1], X[kp][0], X[kp][1]);
     }
-    const double vol = 0.5 * r6;
+    const double vol = half(r6);
     v.vL[c] = vol;
     double r7a = 0.0, r7b = 0.0;
 #pragma unroll
@@ -407,11 +407,11 @@ struct EucCells {
         return sqrt(dot2(d0, d1, d0, d1));
       };
       double hx = 0.;
-      hx += 0.5 * len(0, 1);
-      hx += 0.5 * len(3, 2);
+      hx += half(len(0, 1));
+      hx += half(len(3, 2));
       double hy = 0.;
-      hy += 0.5 * len(1, 2);
-      hy += 0.5 * len(0, 3);
+      hy += half(len(1, 2));
+      hy += half(len(0, 3));
       v.Hx[c] = hx;
       v.Hy[c] = hy;
     }
@@ -457,7 +457,7 @@ struct EucCells {
     const double uc0 = v.uc[c], uc1 = v.uc[P + c];
     const double uL0 = uc0 + r3a * dt / cmass;
     const double uL1 = uc1 + r3b * dt / cmass;
-    const double mid0 = (uc0 + uL0) * 0.5, mid1 = (uc1 + uL1) * 0.5;
+    const double mid0 = half(uc0 + uL0), mid1 = half(uc1 + uL1);
     double pr4[3] = {0.0, 0.0, 0.0}, fsa[3] = {0.0, 0.0, 0.0}, fsb[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {

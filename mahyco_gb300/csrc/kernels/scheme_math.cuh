@@ -144,6 +144,68 @@ HD double twice(double x) {
   return from_bits((b & ~kMag) | m2);
 }
 
+// x * 2^-K (K = 1: x * 0.5, K = 2: x * 0.25), exactly as the IEEE product,
+// on the integer pipe: when the result is normal only the exponent field
+// changes.  The rest (results in the subnormal range: the significand shifts
+// with round-to-nearest-even; infinities and NaNs: the FP64 multiply) is the
+// out-of-line slow path.
+template <int K>
+HD double mul_pow2m_slow(double x) {
+  const unsigned long long b = ubits(x), m = b & kMag, e = m >> 52;
+  if (e == 0x7ffull) return x * (K == 1 ? 0.5 : 0.25);
+  // value = sig * 2^-1074 * 2^(e ? e - 1 : 0); result = value * 2^-K
+  const unsigned long long sig = e ? ((m & 0xfffffffffffffull) | (1ull << 52)) : m;
+  const int sh = e ? (K + 1 - (int)e) : K;  // 1 .. K
+  const unsigned long long q = sig >> sh, r = sig & ((1ull << sh) - 1);
+  const unsigned long long hw = 1ull << (sh - 1);
+  const unsigned long long qq = q + ((r > hw || (r == hw && (q & 1ull))) ? 1ull : 0ull);
+  return from_bits((b & ~kMag) | qq);
+}
+#ifdef __CUDA_ARCH__
+template <int K>
+static __device__ __noinline__ double mul_pow2m_call(double x) { return mul_pow2m_slow<K>(x); }
+#else
+template <int K>
+static inline double mul_pow2m_call(double x) { return mul_pow2m_slow<K>(x); }
+#endif
+template <int K>
+HD double mul_pow2m(double x) {
+  const unsigned long long b = ubits(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (e - (unsigned)(K + 1) < 0x7feu - (unsigned)K)  // K < e < 0x7ff
+    return from_bits(b - ((unsigned long long)K << 52));
+  return mul_pow2m_call<K>(x);
+}
+HD double half(double x) { return mul_pow2m<1>(x); }
+HD double quarter(double x) { return mul_pow2m<2>(x); }
+// 2 * x for any x: exponent + 1 while the result stays finite and normal;
+// zeros, subnormals, overflow, infinities and NaNs through twice / the FP64
+// multiply
+#ifdef __CUDA_ARCH__
+static __device__ __noinline__ double dbl_slow(double x) { return is_nan(x) ? 2.0 * x : twice(x); }
+#else
+static inline double dbl_slow(double x) { return is_nan(x) ? 2.0 * x : twice(x); }
+#endif
+HD double dbl(double x) {
+  const unsigned long long b = ubits(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (e - 1u < 0x7fdu) return from_bits(b + (1ull << 52));  // 1 <= e <= 0x7fd
+  return dbl_slow(x);
+}
+// x + 0.0 (turns -0 into +0; NaN through the FP64 addition)
+HD double plus_zero(double x) {
+  const unsigned long long b = ubits(x);
+  if (b == 0x8000000000000000ull) return 0.0;
+  return is_nan(x) ? x + 0.0 : x;
+}
+// k * x for a small integer k in {0, 1, 2} (k = 0: the IEEE product's signed
+// zero, or NaN for a non-finite x)
+HD double mul_012(int k, double x) {
+  if (k == 1) return x;
+  if (k == 2) return dbl(x);
+  return is_finite(x) ? from_bits(ubits(x) & ~kMag) : 0.0 * x;
+}
+
 // minmod / superBee limiter of a quotient that is not NaN, with the
 // comparisons on the integer pipe (same values as flux_limiter).
 HD double flux_limiter_q(int id, double r) {
@@ -177,8 +239,8 @@ HD double flux_limiter_pp(int id, double gp, double gm, double yp, double ym,
   } else if (id == HYDRO_LIM_SUPERBEEG) {
     grady = pos(yp - ym) ? smax(fabs(gp), fabs(gm)) : -smax(fabs(gp), fabs(gm));
   } else if (id == HYDRO_LIM_VANLEERG) {
-    double lp = (h0 * 0.5 + hp) / (h0 + hp + hm);
-    double lm = (h0 * 0.5 + hm) / (h0 + hp + hm);
+    double lp = (half(h0) + hp) / (h0 + hp + hm);
+    double lm = (half(h0) + hm) / (h0 + hp + hm);
     if (nz(lp * gp + lm * gm))
       grady = gp * gm / (lp * gp + lm * gm);
     else
@@ -186,8 +248,8 @@ HD double flux_limiter_pp(int id, double gp, double gm, double yp, double ym,
   } else if (id == HYDRO_LIM_ULTRABEEG) {
     grady = (yp - ym) / h0;
   } else if (id == HYDRO_LIM_ARITHMETICG) {
-    double lp = (h0 * 0.5 + hp) / (h0 + hp + hm);
-    double lm = (h0 * 0.5 + hm) / (h0 + hp + hm);
+    double lp = (half(h0) + hp) / (h0 + hp + hm);
+    double lm = (half(h0) + hm) / (h0 + hp + hm);
     grady = lm * gp + lp * gm;
   }
   double gMp = gp * (h0 + hp) / h0;
@@ -269,7 +331,7 @@ HD double limit_grad1(int id, double gp, double gm, double yp, double ym,
     const double phi = flux_limiter_q(id, qdiv(num, den));
     const double f1 = (which == 1) ? phi : c1;
     const double f2 = (which == 2) ? phi : c2;
-    return (f1 * gm + f2 * gp) * 0.5;
+    return half(f1 * gm + f2 * gp);
   }
   return (flux_limiter(id, divide_no_except(gp, gm)) * gm +
           flux_limiter(id, divide_no_except(gm, gp)) * gp) *
@@ -285,8 +347,8 @@ HD void compute_y0(int id, double yp, double ym, double h0, double hp,
     y0p = yp;
     y0m = ym;
   } else if (id == HYDRO_LIM_SUPERBEEG || id == HYDRO_LIM_SUPERBEE) {
-    y0p = ((h0 + hm) * yp + h0 * ym) / (2 * h0 + hm);
-    y0m = ((h0 + hp) * ym + h0 * yp) / (2 * h0 + hp);
+    y0p = ((h0 + hm) * yp + h0 * ym) / (dbl(h0) + hm);
+    y0m = ((h0 + hp) * ym + h0 * yp) / (dbl(h0) + hp);
   } else if (id == HYDRO_LIM_VANLEERG || id == HYDRO_LIM_VANLEER) {
     double a = smin(yp, ym);
     double b = smax(yp, ym);
@@ -299,11 +361,11 @@ HD void compute_y0(int id, double yp, double ym, double h0, double hp,
     y0p = smin(smax(xp, a), b);
     y0m = smin(smax(xm, a), b);
   } else if (id == HYDRO_LIM_ULTRABEEG) {
-    y0p = (yp + ym) * 0.5;
-    y0m = (yp + ym) * 0.5;
+    y0p = half(yp + ym);
+    y0m = half(yp + ym);
   } else if (id == HYDRO_LIM_ARITHMETICG) {
-    y0p = ((h0 + hm + hp) * yp + h0 * ym) / (2 * h0 + hm + hp);
-    y0m = ((h0 + hm + hp) * ym + h0 * yp) / (2 * h0 + hm + hp);
+    y0p = ((h0 + hm + hp) * yp + h0 * ym) / (dbl(h0) + hm + hp);
+    y0m = ((h0 + hm + hp) * ym + h0 * yp) / (dbl(h0) + hm + hp);
   } else if (id == 3000) {
     y0p = yp;
     y0m = ym;
@@ -328,7 +390,7 @@ HD double int2y(double X, double x0, double y0, double x1, double y1) {
       eta = 1.;
     else
       eta = smin(smax(0., ddiv_call(n, d)), 1.);
-    flux = (y0 + 0.5 * eta * (y1 - y0)) * d * eta;
+    flux = (y0 + half(eta) * (y1 - y0)) * d * eta;
   }
   return flux;
 }
@@ -348,12 +410,12 @@ HD PPShape pp_shape(int lim, double thr, double y0, double yp, double ym,
   PPShape s;
   s.xd = +h0 * smin(smax(xp, -0.5), 0.5);
   s.xg = -h0 * smin(smax(xm, -0.5), 0.5);
-  double xtd = y0 + h0 * 0.5 * grad;
-  double xtg = y0 - h0 * 0.5 * grad;
-  double ad = smin(yp, 2. * y0m - ym);
-  double bd = smax(yp, 2. * y0m - ym);
-  double ag = smin(ym, 2. * y0p - yp);
-  double bg = smax(ym, 2. * y0p - yp);
+  double xtd = y0 + half(h0) * grad;
+  double xtg = y0 - half(h0) * grad;
+  double ad = smin(yp, dbl(y0m) - ym);
+  double bd = smax(yp, dbl(y0m) - ym);
+  double ag = smin(ym, dbl(y0p) - yp);
+  double bg = smax(ym, dbl(y0p) - yp);
   s.yd = smin(smax(xtd, ad), bd);
   s.yg = smin(smax(xtg, ag), bg);
   return s;
@@ -364,12 +426,12 @@ HD PPShape pp_shape(int lim, double thr, double y0, double yp, double ym,
 // "formule 16" replacement at extrema.
 HD double pp_integral(const PPShape& s, double a, double b, double h0,
                       double y0, double yp, double ym, double ppv) {
-  double f1b = int2y(b, -h0 * 0.5, ym, s.xg, s.yg);
-  double f1a = int2y(a, -h0 * 0.5, ym, s.xg, s.yg);
+  double f1b = int2y(b, half(-h0), ym, s.xg, s.yg);
+  double f1a = int2y(a, half(-h0), ym, s.xg, s.yg);
   double f2b = int2y(b, s.xg, s.yg, s.xd, s.yd);
   double f2a = int2y(a, s.xg, s.yg, s.xd, s.yd);
-  double f3b = int2y(b, s.xd, s.yd, h0 * 0.5, yp);
-  double f3a = int2y(a, s.xd, s.yd, h0 * 0.5, yp);
+  double f3b = int2y(b, s.xd, s.yd, half(h0), yp);
+  double f3a = int2y(a, s.xd, s.yd, half(h0), yp);
   double F = smax(((f1b - f1a) + (f2b - f2a) + (f3b - f3a)), 0.);
   if (nonneg((yp - y0) * (ym - y0))) F = y0 * ppv;
   return F;

@@ -139,7 +139,7 @@ DV double cell_dt(const RunView& v, long long c, int i, int j) {
   const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
   double uc = 0.0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) uc += ld(v.speed, nd[k]) * 0.25;
+  for (int k = 0; k < 4; ++k) uc += quarter(ld(v.speed, nd[k]));
   return ld(v.cflsq, c) / (uc + v.c[c]);
 }
 
@@ -167,7 +167,7 @@ struct LagNodes {
 
     double ux = v.u[p], uy = v.u[v.npitch + p];
     if (v.sans_lagrange == 0) {
-      const double dt = 0.5 * (C.dt_np1 + C.dt_n);
+      const double dt = half(C.dt_np1 + C.dt_n);
       const double s = dt / m;
       auto force = [&](bool sym, double sx, double sy, double& r0, double& r1) {
         r0 = 0.0;
@@ -184,7 +184,7 @@ struct LagNodes {
             double d = 0.0;
             d = d + C0 * sx;
             d = d + C1 * sy;
-            const double s2 = 2.0 * d;
+            const double s2 = dbl(d);
             const double sv0 = sx * s2 - C0, sv1 = sy * s2 - C1;
             r0 = r0 + w * (C0 + sv0);
             r1 = r1 + w * (C1 + sv1);
@@ -291,19 +291,19 @@ struct LagCells {
       xc0 = xc0 + X[k][0];
       xc1 = xc1 + X[k][1];
     }
-    xc0 = 0.25 * xc0;
-    xc1 = 0.25 * xc1;
+    xc0 = quarter(xc0);
+    xc1 = quarter(xc1);
     double vol = 0.0;
   #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int km = (k + 3) & 3, kp = (k + 1) & 3;
-      const double x2a = 0.5 * (X[km][0] + X[k][0]), x2b = 0.5 * (X[km][1] + X[k][1]);
-      const double x4a = 0.5 * (X[kp][0] + X[k][0]), x4b = 0.5 * (X[kp][1] + X[k][1]);
+      const double x2a = half(X[km][0] + X[k][0]), x2b = half(X[km][1] + X[k][1]);
+      const double x4a = half(X[kp][0] + X[k][0]), x4b = half(X[kp][1] + X[k][1]);
       const double c12 = xc0 * x2b - xc1 * x2a;
       const double c23 = x2a * X[k][1] - x2b * X[k][0];
       const double c34 = X[k][0] * x4b - X[k][1] * x4a;
       const double c41 = x4a * xc1 - x4b * xc0;
-      vol = vol + 0.5 * (c12 + c23 + c34 + c41);
+      vol = vol + half(c12 + c23 + c34 + c41);
     }
     const int nb = v.nbmat;
     const double thr = v.threshold;
@@ -322,14 +322,14 @@ struct LagCells {
     double e_new, q_new;
     if (v.sans_lagrange == 0) {
       const double rho_old = v.rho[c];
-      const double tau = 0.5 * (1.0 / rho_new + 1.0 / rho_old);
+      const double tau = half(1.0 / rho_new + 1.0 / rho_old);
       const double divu_new = C.rdt_np1 * (1.0 / rho_new - 1.0 / rho_old) / tau;
       const double c_old = v.c[c];
       if (neg(v.divu[c])) {
         const double s0 = ld(v.s0, c);
         q_new = 1.0 / tau *
-                (-0.5 * ld(v.sqs0, c) * c_old * divu_new +
-                 (v.gamma_scalar + 1) * 0.5 * s0 * divu_new * divu_new);
+                (-half(ld(v.sqs0, c)) * c_old * divu_new +
+                 half(v.gamma_scalar + 1) * s0 * divu_new * divu_new);
       } else {
         q_new = 0.0;
       }
@@ -350,10 +350,10 @@ struct LagCells {
         if (dgt(rn, thr) && dgt(ro, thr)) {
           double pseudo = 0.;
           if ((v.pseudo_centree == 1) && pos((qm_new + qm_old) * (1.0 / rn - 1.0 / ro)))
-            pseudo = 0.5 * (qm_new + qm_old);
+            pseudo = half(qm_new + qm_old);
           if (v.pseudo_centree == 0) pseudo = qm_new;
-          const double den = 1 + 0.5 * (gamma_of(v, m) - 1.0) * rn * (1.0 / rn - 1.0 / ro);
-          const double num = v.em[m * P + c] - (0.5 * v.pm[m * P + c] + pseudo) * (1.0 / rn - 1.0 / ro);
+          const double den = 1 + half(gamma_of(v, m) - 1.0) * rn * (1.0 / rn - 1.0 / ro);
+          const double num = v.em[m * P + c] - (half(v.pm[m * P + c]) + pseudo) * (1.0 / rn - 1.0 / ro);
           em_new[m] = num / den;
           e_new += mf[m] * em_new[m];
           if (pos(v.energy_limit) && abs_gt(em_new[m], v.energy_limit)) bad = true;
@@ -445,11 +445,11 @@ struct LagCells {
         return sqrt(r);
       };
       double hx = 0.;
-      hx += 0.5 * len(0, 1);  // bottom face
-      hx += 0.5 * len(3, 2);  // top face
+      hx += half(len(0, 1));  // bottom face
+      hx += half(len(3, 2));  // top face
       double hy = 0.;
-      hy += 0.5 * len(1, 2);  // right face
-      hy += 0.5 * len(0, 3);  // left face
+      hy += half(len(1, 2));  // right face
+      hy += half(len(0, 3));  // left face
       v.Hx[c] = hx;
       v.Hy[c] = hy;
     }
@@ -460,10 +460,10 @@ struct LagCells {
 // Lagrange velocities along the face normal; "+ 0.0" is the dot product's
 // zero start for the other axis.
 DV double fnv_vertical(const RunView& v, long long na, long long nb) {
-  return 0.5 * (v.u[na] + v.u[nb]) + 0.0;
+  return plus_zero(half(v.u[na] + v.u[nb]));
 }
 DV double fnv_horizontal(const RunView& v, long long na, long long nb) {
-  return 0.5 * (v.u[v.npitch + na] + v.u[v.npitch + nb]) + 0.0;
+  return plus_zero(half(v.u[v.npitch + na] + v.u[v.npitch + nb]));
 }
 
 // ----------------------------------------------------------- remap sweep
@@ -495,7 +495,7 @@ struct FaceGrad {
       fidx = (long long)i * v.nx + j;
       ax = 1;
     }
-    const double dx = (v.XcL[ax * P + front] - v.XcL[ax * P + back]) + 0.0;
+    const double dx = plus_zero(v.XcL[ax * P + front] - v.XcL[ax * P + back]);
     // with PenteBorne only the integrated components' slopes are read (see
     // SweepGrad): the most any cell integrates
     int nk = v.ncomp;
@@ -588,19 +588,19 @@ struct SweepGrad {
         fb_v = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);      // right face
         Fa = ld(v.nout, 0 * P + c) * fa_v;
         Fb = ld(v.nout, 1 * P + c) * fb_v;
-        flen = (ld(v.flv, i) + ld(v.flv, i)) * 0.5;
+        flen = half(ld(v.flv, i) + ld(v.flv, i));
       } else {
         fa_v = fnv_horizontal(v, n0, n0 + 1);               // bottom face
         fb_v = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);  // top face
         Fa = ld(v.nout, 2 * P + c) * fa_v;
         Fb = ld(v.nout, 3 * P + c) * fb_v;
-        flen = (ld(v.flh, j) + ld(v.flh, j)) * 0.5;
+        flen = half(ld(v.flh, j) + ld(v.flh, j));
       }
-      const double fdual = 0.5 * (fa_v + fb_v);
+      const double fdual = half(fa_v + fb_v);
       const double dt = C.dt_n;
-      const double ppa = 0.5 * (Fa + fabs(Fa)) * dt;
-      const double ppb = 0.5 * (Fb + fabs(Fb)) * dt;
-      const double ppd = 0.5 * (fdual + fabs(fdual)) * dt;
+      const double ppa = half(Fa + fabs(Fa)) * dt;
+      const double ppb = half(Fb + fabs(Fb)) * dt;
+      const double ppd = half(fdual + fabs(fdual)) * dt;
       const int plim = vp ? v.limiter_pure : v.limiter;
       double Fr[kMaxComp], Fv[kMaxComp];
       const double hh = h0;
@@ -618,8 +618,8 @@ struct SweepGrad {
           fd_ = y0 * ppd;
         } else {
           const PPShape sh = pp_shape(plim, v.threshold, y0, yp, ym, hh, hp, hm, grad[k]);
-          fa_ = (k < nint) ? pp_integral(sh, -hh * 0.5, -hh * 0.5 + ppa, hh, y0, yp, ym, ppa) : 0.;
-          fb_ = (k < nint) ? pp_integral(sh, hh * 0.5 - ppb, hh * 0.5, hh, y0, yp, ym, ppb) : 0.;
+          fa_ = (k < nint) ? pp_integral(sh, half(-hh), half(-hh) + ppa, hh, y0, yp, ym, ppa) : 0.;
+          fb_ = (k < nint) ? pp_integral(sh, half(hh) - ppb, half(hh), hh, y0, yp, ym, ppb) : 0.;
           fd_ = dual_k ? pp_integral(sh, 0., ppd, hh, y0, yp, ym, ppd) : 0.;
         }
         if (k < nint) {
@@ -703,10 +703,10 @@ struct SweepFace {
     const int ax = dirx ? 0 : 1;
     if (v.order <= 2) {
       if (v.pb == 0) {
-        const double dxl = (v.XcL[ax * P + cf] - v.XcL[ax * P + cb]) + 0.0;
+        const double dxl = plus_zero(v.XcL[ax * P + cf] - v.XcL[ax * P + cb]);
         const double xf = dirx ? ld(v.xs, j) : ld(v.ys, i);
         const long long cu = pos(fnv * dxl) ? cb : cf;
-        const double s = (xf - v.XcL[ax * P + cu]) + 0.0;
+        const double s = plus_zero(xf - v.XcL[ax * P + cu]);
         for (int k = 0; k < ncomp; ++k)
           out[k * FP] = v.Phi[k * P + cu] + s * v.gP[k * P + cu];
       } else {
@@ -893,18 +893,18 @@ struct DualGrad {
         const double xp = v.XL[ax * NP + p], xr = v.XL[ax * NP + R],
                      xl = v.XL[ax * NP + L];
         double hm, hp;
-        const double h0 = 0.5 * (xr - xl);
+        const double h0 = half(xr - xl);
         const bool hasLL = (at - 1 != 0), hasRR = (at + 1 != lastpos);
         if (!hasLL) {
           hm = 0.;
           const double xrr = hasRR ? v.XL[ax * NP + R + stride] : 0.0;
-          hp = 0.5 * (xrr - xp);
+          hp = half(xrr - xp);
         } else if (!hasRR) {
           hp = 0.;
-          hm = 0.5 * (xp - v.XL[ax * NP + L - stride]);
+          hm = half(xp - v.XL[ax * NP + L - stride]);
         } else {
-          hm = 0.5 * (xp - v.XL[ax * NP + L - stride]);
-          hp = 0.5 * (v.XL[ax * NP + R + stride] - xp);
+          hm = half(xp - v.XL[ax * NP + L - stride]);
+          hp = half(v.XL[ax * NP + R + stride] - xp);
         }
         double g[2];
   #pragma unroll
@@ -1033,32 +1033,32 @@ struct DualUpdate {
     {
       const double dn0 = hasL ? D[L] : 0.0, dn1 = hasL ? D[NP + L] : 0.0;
       const double xn = hasL ? v.XL[ax * NP + L] : 0.0;
-      const double u = 0.5 * ((ax == 0 ? dn0 : dn1) + (ax == 0 ? dp0 : dp1));
-      const int sg = pos(u) ? 1 : -1;
+      const double u = half((ax == 0 ? dn0 : dn1) + (ax == 0 ? dp0 : dp1));
       const double dx = xp - xn;
+      const double sdx = pos(u) ? dx : -dx;  // sign(u) * dx
       if (pos(Fm)) {
         const double g0 = hasL ? v.gD[L] : 0.0, g1 = hasL ? v.gD[NP + L] : 0.0;
-        um[0] = dn0 + order2 * (0.5 * g0 * (sg * dx - dt * u));
-        um[1] = dn1 + order2 * (0.5 * g1 * (sg * dx - dt * u));
+        um[0] = dn0 + mul_012(order2, half(g0) * (sdx - dt * u));
+        um[1] = dn1 + mul_012(order2, half(g1) * (sdx - dt * u));
       } else {
-        um[0] = dp0 + order2 * (0.5 * gp0 * (sg * dx - dt * u));
-        um[1] = dp1 + order2 * (0.5 * gp1 * (sg * dx - dt * u));
+        um[0] = dp0 + mul_012(order2, half(gp0) * (sdx - dt * u));
+        um[1] = dp1 + mul_012(order2, half(gp1) * (sdx - dt * u));
       }
     }
     // plus side (right / top)
     {
       const double dn0 = hasR ? D[R] : 0.0, dn1 = hasR ? D[NP + R] : 0.0;
       const double xn = hasR ? v.XL[ax * NP + R] : 0.0;
-      const double u = 0.5 * ((ax == 0 ? dp0 : dp1) + (ax == 0 ? dn0 : dn1));
-      const int sg = pos(u) ? 1 : -1;
+      const double u = half((ax == 0 ? dp0 : dp1) + (ax == 0 ? dn0 : dn1));
       const double dx = xn - xp;
+      const double sdx = pos(u) ? dx : -dx;  // sign(u) * dx
       if (neg(Fp)) {
         const double g0 = hasR ? v.gD[R] : 0.0, g1 = hasR ? v.gD[NP + R] : 0.0;
-        up[0] = dn0 + order2 * (0.5 * g0 * (sg * dx - dt * u));
-        up[1] = dn1 + order2 * (0.5 * g1 * (sg * dx - dt * u));
+        up[0] = dn0 + mul_012(order2, half(g0) * (sdx - dt * u));
+        up[1] = dn1 + mul_012(order2, half(g1) * (sdx - dt * u));
       } else {
-        up[0] = dp0 + order2 * (0.5 * gp0 * (sg * dx - dt * u));
-        up[1] = dp1 + order2 * (0.5 * gp1 * (sg * dx - dt * u));
+        up[0] = dp0 + mul_012(order2, half(gp0) * (sdx - dt * u));
+        up[1] = dp1 + mul_012(order2, half(gp1) * (sdx - dt * u));
       }
     }
     const double Un0 = Ui0 + Fm * um[0] - Fp * up[0];

@@ -70,12 +70,34 @@ int main() {
     bad += is_finite(a) != (bool)std::isfinite(a);
     bad += abs_lt(a, 1e-12) != (std::fabs(a) < 1e-12);
     bad += abs_gt(a, 1e-14) != (std::fabs(a) > 1e-14);
+    bad += !same(half(a), a * 0.5);
+    bad += !same(quarter(a), a * 0.25);
+    bad += !same(dbl(a), 2.0 * a);
+    bad += !same(plus_zero(a), a + 0.0);
+    for (int k = 0; k < 3; ++k) bad += !same(mul_012(k, a), (double)k * a);
     if (!std::isnan(a)) {
       bad += !same(twice(a), 2.0 * a);
       for (int id : {HYDRO_LIM_MINMOD, HYDRO_LIM_SUPERBEE})
         bad += !same(flux_limiter_q(id, a), ref_flux_limiter(id, a));
     }
   }
+  // exponent helpers: every significand pattern class near and below the
+  // smallest normal exponents, both signs
+  long pbad = 0, pn = 0;
+  for (int i = 0; i < 4000000; ++i) {
+    unsigned long long b = g();
+    const unsigned long long e = g() % 6;  // exponents 0..5
+    b = (b & 0x800fffffffffffffull) | (e << 52);
+    if (i % 7 == 0) b = (b & ~0xfull) | (g() & 0xf);  // low bits that round
+    double a;
+    memcpy(&a, &b, 8);
+    ++pn;
+    pbad += !same(half(a), a * 0.5);
+    pbad += !same(quarter(a), a * 0.25);
+    pbad += !same(dbl(a), 2.0 * a);
+  }
+  if (pbad) printf("exponent helpers: %ld mismatches of %ld\n", pbad, pn);
+  bad += pbad;
   // limiter on gradient pairs: specials, random, and ratios near breakpoints
   std::vector<std::pair<double, double>> pairs;
   for (double a : v)
