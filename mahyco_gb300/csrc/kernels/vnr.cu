@@ -322,8 +322,9 @@ struct LagCells {
     double e_new, q_new;
     if (v.sans_lagrange == 0) {
       const double rho_old = v.rho[c];
-      const double tau = half(1.0 / rho_new + 1.0 / rho_old);
-      const double divu_new = C.rdt_np1 * (1.0 / rho_new - 1.0 / rho_old) / tau;
+      const double irho_new = 1.0 / rho_new, irho_old = 1.0 / rho_old;
+      const double tau = half(irho_new + irho_old);
+      const double divu_new = C.rdt_np1 * (irho_new - irho_old) / tau;
       const double c_old = v.c[c];
       if (neg(v.divu[c])) {
         const double s0 = ld(v.s0, c);
@@ -337,7 +338,7 @@ struct LagCells {
       v.divu[c] = divu_new;
       // energies (updateEnergy) and EOS
       e_new = 0.;
-      double pm_new[3], cm_new[3], em_new[3];
+      double cm_new[3], em_new[3];
       bool bad = false;
   #pragma unroll
       for (int m = 0; m < 3; ++m) {
@@ -348,12 +349,20 @@ struct LagCells {
         const double rn = rhom_new[m], ro = v.rhom[m * P + c];
         em_new[m] = 0.;
         if (dgt(rn, thr) && dgt(ro, thr)) {
+          // 1/rho_m: in a pure cell the material density is the cell's,
+          // bit for bit, and so is its reciprocal
+          double irn, iro;
+          if (ubits(rn) == ubits(rho_new)) irn = irho_new;
+          else irn = 1.0 / rn;
+          if (ubits(ro) == ubits(rho_old)) iro = irho_old;
+          else iro = 1.0 / ro;
+          const double dvi = irn - iro;
           double pseudo = 0.;
-          if ((v.pseudo_centree == 1) && pos((qm_new + qm_old) * (1.0 / rn - 1.0 / ro)))
+          if ((v.pseudo_centree == 1) && pos((qm_new + qm_old) * dvi))
             pseudo = half(qm_new + qm_old);
           if (v.pseudo_centree == 0) pseudo = qm_new;
-          const double den = 1 + half(gamma_of(v, m) - 1.0) * rn * (1.0 / rn - 1.0 / ro);
-          const double num = v.em[m * P + c] - (half(v.pm[m * P + c]) + pseudo) * (1.0 / rn - 1.0 / ro);
+          const double den = 1 + half(gamma_of(v, m) - 1.0) * rn * dvi;
+          const double num = v.em[m * P + c] - (half(v.pm[m * P + c]) + pseudo) * dvi;
           em_new[m] = num / den;
           e_new += mf[m] * em_new[m];
           if (pos(v.energy_limit) && abs_gt(em_new[m], v.energy_limit)) bad = true;
@@ -363,32 +372,37 @@ struct LagCells {
         atomicOr(&C.err, HYDRO_ERR_ENERGY);
         atomicMin((unsigned long long*)&C.err_cell, (unsigned long long)c);
       }
+      // computeEOS: only the materials' sound speeds and the Void state
+      // matter here (the pressures are recomputed after the remap)
   #pragma unroll
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
-        if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
-          const double g = gamma_of(v, m);
-          pm_new[m] = (g - 1.0) * rhom_new[m] * em_new[m];
-          cm_new[m] = sqrt(g * (g - 1.0) * em_new[m]);
-        } else {  // Void: state kept
-          pm_new[m] = v.pm[m * P + c];
+        if (eos_of(v, m) != HYDRO_EOS_PERFECT_GAS) {  // Void: state kept
           cm_new[m] = v.cm[m * P + c];
           em_new[m] = v.em[m * P + c];
         }
       }
       for (int m = 0; m < nb; ++m)
         if (eos_of(v, m) == HYDRO_EOS_VOID) e_new = 0.;
-      // computePressionMoyenne: the stale max argument is the in-place c
+      // computePressionMoyenne: max of the in-place c and the materials'
+      // sound speeds, replaced by the mixture's when rho > 0 (then the
+      // materials' values are not needed)
       double cc = c_old;
-      for (int m = 0; m < nb; ++m) cc = smax(cc, cm_new[m]);
       if (pos(rho_new)) {
         const double g0 = v.gamma[0];
         cc = sqrt(g0 * (g0 - 1.0) * e_new);
+      } else {
+        for (int m = 0; m < nb; ++m) {
+          if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
+            const double g = gamma_of(v, m);
+            cm_new[m] = sqrt(g * (g - 1.0) * em_new[m]);
+          }
+          cc = smax(cc, cm_new[m]);
+        }
       }
       for (int m = 0; m < nb; ++m)
         if (eos_of(v, m) == HYDRO_EOS_VOID) e_new += mf[m] * em_new[m];
       v.c[c] = cc;
-      (void)pm_new;
     } else {
       // no Lagrange phase (advection cases): energy and q are carried over
       e_new = v.e[c];
