@@ -113,11 +113,6 @@ HD double qdiv(double n, double d) {
   return ddiv_call(n, d);
 }
 
-// x / k for k = 1, 2 or 4, as the exact multiplication by 1/k (division by
-// a power of two and multiplication by its reciprocal round identically).
-HD double div_pow2(double x, int k) {
-  return x * (k == 4 ? 0.25 : (k == 2 ? 0.5 : 1.0));
-}
 
 // Remap::fluxLimiter (remap/UtilesRemap.cc:9-23)
 HD double flux_limiter(int id, double r) {
@@ -176,6 +171,11 @@ HD double mul_pow2m(double x) {
     return from_bits(b - ((unsigned long long)K << 52));
   return mul_pow2m_call<K>(x);
 }
+// x / k for k = 1, 2 or 4, as the exact multiplication by 1/k (division by
+// a power of two and multiplication by its reciprocal round identically).
+HD double div_pow2(double x, int k) {
+  return k == 4 ? mul_pow2m<2>(x) : (k == 2 ? mul_pow2m<1>(x) : x);
+}
 HD double half(double x) { return mul_pow2m<1>(x); }
 HD double quarter(double x) { return mul_pow2m<2>(x); }
 // 2 * x for any x: exponent + 1 while the result stays finite and normal;
@@ -198,6 +198,15 @@ HD double plus_zero(double x) {
   if (b == 0x8000000000000000ull) return 0.0;
   return is_nan(x) ? x + 0.0 : x;
 }
+// x * n, with n = +1 or -1 (the outer normals of the Cartesian Euler mesh)
+// decided on the integer pipe: x or -x, exactly the IEEE products
+HD double mul_pm1(double x, double n) {
+  const unsigned long long b = ubits(n);
+  if (b == 0x3ff0000000000000ull) return x;
+  if (b == 0xbff0000000000000ull) return -x;
+  return x * n;
+}
+
 // k * x for a small integer k in {0, 1, 2} (k = 0: the IEEE product's signed
 // zero, or NaN for a non-finite x)
 HD double mul_012(int k, double x) {

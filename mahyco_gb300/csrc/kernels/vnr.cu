@@ -803,8 +803,8 @@ struct SweepUpdate {
         coef[0] = na * va * fl * dt;
         coef[1] = nb_ * vb * fl * dt;
       } else {
-        coef[0] = na * fl;
-        coef[1] = nb_ * fl;
+        coef[0] = mul_pm1(fl, na);
+        coef[1] = mul_pm1(fl, nb_);
       }
     } else {
       has[0] = (i >= 1);
@@ -819,8 +819,8 @@ struct SweepUpdate {
         coef[0] = na * va * fl * dt;
         coef[1] = nb_ * vb * fl * dt;
       } else {
-        coef[0] = na * fl;
-        coef[1] = nb_ * fl;
+        coef[0] = mul_pm1(fl, na);
+        coef[1] = mul_pm1(fl, nb_);
       }
     }
     // dual-method components: masses (A1) or volumes (A2)
@@ -996,10 +996,10 @@ struct DualUpdate {
         } else {
           // FFd planes: [0..nb) flux through the cell's minus face,
           // [nb..2nb) through its plus face
-          double va = v.FFd[m * P + a] * ld(v.nout, pl_pn * P + a) +
-                      v.FFd[(nb + m) * P + a] * ld(v.nout, pl_pf * P + a);
-          double vb = v.FFd[(nb + m) * P + b] * ld(v.nout, pl_mn * P + b) +
-                      v.FFd[m * P + b] * ld(v.nout, pl_mf * P + b);
+          double va = mul_pm1(v.FFd[m * P + a], ld(v.nout, pl_pn * P + a)) +
+                      mul_pm1(v.FFd[(nb + m) * P + a], ld(v.nout, pl_pf * P + a));
+          double vb = mul_pm1(v.FFd[(nb + m) * P + b], ld(v.nout, pl_mn * P + b)) +
+                      mul_pm1(v.FFd[m * P + b], ld(v.nout, pl_mf * P + b));
           if (v.dual_method == 1) {
             va = v.rL[a] * va;
             vb = v.rL[b] * vb;
