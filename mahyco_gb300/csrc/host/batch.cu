@@ -194,7 +194,10 @@ int set_members(BatchPlan* p, hydro_run* const* runs, int n) {
         p->d_tiles[on][w] = reinterpret_cast<Tile*>(p->dmem + o_t[on][w]);
   }
   std::vector<RunView> views(n);
-  for (int r = 0; r < n; ++r) views[r] = rv[r]->v;
+  for (int r = 0; r < n; ++r) {
+    views[r] = rv[r]->v;
+    views[r].o3g = views[r].o3y = nullptr;  // order-3 values per face
+  }
   int nt[2 * kNumTileShapes];
   for (int on = 0; on < 2; ++on)
     for (int w = 0; w < kNumTileShapes; ++w) {

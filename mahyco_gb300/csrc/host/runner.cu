@@ -85,6 +85,12 @@ size_t layout(RunView& v, char* base) {
   v.DPF = a.take<double>(nb * P);
   v.phiF = a.take<double>(nc * FP);
   v.FFd = a.take<double>(2 * nb * P);
+  if (v.order == 3) {
+    v.o3g = a.take<double>(nc * P);
+    v.o3y = a.take<double>(nc * FP);
+  } else {
+    v.o3g = v.o3y = nullptr;
+  }
   v.DPv = a.take<double>(2 * NP);
   v.gD = a.take<double>(2 * NP);
   v.UD1 = a.take<double>(3 * NP);
@@ -270,6 +276,7 @@ size_t run_arena_bytes(const hydro_spec& spec) {
                       32);
   v.nbmat = spec.nbmat;
   v.scheme = spec.scheme;
+  v.order = spec.projection_order;
   v.ncomp = spec.scheme == HYDRO_SCHEME_EUCCLHYD
                 ? 3 * spec.nbmat + 2 + (spec.projection_conservative == 1 ? 1 : 0)
                 : 3 * spec.nbmat + 1;

@@ -88,6 +88,11 @@ struct RunView {
   double* DPF;        // nbmat planes (plateau-slope dual mass flux)
   double* phiF;       // ncomp face planes
   double* FFd;        // 2*nbmat planes: dual-method flux comps, minus / plus
+  double* o3g;        // order 3: ncomp cell planes, each cell's limited-free
+                      // gradient along the sweep (eval_grad); null otherwise
+                      // and in batched launches, which work per face
+  double* o3y;        // order 3: ncomp face planes, the interpolated value
+                      // at each inner face (eval_ystar)
   double* DPv;        // 2 node planes: nodal velocity after sweep 1
   double* gD;         // 2 node planes: limited nodal velocity gradient
   double* UD1;        // 3 node planes: m*u, m*v, m after sweep 1
@@ -160,7 +165,7 @@ __device__ __forceinline__ bool output_pause_here(Ctrl& C) {
 
 // Per-kernel timing hook for launch_cycle.
 using LaunchHook = std::function<void(int)>;
-constexpr int kNumKernelKinds = 16;
+constexpr int kNumKernelKinds = 18;
 extern const char* const kKernelNames[kNumKernelKinds];
 
 // ---- batched execution: many independent runs advance in one launch per

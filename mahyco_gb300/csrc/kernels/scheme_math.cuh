@@ -522,25 +522,24 @@ struct O3Face {
   double R1, R2;                             // (1 - nu-) / nu-, (1 + nu+) / nu+
   bool fwd;                                  // vdt >= 0
 };
-HD O3Face o3_face(const double* h, double vdt) {
-  O3Face F;
-#pragma unroll
-  for (int g = 0; g < 4; ++g) {  // eval_grad(h[g], h[g+1], h[g+2], ...)
-    const double hm = h[g], h0 = h[g + 1], hp = h[g + 2];
-    F.G0[g] = h0 / (hm + h0 + hp);
-    F.A[g] = (2. * hm + h0) / (h0 + hp);
-    F.B[g] = (h0 + 2. * hp) / (hm + h0);
-  }
-#pragma unroll
-  for (int g = 0; g < 3; ++g) {  // eval_ystar(h[g], .., h[g+3], ...)
-    const double hmm = h[g], hm = h[g + 1], hp = h[g + 2], hpp = h[g + 3];
-    F.T1[g] = (2. * hp * hm) / (hm + hp) *
-              ((hmm + hm) / (2. * hm + hp) - (hpp + hp) / (2. * hp + hm));
-    F.T2[g] = -hm * (hmm + hm) / (2. * hm + hp);
-    F.T3[g] = hp * (hp + hpp) / (hm + 2. * hp);
-    F.T4[g] = hm / (hm + hp);
-    F.T5[g] = 1. / (hmm + hm + hp + hpp);
-  }
+// eval_grad's coefficients for a cell of width h0 between widths hm, hp
+HD void o3_grad_coef(double hm, double h0, double hp, double& G0, double& A, double& B) {
+  G0 = h0 / (hm + h0 + hp);
+  A = (2. * hm + h0) / (h0 + hp);
+  B = (h0 + 2. * hp) / (hm + h0);
+}
+// eval_ystar's coefficients for a face between widths hm | hp, with the
+// next widths hmm, hpp outside
+HD void o3_ystar_coef(double hmm, double hm, double hp, double hpp, double* T) {
+  T[0] = (2. * hp * hm) / (hm + hp) *
+         ((hmm + hm) / (2. * hm + hp) - (hpp + hp) / (2. * hp + hm));
+  T[1] = -hm * (hmm + hm) / (2. * hm + hp);
+  T[2] = hp * (hp + hpp) / (hm + 2. * hp);
+  T[3] = hm / (hm + hp);
+  T[4] = 1. / (hmm + hm + hp + hpp);
+}
+// the face's coefficients that depend on vdt
+HD void o3_face_dt(O3Face& F, const double* h, double vdt) {
   F.fwd = nonneg(vdt);
   const double x = F.fwd ? vdt : -vdt, dx = F.fwd ? h[2] : h[3];
   F.Q1 = 0.5 * x / dx;
@@ -548,22 +547,41 @@ HD O3Face o3_face(const double* h, double vdt) {
   const double num = vdt / h[2], nup = vdt / h[3];
   F.R1 = (1. - num) / num;
   F.R2 = (1. + nup) / nup;
+}
+HD O3Face o3_face(const double* h, double vdt) {
+  O3Face F;
+#pragma unroll
+  for (int g = 0; g < 4; ++g)  // eval_grad(h[g], h[g+1], h[g+2], ...)
+    o3_grad_coef(h[g], h[g + 1], h[g + 2], F.G0[g], F.A[g], F.B[g]);
+#pragma unroll
+  for (int g = 0; g < 3; ++g) {  // eval_ystar(h[g], .., h[g+3], ...)
+    double T[5];
+    o3_ystar_coef(h[g], h[g + 1], h[g + 2], h[g + 3], T);
+    F.T1[g] = T[0];
+    F.T2[g] = T[1];
+    F.T3[g] = T[2];
+    F.T4[g] = T[3];
+    F.T5[g] = T[4];
+  }
+  o3_face_dt(F, h, vdt);
   return F;
 }
-HD double flux_ordre3_c(const O3Face& F, const double* y) {
-  double gr[4];
-#pragma unroll
-  for (int g = 0; g < 4; ++g)
-    gr[g] = F.G0[g] * (F.A[g] * (y[g + 2] - y[g + 1]) + F.B[g] * (y[g + 1] - y[g]));
-  double ys[3];
-#pragma unroll
-  for (int g = 0; g < 3; ++g) {
-    const double ym = y[g + 1], yp = y[g + 2];
-    const double tmp1 = F.T1[g] * (yp - ym);
-    const double tmp2 = F.T2[g] * gr[g + 1] + F.T3[g] * gr[g];
-    ys[g] = ym + F.T4[g] * (yp - ym) + F.T5[g] * (tmp1 + tmp2);
-  }
-  const double ym = y[2], yp = y[3];
+// eval_grad with its coefficients
+HD double o3_grad(double G0, double A, double B, double ym, double y0, double yp) {
+  return G0 * (A * (yp - y0) + B * (y0 - ym));
+}
+// eval_ystar with its coefficients T (o3_ystar_coef) at the face between
+// ym | yp, from the gradients of the cells on its minus / plus side
+HD double o3_ystar(const double* T, double ym, double yp, double grm, double grp) {
+  const double tmp1 = T[0] * (yp - ym);
+  const double tmp2 = T[1] * grp + T[2] * grm;
+  return ym + T[3] * (yp - ym) + T[4] * (tmp1 + tmp2);
+}
+// the face value from the interpolated values ys of the faces at -1, 0, +1
+// and the cell values y1 | ym | yp | y4 (ComputeFluxOrdre3's parabola and
+// its TVD interval)
+HD double o3_tail(const O3Face& F, const double* ys, double y1, double ym, double yp,
+                  double y4) {
   const double grad_m = ys[1] - ys[0], grad_p = ys[2] - ys[1];
   const double ym6 = 6. * (ym - 0.5 * (ys[0] + ys[1]));
   const double yp6 = 6. * (yp - 0.5 * (ys[1] + ys[2]));
@@ -572,8 +590,8 @@ HD double flux_ordre3_c(const O3Face& F, const double* y) {
     flux = ys[1] - F.Q1 * (grad_m - (1. - F.Q2) * ym6);
   else
     flux = ys[1] + F.Q1 * (grad_p - (1. - F.Q2) * yp6);
-  const double ym_ym = ym + F.R1 * (ym - y[1]);
-  const double yp_ym = yp - F.R2 * (yp - y[4]);
+  const double ym_ym = ym + F.R1 * (ym - y1);
+  const double yp_ym = yp - F.R2 * (yp - y4);
   const double i1inf = smin(ym, yp), i1sup = smax(ym, yp);
   double i2inf, i2sup;
   if (F.fwd) {
@@ -594,6 +612,18 @@ HD double flux_ordre3_c(const O3Face& F, const double* y) {
   if (dlt(flux, linf)) flux = linf;
   if (dgt(flux, lsup)) flux = lsup;
   return flux;
+}
+HD double flux_ordre3_c(const O3Face& F, const double* y) {
+  double gr[4];
+#pragma unroll
+  for (int g = 0; g < 4; ++g) gr[g] = o3_grad(F.G0[g], F.A[g], F.B[g], y[g], y[g + 1], y[g + 2]);
+  double ys[3];
+#pragma unroll
+  for (int g = 0; g < 3; ++g) {
+    const double T[5] = {F.T1[g], F.T2[g], F.T3[g], F.T4[g], F.T5[g]};
+    ys[g] = o3_ystar(T, y[g + 1], y[g + 2], gr[g], gr[g + 1]);
+  }
+  return o3_tail(F, ys, y[1], y[2], y[3], y[4]);
 }
 
 }  // namespace hydro

@@ -685,11 +685,74 @@ struct SweepGrad {
   }
 };
 
+// Order-3 face values (ComputeFluxOrdre3) share most of their work between
+// neighbouring faces: each cell's gradient (eval_grad) enters four faces,
+// each face's interpolated value (eval_ystar) three.  They are computed once
+// per sweep by O3Grad (one thread per cell) and O3Ystar (one thread per
+// inner face) and read by SweepFace for faces whose six-cell stencil is not
+// clamped at the ends of the row / column (the two faces next to each end
+// compute everything themselves).  Same arithmetic, same values.
+DV double o3_value(const RunView& v, int sweep, int k, long long c) {
+  // the component value the order-3 reconstruction works on: U / vLagrange,
+  // which is what Phi holds without PenteBorne (same division)
+  if (v.pb == 0) return v.Phi[k * v.pitch + c];
+  const double* Uin = (sweep == 1) ? v.UL : v.U1;
+  return qdiv(Uin[k * v.pitch + c], v.vL[c]);
+}
+struct O3Grad {
+  int sweep;
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    if (i >= v.ny || j >= v.nx || !v.o3g) return;
+    const Ctrl& C = *v.ctrl;
+    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+    const long long P = v.pitch;
+    const long long c = (long long)i * v.nx + j;
+    const double* H = dirx ? v.Hx : v.Hy;
+    const int q = dirx ? j : i, n = dirx ? v.nx : v.ny;
+    const long long st = dirx ? 1 : v.nx;  // cell stride along the axis
+    // neighbours clamped at the ends, as the face stencil clamps them
+    const long long cm = q > 0 ? c - st : c, cp = q < n - 1 ? c + st : c;
+    double G0, A, B;
+    o3_grad_coef(H[cm], H[c], H[cp], G0, A, B);
+    for (int k = 0; k < v.ncomp; ++k)
+      v.o3g[k * P + c] = o3_grad(G0, A, B, o3_value(v, sweep, k, cm),
+                                 o3_value(v, sweep, k, c), o3_value(v, sweep, k, cp));
+  }
+};
+// the inner face between positions q-1 and q of cell c's row / column
+struct O3Ystar {
+  int sweep;
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    if (i >= v.ny || j >= v.nx || !v.o3g) return;
+    const Ctrl& C = *v.ctrl;
+    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+    const long long P = v.pitch, FP = v.fpitch;
+    const long long c = (long long)i * v.nx + j;
+    const int q = dirx ? j : i, n = dirx ? v.nx : v.ny;
+    if (q < 1) return;
+    const double* H = dirx ? v.Hx : v.Hy;
+    const long long st = dirx ? 1 : v.nx;
+    const long long cm = c - st;                           // q-1
+    const long long cmm = q > 1 ? cm - st : cm;            // left(q-1)
+    const long long cpp = q < n - 1 ? c + st : c;          // right(q)
+    double T[5];
+    o3_ystar_coef(H[cmm], H[cm], H[c], H[cpp], T);
+    const long long f = dirx ? (long long)i * (v.nx + 1) + j : c;
+    for (int k = 0; k < v.ncomp; ++k)
+      v.o3y[k * FP + f] = o3_ystar(T, o3_value(v, sweep, k, cm), o3_value(v, sweep, k, c),
+                                   v.o3g[k * P + cm], v.o3g[k * P + c]);
+  }
+};
+
 // Face values of one sweep (Remap::computeUpwindFaceQuantitiesForProjection
 // {1,2}, remap/PhaseRemap1.cc:331-452, PhaseRemap2.cc:331-447).  One thread
 // per inner face perpendicular to the sweep; face (i, j) is the left face of
 // cell (i, j) (x sweep) or the bottom face of cell (i, j) (y sweep).
-struct SweepFace {
+// ORDERS: 3 = the run's order decides (batched launches), 2 = orders 1-2
+// only, 1 = order 3 only (the plain launches compile the two apart so that
+// neither carries the other's registers).
+template <int ORDERS>
+struct SweepFaceT {
   int sweep;
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
     const Ctrl& C = *v.ctrl;
@@ -715,7 +778,8 @@ struct SweepFace {
     }
     double* out = v.phiF + fidx;
     const int ax = dirx ? 0 : 1;
-    if (v.order <= 2) {
+    const bool low = (ORDERS == 2) || (ORDERS == 3 && v.order <= 2);
+    if (low) {
       if (v.pb == 0) {
         const double dxl = plus_zero(v.XcL[ax * P + cf] - v.XcL[ax * P + cb]);
         const double xf = dirx ? ld(v.xs, j) : ld(v.ys, i);
@@ -753,17 +817,29 @@ struct SweepFace {
       const double vdt = fnv * C.dt_n;
       double h[6];
       for (int t = 0; t < 6; ++t) h[t] = H[cs[t]];
-      // every division of the order-3 value depends on the face only
-      const O3Face F = o3_face(h, vdt);
-      for (int k = 0; k < ncomp; ++k) {
-        double y[6];
-        if (v.pb == 0) {
-          // U / vLagrange is what Phi holds without PenteBorne (same division)
-          for (int t = 0; t < 6; ++t) y[t] = v.Phi[k * P + cs[t]];
-        } else {
-          for (int t = 0; t < 6; ++t) y[t] = qdiv(Uin[k * P + cs[t]], v.vL[cs[t]]);
+      // every division of the order-3 value depends on the face only; the
+      // coefficients shared with the neighbouring faces come from O3Coef
+      // unless the stencil is clamped (faces next to the ends)
+      const int q = dirx ? j : i, n = dirx ? v.nx : v.ny;
+      if (v.o3g && q >= 2 && q <= n - 2) {
+        // interior face: gradients and interpolated values from O3Grad /
+        // O3Ystar, only the parabola and its interval here
+        O3Face F;
+        o3_face_dt(F, h, vdt);
+        const long long fst = dirx ? 1 : v.nx;  // face stride along the axis
+        for (int k = 0; k < ncomp; ++k) {
+          const double ys[3] = {v.o3y[k * FP + fidx - fst], v.o3y[k * FP + fidx],
+                                v.o3y[k * FP + fidx + fst]};
+          out[k * FP] = o3_tail(F, ys, o3_value(v, sweep, k, cs[1]), o3_value(v, sweep, k, cs[2]),
+                                o3_value(v, sweep, k, cs[3]), o3_value(v, sweep, k, cs[4]));
         }
-        out[k * FP] = flux_ordre3_c(F, y);
+      } else {
+        const O3Face F = o3_face(h, vdt);
+        for (int k = 0; k < ncomp; ++k) {
+          double y[6];
+          for (int t = 0; t < 6; ++t) y[t] = o3_value(v, sweep, k, cs[t]);
+          out[k * FP] = flux_ordre3_c(F, y);
+        }
       }
     }
   }
@@ -1282,8 +1358,11 @@ __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
 __global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { plain_items(v, FaceGrad{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_o3_grad(RunView v, int sweep) { plain_items(v, O3Grad{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_o3_ystar(RunView v, int sweep) { plain_items(v, O3Ystar{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) { plain_items(v, SweepGrad{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFace{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFaceT<2>{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdate{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
@@ -1320,7 +1399,7 @@ __global__ void __launch_bounds__(kBatchThreads) kb_lag_nodes(BatchArgs b) { bat
 __global__ void __launch_bounds__(kBatchThreads) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGrad{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFace{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdate{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
@@ -1368,7 +1447,8 @@ const char* const kKernelNames[kNumKernelKinds] = {
     "k_begin",      "k_reset_reductions", "k_lag_nodes", "k_lag_cells",
     "k_sweep_grad", "k_sweep_face",       "k_sweep_update", "k_dual_grad",
     "k_dual_update", "k_final",           "k_end",         "k_face_grad",
-    "ke_cell_pre",  "ke_nodes",           "ke_cells",      "ke_final"};
+    "ke_cell_pre",  "ke_nodes",           "ke_cells",      "ke_final",
+    "k_o3_grad",    "k_o3_ystar"};
 
 // Enqueues one full cycle on stream s; hook(kind) is called before each
 // launch (and with kind = -1 after the last) when given.  Returns the number
@@ -1388,7 +1468,13 @@ int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* 
     H(11); k_face_grad<<<fg, blk, 0, s>>>(v, sweep); ++nk;
     H(4); k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk;
   }
-  H(5); k_sweep_face<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+  if (v.order == 3) {
+    H(16); k_o3_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk;
+    H(17); k_o3_ystar<<<cg, blk, 0, s>>>(v, sweep); ++nk;
+    H(5); k_sweep_face3<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+  } else {
+    H(5); k_sweep_face<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+  }
   H(6); k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
   return nk;
 }
