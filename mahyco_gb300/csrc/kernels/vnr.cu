@@ -527,12 +527,16 @@ struct FaceGrad {
 // Limited slopes and plateau-slope integrals of one sweep
 // (Remap::computeGradPhiFace{1,2} + computeGradPhi{1,2},
 // remap/PhaseRemap1.cc:22-323, remap/PhaseRemap2.cc:21-323).
-struct SweepGrad {
+// PB: 2 = the run's option decides (batched launches), 0 / 1 = compiled
+// for runs without / with PenteBorne only (plain launches).
+template <int PB>
+struct SweepGradT {
   int sweep;
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    const int pb = (PB == 2) ? v.pb : PB;
     // no slopes at order 1, nor at order 3 without PenteBorne (batched
     // launches; the plain cycle does not launch these then)
-    if (v.order <= 1 || (v.order == 3 && v.pb == 0)) return;
+    if (v.order <= 1 || (v.order == 3 && pb == 0)) return;
     const Ctrl& C = *v.ctrl;
     if (i >= v.ny || j >= v.nx) return;
     const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
@@ -567,7 +571,7 @@ struct SweepGrad {
                     (v.mixte[c] == 0 && v.mixte[cf] == 0 && v.mixte[cb] == 0 &&
                      v.pure[c] == v.pure[cf] && v.pure[c] == v.pure[cb]);
     int lim = v.limiter;
-    if ((v.pb == 1) && vp) lim = v.limiter_pure;
+    if ((pb == 1) && vp) lim = v.limiter_pure;
     // "plus" / "minus" neighbours in computeAndLimitGradPhi's argument order
     const long long cp = dirx ? cf : cb, cm = dirx ? cb : cf;
     const double h0 = H[c], hp = H[cp], hm = H[cm];
@@ -583,7 +587,7 @@ struct SweepGrad {
     // limited slopes are read; without PenteBorne every slope is stored.
     const int nint = (v.pb_complet == 1) ? (euc ? ncomp : 3 * nb) : (vp ? 2 * nb : nb);
     const int nuse = (cfd && nint < 2 * nb) ? 2 * nb : nint;
-    const int ngrad = (v.pb == 1) ? nuse : ncomp;
+    const int ngrad = (pb == 1) ? nuse : ncomp;
     double grad[kMaxComp];
     for (int k = 0; k < ngrad; ++k) {
       const double y0 = v.Phi[k * P + c];
@@ -591,9 +595,9 @@ struct SweepGrad {
       const double gp = has_gp ? v.phiF[k * FP + fp_idx] : 0.;
       const double gm = has_gm ? v.phiF[k * FP + fm_idx] : 0.;
       grad[k] = limit_grad1(lim, gp, gm, yp, ym, h0, hp, hm);
-      if (v.pb == 0) v.gP[k * P + c] = grad[k];
+      if (pb == 0) v.gP[k * P + c] = grad[k];
     }
-    if (v.pb == 1) {
+    if (pb == 1) {
       // Flux_sortant of the two faces, dual normal velocity, face lengths
       const long long n0 = (long long)i * (v.nx + 1) + j;
       double Fa, Fb, fa_v, fb_v, flen;
@@ -1360,7 +1364,8 @@ __global__ void __launch_bounds__(kBX* kBY) k_lag_cells(RunView v) { plain_items
 __global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { plain_items(v, FaceGrad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_grad(RunView v, int sweep) { plain_items(v, O3Grad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_ystar(RunView v, int sweep) { plain_items(v, O3Ystar{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) { plain_items(v, SweepGrad{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) { plain_items(v, SweepGradT<0>{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_grad_pb(RunView v, int sweep) { plain_items(v, SweepGradT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFaceT<2>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdate{sweep}); }
@@ -1398,7 +1403,7 @@ __device__ __forceinline__ void batch_items(const BatchArgs& b, const F& f) {
 __global__ void __launch_bounds__(kBatchThreads) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdate{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
@@ -1466,7 +1471,10 @@ int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* 
   // limited slopes feed the order-2 face values and PenteBorne only
   if (v.order == 2 || (v.order == 3 && v.pb == 1)) {
     H(11); k_face_grad<<<fg, blk, 0, s>>>(v, sweep); ++nk;
-    H(4); k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk;
+    H(4);
+    if (v.pb == 1) k_sweep_grad_pb<<<cg, blk, 0, s>>>(v, sweep);
+    else k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep);
+    ++nk;
   }
   if (v.order == 3) {
     H(16); k_o3_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk;
