@@ -66,6 +66,7 @@ struct BatchPlan {
   long long h_ntiles[2][kNumTileShapes] = {};
   std::vector<int> h_done;
   int blocks_per_sm[kNumPhases] = {};
+  int occ_variant = 0;  // the kernel variant blocks_per_sm was measured for
   // chosen configuration
   int shape[kNumPhases] = {};
   int mode[kNumPhases] = {};
@@ -121,13 +122,19 @@ void fill_launch(BatchPlan* p) {
       L.tiles[on][w] = p->d_tiles[on][w];
       L.ntiles[on][w] = p->d_ntiles + on * kNumTileShapes + w;
     }
+  L.any_order2 = 0;
+  L.variant = kBatchNoOrder3 | kBatchNoPB;
+  for (auto* r : p->runs) {
+    if (r->v.order > 1) L.any_order2 = 1;
+    if (r->v.order == 3) L.variant &= ~kBatchNoOrder3;
+    if (r->v.pb == 1) L.variant &= ~kBatchNoPB;
+  }
+  if (L.variant != p->occ_variant && batch_occupancy(p->blocks_per_sm, L.variant) == 0)
+    p->occ_variant = L.variant;
   for (int ph = 0; ph < kNumPhases; ++ph) {
     L.shape[ph] = p->shape[ph];
     L.grid[ph] = grid_for(p, ph, p->shape[ph], p->mode[ph]);
   }
-  L.any_order2 = 0;
-  for (auto* r : p->runs)
-    if (r->v.order > 1) L.any_order2 = 1;
 }
 
 void make_tiles(const std::vector<hydro_run*>& runs, int on_nodes, int w,
@@ -219,7 +226,7 @@ int set_members(BatchPlan* p, hydro_run* const* runs, int n) {
                                  sizeof(Tile) * tiles[on][w].size(),
                                  cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaStreamSynchronize(s));
-  const int old_order2 = p->L.any_order2;
+  const int old_order2 = p->L.any_order2, old_variant = p->L.variant;
   p->runs = rv;
   p->cells = cells;
   p->h_done.assign(n, 0);
@@ -228,7 +235,8 @@ int set_members(BatchPlan* p, hydro_run* const* runs, int n) {
   fill_launch(p);
   // the persistent grids do not depend on the membership; one-block-per-tile
   // grids and the slope phases do
-  if (memcmp(old_grid, p->L.grid, sizeof(old_grid)) || old_order2 != p->L.any_order2)
+  if (memcmp(old_grid, p->L.grid, sizeof(old_grid)) || old_order2 != p->L.any_order2 ||
+      old_variant != p->L.variant)
     drop_graph(p);
   return 0;
 }
@@ -244,7 +252,7 @@ int get_plan(hydro_ctx* ctx, hydro_run* const* runs, int n, BatchPlan** out) {
   if (!ctx->plan) {
     auto* p = new BatchPlan();
     p->ctx = ctx;
-    if (batch_occupancy(p->blocks_per_sm)) {
+    if (batch_occupancy(p->blocks_per_sm, 0)) {
       delete p;
       return fail(-3, "batch: occupancy query failed");
     }

@@ -20,7 +20,7 @@ int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook);
 void launch_node_mass(const RunView& v, cudaStream_t s);
 int launch_euc_out_pressure(const RunView& v, double* out, cudaStream_t s);
 int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s, const LaunchHook* hook);
-int batch_occupancy(int* blocks_per_sm);
+int batch_occupancy(int* blocks_per_sm, int variant);
 int measure_fp64_peak(int device, double* tflops);
 
 #define CUDA_TRY(expr)                                                       \

@@ -217,7 +217,11 @@ struct BatchLaunch {
   int shape[kNumPhases];  // tile shape index per phase
   int grid[kNumPhases];   // persistent grid size per phase
   int any_order2;         // launch the slope phases
+  int variant;            // kBatch* bits: lighter kernels when no run needs
+                          // the order-3 faces / the PenteBorne slopes
 };
+constexpr int kBatchNoOrder3 = 1;
+constexpr int kBatchNoPB = 2;
 
 }  // namespace hydro
 

@@ -1404,7 +1404,9 @@ __global__ void __launch_bounds__(kBatchThreads) kb_lag_nodes(BatchArgs b) { bat
 __global__ void __launch_bounds__(kBatchThreads) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_face_lo(BatchArgs b) { batch_items(b, SweepFaceT<2>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdate{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
@@ -1534,9 +1536,19 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
   for (int sweep = 1; sweep <= 2; ++sweep) {
     if (L.any_order2) {
       H(11); kb_face_grad<<<L.grid[kPhFaceGrad], T, 0, s>>>(args(kPhFaceGrad, sweep)); ++nk;
-      H(4); kb_sweep_grad<<<L.grid[kPhSweepGrad], T, 0, s>>>(args(kPhSweepGrad, sweep)); ++nk;
+      H(4);
+      if (L.variant & kBatchNoPB)
+        kb_sweep_grad_nopb<<<L.grid[kPhSweepGrad], T, 0, s>>>(args(kPhSweepGrad, sweep));
+      else
+        kb_sweep_grad<<<L.grid[kPhSweepGrad], T, 0, s>>>(args(kPhSweepGrad, sweep));
+      ++nk;
     }
-    H(5); kb_sweep_face<<<L.grid[kPhSweepFace], T, 0, s>>>(args(kPhSweepFace, sweep)); ++nk;
+    H(5);
+    if (L.variant & kBatchNoOrder3)
+      kb_sweep_face_lo<<<L.grid[kPhSweepFace], T, 0, s>>>(args(kPhSweepFace, sweep));
+    else
+      kb_sweep_face<<<L.grid[kPhSweepFace], T, 0, s>>>(args(kPhSweepFace, sweep));
+    ++nk;
     H(6); kb_sweep_update<<<L.grid[kPhSweepUpdate], T, 0, s>>>(args(kPhSweepUpdate, sweep)); ++nk;
     H(7); kb_dual_grad<<<L.grid[kPhDualGrad], T, 0, s>>>(args(kPhDualGrad, sweep)); ++nk;
     H(8); kb_dual_update<<<L.grid[kPhDualUpdate], T, 0, s>>>(args(kPhDualUpdate, sweep)); ++nk;
@@ -1549,11 +1561,13 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
 
 // Resident blocks per SM of each batched phase kernel at kBatchThreads
 // threads (for the persistent grid sizes).
-int batch_occupancy(int* blocks_per_sm) {
+int batch_occupancy(int* blocks_per_sm, int variant) {
   const void* fns[kNumPhases] = {
       (const void*)kb_lag_nodes,   (const void*)kb_lag_cells,
-      (const void*)kb_face_grad,   (const void*)kb_sweep_grad,
-      (const void*)kb_sweep_face,  (const void*)kb_sweep_update,
+      (const void*)kb_face_grad,
+      (variant & kBatchNoPB) ? (const void*)kb_sweep_grad_nopb : (const void*)kb_sweep_grad,
+      (variant & kBatchNoOrder3) ? (const void*)kb_sweep_face_lo : (const void*)kb_sweep_face,
+      (const void*)kb_sweep_update,
       (const void*)kb_dual_grad,   (const void*)kb_dual_update,
       (const void*)kb_final};
   for (int ph = 0; ph < kNumPhases; ++ph) {
