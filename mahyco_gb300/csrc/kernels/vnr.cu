@@ -1254,13 +1254,14 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     atomicOr(&C.err, HYDRO_ERR_NAN);
     atomicMin((unsigned long long*)&C.err_cell, (unsigned long long)c);
   }
-  // EOS after the remap
+  // EOS after the remap.  A perfect gas's sound speed only matters to the
+  // mean-pressure step when rho <= 0 (otherwise the mixture's replaces the
+  // maximum), and nothing else reads it: it is formed only then.
   double pm[3], cm[3];
   for (int m = 0; m < nb; m++) {
     if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
       const double g = gamma_of(v, m);
       pm[m] = (g - 1.0) * rhom[m] * emo[m];
-      cm[m] = sqrt(g * (g - 1.0) * emo[m]);
     } else {
       pm[m] = v.pm[m * P + c];
       cm[m] = v.cm[m * P + c];
@@ -1269,13 +1270,19 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     }
   }
   double p = 0., cc = v.c[c];
-  for (int m = 0; m < nb; m++) {
-    p += f[m] * pm[m];
-    cc = smax(cc, cm[m]);
-  }
+  for (int m = 0; m < nb; m++) p += f[m] * pm[m];
   if (pos(rho)) {
     const double g0 = v.gamma[0];
     cc = sqrt(g0 * (g0 - 1.0) * e);
+  } else {
+    for (int m = 0; m < nb; m++) {
+      if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
+        const double g = gamma_of(v, m);
+        cm[m] = sqrt(g * (g - 1.0) * emo[m]);
+        v.cm[m * P + c] = cm[m];
+      }
+      cc = smax(cc, cm[m]);
+    }
   }
   for (int m = 0; m < nb; m++)
     if (eos_of(v, m) == HYDRO_EOS_VOID) e += mf[m] * emo[m];
@@ -1289,7 +1296,6 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     v.rhom[m * P + c] = rhom[m];
     v.em[m * P + c] = emo[m];
     v.pm[m * P + c] = pm[m];
-    v.cm[m * P + c] = cm[m];
   }
   // reductions feeding the next cycle
   if (v.sans_lagrange == 0) {
