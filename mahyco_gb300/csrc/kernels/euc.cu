@@ -516,7 +516,8 @@ struct EucCells {
         v.Phi[(2 * nb + m) * P + c] = nz(U[nb + m]) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
       if (v.conservative == 1) v.Phi[(3 * nb + 2) * P + c] = qdiv(U[3 * nb + 2], sm);
     } else {
-      for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv(U[k], vol);
+      const SharedDiv Sv = shared_div(vol);  // one denominator, ncomp quotients
+      for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv_shared(Sv, U[k]);
     }
   }
 };

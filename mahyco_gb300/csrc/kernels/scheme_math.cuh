@@ -171,6 +171,57 @@ HD double mul_pow2m(double x) {
     return from_bits(b - ((unsigned long long)K << 52));
   return mul_pow2m_call<K>(x);
 }
+// Several numerators over one denominator, each result the IEEE quotient
+// a / b bit for bit.  y = 1 / b is formed once by the IEEE division (so it is
+// the correctly rounded reciprocal); per numerator q0 = a * y is corrected
+// twice with exact residuals, q <- q + (a - b q) y (fused multiply-adds).
+// q0 is within two ulps of a / b, the first correction brings it within one
+// ulp, and then (Markstein's theorem: with y = RN(1/b) and q within one ulp
+// of a / b, RN(q + (a - bq) y) = RN(a / b), the residual a - bq being exact)
+// the second gives the correctly rounded quotient.  The theorem needs no
+// underflow or overflow in any step: operands whose exponents lie outside
+// [-500, 500], zeros, subnormals, infinities and NaNs take the IEEE division.
+struct SharedDiv {
+  double b, y;
+  bool ok;
+};
+HD bool div_safe_exp(double x) {
+  const unsigned e = (unsigned)(ubits(x) >> 52) & 0x7ffu;
+  return e - (1023u - 500u) <= 1000u;  // 523 <= e <= 1523
+}
+HD SharedDiv shared_div(double b) {
+  SharedDiv S;
+  S.b = b;
+  S.ok = div_safe_exp(b);
+  S.y = S.ok ? 1.0 / b : 0.0;
+  return S;
+}
+HD double fma_rn(double a, double b, double c) {
+#ifdef __CUDA_ARCH__
+  return __fma_rn(a, b, c);
+#else
+  return __builtin_fma(a, b, c);
+#endif
+}
+HD double div_shared(const SharedDiv& S, double a) {
+  if (!(S.ok && div_safe_exp(a))) return ddiv_call(a, S.b);
+  const double q0 = a * S.y;
+  const double q1 = fma_rn(fma_rn(-q0, S.b, a), S.y, q0);
+  return fma_rn(fma_rn(-q1, S.b, a), S.y, q1);
+}
+// qdiv's exact shortcuts (0 / d, x / 1, x / x), then div_shared
+HD double qdiv_shared(const SharedDiv& S, double n) {
+  const unsigned long long nb = ubits(n);
+  const unsigned long long db = ubits(S.b);
+  const bool dfin = ((db >> 52) & 0x7ffull) != 0x7ffull;
+  const bool dnz = (db << 1) != 0ull;
+  if ((nb << 1) == 0ull && dnz && dfin)
+    return from_bits((nb ^ db) & 0x8000000000000000ull);
+  if (db == 0x3ff0000000000000ull) return n;
+  if (nb == db && dnz && dfin) return 1.0;
+  return div_shared(S, n);
+}
+
 // x / k for k = 1, 2 or 4, as the exact multiplication by 1/k (division by
 // a power of two and multiplication by its reciprocal round identically).
 HD double div_pow2(double x, int k) {

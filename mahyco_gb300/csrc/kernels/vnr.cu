@@ -433,7 +433,8 @@ struct LagCells {
       }
       v.Phi[3 * nb * P + c] = q_new;
     } else {
-      for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv(U[k], vol);
+      const SharedDiv Sv = shared_div(vol);  // one denominator, ncomp quotients
+      for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv_shared(Sv, U[k]);
     }
     v.vL[c] = vol;
     v.rL[c] = rho_new;
@@ -944,7 +945,8 @@ struct SweepUpdate {
           for (int k = 3 * nb; k < ncomp; ++k) Phi[k * P + c] = qdiv(U[k], sm);
       } else {
         const double vl = v.vL[c];
-        for (int k = 0; k < ncomp; ++k) Phi[k * P + c] = qdiv(U[k], vl);
+        const SharedDiv Sv = shared_div(vl);  // one denominator, ncomp quotients
+        for (int k = 0; k < ncomp; ++k) Phi[k * P + c] = qdiv_shared(Sv, U[k]);
       }
       int matcell = 0, imatpure = -1;
       for (int m = 0; m < nb; m++)

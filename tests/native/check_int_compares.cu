@@ -100,6 +100,45 @@ int main() {
   }
   if (pbad) printf("exponent helpers: %ld mismatches of %ld\n", pbad, pn);
   bad += pbad;
+  // shared-denominator division against the IEEE quotient: random bit
+  // patterns (all exponents, so the fallback is exercised), operands of
+  // similar scale, and quotients next to rounding ties (a = b * m rounded,
+  // m the midpoint of two neighbouring doubles)
+  long dbad = 0, dn = 0;
+  auto check_div = [&](double a, double b) {
+    ++dn;
+    const SharedDiv S = shared_div(b);
+    if (!same(div_shared(S, a), a / b) || !same(qdiv_shared(S, a), qdiv(a, b))) {
+      if (dbad < 5) printf("div_shared(%a, %a) = %a, want %a\n", a, b, div_shared(S, a), a / b);
+      ++dbad;
+    }
+  };
+  for (double a : v)
+    for (double b : v) check_div(a, b);
+  for (int i = 0; i < 3000000; ++i) {
+    unsigned long long ba = g(), bb = g();
+    double a, b;
+    memcpy(&a, &ba, 8);
+    memcpy(&b, &bb, 8);
+    check_div(a, b);
+    a = std::ldexp(1.0 + (double)(g() >> 11) * 0x1p-53, (int)(g() % 1200) - 600);
+    b = std::ldexp(1.0 + (double)(g() >> 11) * 0x1p-53, (int)(g() % 1200) - 600);
+    if (g() & 1) a = -a;
+    if (g() & 1) b = -b;
+    check_div(a, b);
+    // near ties: q and its successor, a = RN(b * midpoint) nudged by an ulp
+    const double q = std::ldexp(1.0 + (double)(g() >> 11) * 0x1p-53, (int)(g() % 200) - 100);
+    const double mid = q + (std::nextafter(q, 1e300) - q) * 0.5;  // rounds to q or next
+    double a2 = b * mid;
+    unsigned long long x;
+    memcpy(&x, &a2, 8);
+    x += (long long)(g() % 3) - 1;
+    memcpy(&a2, &x, 8);
+    check_div(a2, b);
+    check_div(b * q, b);
+  }
+  if (dbad) printf("shared division: %ld mismatches of %ld\n", dbad, dn);
+  bad += dbad;
   // limiter on gradient pairs: specials, random, and ratios near breakpoints
   std::vector<std::pair<double, double>> pairs;
   for (double a : v)
