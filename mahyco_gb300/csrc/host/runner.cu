@@ -84,7 +84,7 @@ size_t layout(RunView& v, char* base) {
   v.dPAr = a.take<double>(nc * P);
   v.DPF = a.take<double>(nb * P);
   v.phiF = a.take<double>(nc * FP);
-  v.FFd = a.take<double>(2 * nb * P);
+  v.FFd = a.take<double>(nb * P);
   if (v.order == 3) {
     v.o3g = a.take<double>(nc * P);
     v.o3y = a.take<double>(nc * FP);

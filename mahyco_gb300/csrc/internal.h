@@ -87,7 +87,8 @@ struct RunView {
   double *dPAv, *dPAr;  // ncomp planes (plateau-slope swept integrals)
   double* DPF;        // nbmat planes (plateau-slope dual mass flux)
   double* phiF;       // ncomp face planes
-  double* FFd;        // 2*nbmat planes: dual-method flux comps, minus / plus
+  double* FFd;        // nbmat planes: each cell's share of the nodal mass
+                      // fluxes of the sweep (A1 / A2 dual methods)
   double* o3g;        // order 3: ncomp cell planes, each cell's limited-free
                       // gradient along the sweep (eval_grad); null otherwise
                       // and in batched launches, which work per face

@@ -870,6 +870,7 @@ struct SweepUpdate {
     bool has[2];
     long long fidx[2];
     double coef[2];
+    double nrm[2];  // outer normal component of face 0 / face 1 along the sweep
     const long long n0 = (long long)i * (v.nx + 1) + j;
     if (dirx) {
       has[0] = (j >= 1);
@@ -880,6 +881,8 @@ struct SweepUpdate {
       const double va = fnv_vertical(v, n0, n0 + v.nx + 1);
       const double vb = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);
       const double na = ld(v.nout, 0 * P + c), nb_ = ld(v.nout, 1 * P + c);
+      nrm[0] = na;
+      nrm[1] = nb_;
       if (v.pb == 0) {
         coef[0] = na * va * fl * dt;
         coef[1] = nb_ * vb * fl * dt;
@@ -896,6 +899,8 @@ struct SweepUpdate {
       const double va = fnv_horizontal(v, n0, n0 + 1);
       const double vb = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);
       const double na = ld(v.nout, 2 * P + c), nb_ = ld(v.nout, 3 * P + c);
+      nrm[0] = na;
+      nrm[1] = nb_;
       if (v.pb == 0) {
         coef[0] = na * va * fl * dt;
         coef[1] = nb_ * vb * fl * dt;
@@ -921,9 +926,15 @@ struct SweepUpdate {
       U[k] = Uin[k * P + c] - red;
       Uout[k * P + c] = U[k];
       if (v.scheme != HYDRO_SCHEME_EUCCLHYD && v.dual_method != 2 && k >= doff &&
-        k < doff + nb) {
-        v.FFd[(k - doff) * P + c] = F0;
-        v.FFd[(nb + k - doff) * P + c] = F1;
+          k < doff + nb) {
+        // the cell's share of the nodal mass flux (UtilesDualRemap.cc A1
+        // :10-233, A2 :401-644): the two face fluxes times their outer
+        // normals, summed; every node this cell feeds uses the same value
+        // (its two sums differ only in the order of the terms, and IEEE
+        // addition commutes)
+        double w = mul_pm1(F0, nrm[0]) + mul_pm1(F1, nrm[1]);
+        if (v.dual_method == 1) w = v.rL[c] * w;
+        v.FFd[(k - doff) * P + c] = w;
       }
     }
     if (sweep == 1) {
@@ -1062,11 +1073,6 @@ struct DualUpdate {
         }
       }
     }
-    // outer-normal planes of the near / far faces: x: plus cell (left=near,
-    // right=far), minus cell (right=near, left=far); y: plus cell (bottom,
-    // top), minus cell (top, bottom).  Plane order of nout: L.x R.x B.y T.y.
-    const int pl_pn = dirx ? 0 : 2, pl_pf = dirx ? 1 : 3;
-    const int pl_mn = dirx ? 1 : 3, pl_mf = dirx ? 0 : 2;
     double Fp = 0., Fm = 0.;
     for (int m = 0; m < nb; ++m) {
       double pp = 0., pm = 0.;
@@ -1076,18 +1082,9 @@ struct DualUpdate {
           pp += v.DPF[m * P + a];
           pm += v.DPF[m * P + b];
         } else {
-          // FFd planes: [0..nb) flux through the cell's minus face,
-          // [nb..2nb) through its plus face
-          double va = mul_pm1(v.FFd[m * P + a], ld(v.nout, pl_pn * P + a)) +
-                      mul_pm1(v.FFd[(nb + m) * P + a], ld(v.nout, pl_pf * P + a));
-          double vb = mul_pm1(v.FFd[(nb + m) * P + b], ld(v.nout, pl_mn * P + b)) +
-                      mul_pm1(v.FFd[m * P + b], ld(v.nout, pl_mf * P + b));
-          if (v.dual_method == 1) {
-            va = v.rL[a] * va;
-            vb = v.rL[b] * vb;
-          }
-          pp += va;
-          pm += vb;
+          // each cell's share, formed by k_sweep_update
+          pp += v.FFd[m * P + a];
+          pm += v.FFd[m * P + b];
         }
       }
       if (v.dual_method == 2) {
