@@ -44,10 +44,10 @@ DV double gam(const RunView& v, int m) {
 DV int eosm(const RunView& v, int m) {
   return m == 0 ? v.eos[0] : (m == 1 ? v.eos[1] : v.eos[2]);
 }
-// dot product accumulated from 0.0 (includes/Freefunctions.h:15-20)
+// dot product accumulated from 0.0 (includes/Freefunctions.h:15-20); the
+// first addition 0.0 + a0 b0 is plus_zero (integer pipe)
 DV double dot2(double a0, double a1, double b0, double b1) {
-  double r = 0.0;
-  r += a0 * b0;
+  double r = plus_zero(a0 * b0);
   r += a1 * b1;
   return r;
 }

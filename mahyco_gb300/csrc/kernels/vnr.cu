@@ -137,9 +137,10 @@ __device__ void block_reduce_minmax(unsigned long long dtv,
 DV double cell_dt(const RunView& v, long long c, int i, int j) {
   const long long n0 = (long long)i * (v.nx + 1) + j;
   const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
-  double uc = 0.0;
+  // 0.0 + x = x for the first term (a speed is >= +0)
+  double uc = quarter(ld(v.speed, nd[0]));
 #pragma unroll
-  for (int k = 0; k < 4; ++k) uc += quarter(ld(v.speed, nd[k]));
+  for (int k = 1; k < 4; ++k) uc += quarter(ld(v.speed, nd[k]));
   return ld(v.cflsq, c) / (uc + v.c[c]);
 }
 
@@ -285,9 +286,11 @@ struct LagCells {
       X[k][1] = v.XL[NP + nd[k]];
     }
     // centre and sub-volumes
-    double xc0 = 0.0, xc1 = 0.0;
+    // sums from 0.0: the first addition 0.0 + x is plus_zero(x) (integer
+    // pipe) here and below
+    double xc0 = plus_zero(X[0][0]), xc1 = plus_zero(X[0][1]);
   #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 1; k < 4; ++k) {
       xc0 = xc0 + X[k][0];
       xc1 = xc1 + X[k][1];
     }
@@ -303,7 +306,8 @@ struct LagCells {
       const double c23 = x2a * X[k][1] - x2b * X[k][0];
       const double c34 = X[k][0] * x4b - X[k][1] * x4a;
       const double c41 = x4a * xc1 - x4b * xc0;
-      vol = vol + half(c12 + c23 + c34 + c41);
+      const double t = half(c12 + c23 + c34 + c41);
+      vol = (k == 0) ? plus_zero(t) : vol + t;
     }
     const int nb = v.nbmat;
     const double thr = v.threshold;
@@ -317,7 +321,7 @@ struct LagCells {
       const double rm = v.rhom[m * P + c];
       rhom_new[m] = rm;
       if (dgt(f[m], thr)) rhom_new[m] = v.cmassm[m * P + c] / (f[m] * vol);
-      rho_new += f[m] * rhom_new[m];
+      rho_new = (m == 0) ? plus_zero(f[m] * rhom_new[m]) : rho_new + f[m] * rhom_new[m];
     }
     double e_new, q_new;
     if (v.sans_lagrange == 0) {
@@ -424,8 +428,8 @@ struct LagCells {
     U[3 * nb] = q_new * vol;  // reference slot 3*nbmat+3
     for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
     if (v.pb == 1) {
-      double sv = 0.;
-      for (int m = 0; m < nb; ++m) sv += U[m];
+      double sv = plus_zero(U[0]);
+      for (int m = 1; m < nb; ++m) sv += U[m];
       for (int m = 0; m < nb; ++m) {
         v.Phi[m * P + c] = qdiv(U[m], sv);
         v.Phi[(nb + m) * P + c] = nz(U[m]) ? qdiv(U[nb + m], U[m]) : 0.;
@@ -444,8 +448,9 @@ struct LagCells {
     for (int k = 0; k < 4; ++k) {
       const int kp = (k + 1) & 3;
       const double cr = X[k][0] * X[kp][1] - X[k][1] * X[kp][0];
-      r0 = r0 + cr * (X[k][0] + X[kp][0]);
-      r1 = r1 + cr * (X[k][1] + X[kp][1]);
+      const double t0 = cr * (X[k][0] + X[kp][0]), t1 = cr * (X[k][1] + X[kp][1]);
+      r0 = (k == 0) ? plus_zero(t0) : r0 + t0;
+      r1 = (k == 0) ? plus_zero(t1) : r1 + t1;
     }
     const double sc = 1.0 / (6.0 * vol);
     v.XcL[c] = sc * r0;
@@ -454,17 +459,15 @@ struct LagCells {
     if (v.order > 1) {
       auto len = [&](int a, int b) {
         const double d0 = X[b][0] - X[a][0], d1 = X[b][1] - X[a][1];
-        double r = 0.0;
-        r = r + d0 * d0;
+        double r = d0 * d0;  // 0.0 + a square (never -0) is the square
         r = r + d1 * d1;
         return sqrt(r);
       };
-      double hx = 0.;
-      hx += half(len(0, 1));  // bottom face
-      hx += half(len(3, 2));  // top face
-      double hy = 0.;
-      hy += half(len(1, 2));  // right face
-      hy += half(len(0, 3));  // left face
+      // lengths are >= +0: 0.0 + the first half-length is that half-length
+      double hx = half(len(0, 1));  // bottom face
+      hx += half(len(3, 2));        // top face
+      double hy = half(len(1, 2));  // right face
+      hy += half(len(0, 3));        // left face
       v.Hx[c] = hx;
       v.Hy[c] = hy;
     }
@@ -917,11 +920,11 @@ struct SweepUpdate {
       double F0 = 0., F1 = 0.;
       if (has[0]) {
         F0 = coef[0] * v.phiF[k * FP + fidx[0]];
-        red = red + F0;
+        red = plus_zero(F0);  // 0.0 + F0
       }
       if (has[1]) {
         F1 = coef[1] * v.phiF[k * FP + fidx[1]];
-        red = red + F1;
+        red = has[0] ? red + F1 : plus_zero(F1);
       }
       U[k] = Uin[k * P + c] - red;
       Uout[k * P + c] = U[k];
@@ -1075,17 +1078,14 @@ struct DualUpdate {
     }
     double Fp = 0., Fm = 0.;
     for (int m = 0; m < nb; ++m) {
+      // sums from 0.0: the first addition is plus_zero (integer pipe)
       double pp = 0., pm = 0.;
-      for (int s = 0; s < nface; ++s) {
+      const double* W = (v.dual_method == 2) ? v.DPF : v.FFd;  // FFd: each
+      for (int s = 0; s < nface; ++s) {                         // cell's share
         const long long a = cplus[s], b = cminus[s];
-        if (v.dual_method == 2) {
-          pp += v.DPF[m * P + a];
-          pm += v.DPF[m * P + b];
-        } else {
-          // each cell's share, formed by k_sweep_update
-          pp += v.FFd[m * P + a];
-          pm += v.FFd[m * P + b];
-        }
+        const double wa = W[m * P + a], wb = W[m * P + b];
+        pp = (s == 0) ? plus_zero(wa) : pp + wa;
+        pm = (s == 0) ? plus_zero(wb) : pm + wb;
       }
       if (v.dual_method == 2) {
         if (nface != 0) {
@@ -1096,8 +1096,8 @@ struct DualUpdate {
         pp = div_pow2(pp, 2 * nface);
         pm = div_pow2(pm, 2 * nface);
       }
-      Fp += pp;
-      Fm += pm;
+      Fp = (m == 0) ? plus_zero(pp) : Fp + pp;
+      Fm = (m == 0) ? plus_zero(pm) : Fm + pm;
     }
     // previous nodal conserved values and DualPhi
     const double* D = (sweep == 1) ? v.u : v.DPv;
@@ -1186,22 +1186,28 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   const double thr = v.threshold;
   const double* U = v.UL + c;  // second sweep output
   const double vol = v.euler_volume;
-  double volt = 0., masset = 0., vn[3];
-  for (int m = 0; m < nb; m++) {
+  // every sum below starts from 0.0 in the reference: its first addition
+  // 0.0 + x is plus_zero(x), on the integer pipe (materials 0 .. nb-1, nb >= 1)
+  double vn[3];
+  vn[0] = U[0];
+  double volt = plus_zero(vn[0]), masset = plus_zero(U[nb * P]);
+  for (int m = 1; m < nb; m++) {
     vn[m] = U[m * P];
     volt += vn[m];
     masset += U[(nb + m) * P];
   }
-  double vnorm = 0.;
-  for (int m = 0; m < nb; m++) {
-    vn[m] *= qdiv(vol, volt);
+  const double rv = qdiv(vol, volt);
+  vn[0] *= rv;
+  double vnorm = plus_zero(vn[0]);
+  for (int m = 1; m < nb; m++) {
+    vn[m] *= rv;
     vnorm += vn[m];
   }
   double f[3], mf[3], sf = 0.;
   for (int m = 0; m < nb; m++) {
     f[m] = qdiv(vn[m], vnorm);
     if (dlt(f[m], thr)) f[m] = 0.;
-    sf += f[m];
+    sf = (m == 0) ? plus_zero(f[m]) : sf + f[m];
   }
   for (int m = 0; m < nb; m++) f[m] = qdiv(f[m], sf);
   int matcell = 0, imatpure = -1;
@@ -1216,13 +1222,13 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   double fmt = 0.;
   for (int m = 0; m < nb; m++) {
     if (dlt(f[m], thr)) mf[m] = 0.;
-    fmt += mf[m];
+    fmt = (m == 0) ? plus_zero(mf[m]) : fmt + mf[m];
   }
   for (int m = 0; m < nb; m++) mf[m] = qdiv(mf[m], fmt);
   double dm[3] = {0., 0., 0.}, dens = 0.;
   for (int m = 0; m < nb; m++) {
     if (dgt(f[m], thr)) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
-    dens += f[m] * dm[m];
+    dens = (m == 0) ? plus_zero(f[m] * dm[m]) : dens + f[m] * dm[m];
   }
   double em[3] = {0., 0., 0.};
   for (int m = 0; m < nb; m++)
@@ -1234,7 +1240,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   v.cell_mass[c] = cmass;
   for (int m = 0; m < nb; m++) v.cmassm[m * P + c] = mf[m] * cmass;
   v.q[c] = qdiv(U[3 * nb * P], vol);
-  for (int m = 0; m < nb; m++) e += mf[m] * em[m];
+  for (int m = 0; m < nb; m++) e = (m == 0) ? plus_zero(mf[m] * em[m]) : e + mf[m] * em[m];
   double rhom[3], emo[3];
   for (int m = 0; m < nb; m++) {
     rhom[m] = dm[m];
@@ -1269,7 +1275,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     }
   }
   double p = 0., cc = v.c[c];
-  for (int m = 0; m < nb; m++) p += f[m] * pm[m];
+  for (int m = 0; m < nb; m++) p = (m == 0) ? plus_zero(f[m] * pm[m]) : p + f[m] * pm[m];
   if (pos(rho)) {
     const double g0 = v.gamma[0];
     cc = sqrt(g0 * (g0 - 1.0) * e);
