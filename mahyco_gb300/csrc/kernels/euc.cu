@@ -157,7 +157,8 @@ struct EucCellPre {
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
-        p += v.fm[m * P + c] * pm[m];
+        const double t = v.fm[m * P + c] * pm[m];
+        p = (m == 0) ? plus_zero(t) : p + t;  // 0.0 + t first
         snd = smax(snd, cm[m]);
       }
       const double rho = v.rho[c];
@@ -173,10 +174,9 @@ struct EucCellPre {
         for (int k = 0; k < 4; ++k) {
           const double u0 = v.u[nd[k]], u1 = v.u[NP + nd[k]];
           const double l0 = ldg(v.lpc, (2 * k) * P + c), l1 = ldg(v.lpc, (2 * k + 1) * P + c);
-          r14[0] = r14[0] + u0 * l0;
-          r14[1] = r14[1] + u0 * l1;
-          r14[2] = r14[2] + u1 * l0;
-          r14[3] = r14[3] + u1 * l1;
+          const double t[4] = {u0 * l0, u0 * l1, u1 * l0, u1 * l1};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) r14[q] = (k == 0) ? plus_zero(t[q]) : r14[q] + t[q];
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) v.vg[q * P + c] = qdiv(r14[q], V);
@@ -274,7 +274,8 @@ struct EucNodes {
                             dot2(v.Fs[(2 * m) * P + c], v.Fs[(2 * m + 1) * P + c], d0, d1);
           const double pe = smax(smin(maxP[m], pr), minP[m]);
           v.peex[(k * nb + m) * P + c] = pe;
-          pt += v.fm[m * P + c] * pe;
+          const double tp = v.fm[m * P + c] * pe;
+          pt = (m == 0) ? plus_zero(tp) : pt + tp;
         }
         pe_tot[t] = pt;
         v.pex[k * P + c] = pt;
@@ -316,12 +317,22 @@ struct EucNodes {
       const double mv0 = dot2(m00, m01, ue0[t], ue1[t]);
       const double mv1 = dot2(m01, m11, ue0[t], ue1[t]);
       const double l0 = ldg(v.lpc, (2 * k) * P + c), l1 = ldg(v.lpc, (2 * k + 1) * P + c);
-      G[0] = G[0] + (mv0 + l0 * pe_tot[t]);
-      G[1] = G[1] + (mv1 + l1 * pe_tot[t]);
-      Mp[0] = Mp[0] + m00;
-      Mp[1] = Mp[1] + m01;
-      Mp[2] = Mp[2] + m01;
-      Mp[3] = Mp[3] + m11;
+      const double g0 = mv0 + l0 * pe_tot[t], g1 = mv1 + l1 * pe_tot[t];
+      if (t == 0) {  // sums from 0.0: 0.0 + x as plus_zero
+        G[0] = plus_zero(g0);
+        G[1] = plus_zero(g1);
+        Mp[0] = plus_zero(m00);
+        Mp[1] = plus_zero(m01);
+        Mp[2] = Mp[1];
+        Mp[3] = plus_zero(m11);
+      } else {
+        G[0] = G[0] + g0;
+        G[1] = G[1] + g1;
+        Mp[0] = Mp[0] + m00;
+        Mp[1] = Mp[1] + m01;
+        Mp[2] = Mp[2] + m01;
+        Mp[3] = Mp[3] + m11;
+      }
     }
     // node velocity: the boundary rule of the last list holding the node
     // (sides, then corners), inverse(Mp) . G inside
@@ -386,7 +397,8 @@ struct EucCells {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int kp = (k + 1) & 3;
-      r6 = r6 + cross2(X[k][0], X[k][1], X[kp][0], X[kp][1]);
+      const double t = cross2(X[k][0], X[k][1], X[kp][0], X[kp][1]);
+      r6 = (k == 0) ? plus_zero(t) : r6 + t;
     }
     const double vol = half(r6);
     v.vL[c] = vol;
@@ -395,8 +407,9 @@ struct EucCells {
     for (int k = 0; k < 4; ++k) {
       const int kp = (k + 1) & 3;
       const double cr = cross2(X[k][0], X[k][1], X[kp][0], X[kp][1]);
-      r7a = r7a + (X[k][0] + X[kp][0]) * cr;
-      r7b = r7b + (X[k][1] + X[kp][1]) * cr;
+      const double ta = (X[k][0] + X[kp][0]) * cr, tb = (X[k][1] + X[kp][1]) * cr;
+      r7a = (k == 0) ? plus_zero(ta) : r7a + ta;
+      r7b = (k == 0) ? plus_zero(tb) : r7b + tb;
     }
     const double sc = 1.0 / (6.0 * vol);
     v.XcL[c] = r7a * sc;
@@ -406,11 +419,10 @@ struct EucCells {
         const double d0 = X[b][0] - X[a][0], d1 = X[b][1] - X[a][1];
         return sqrt(dot2(d0, d1, d0, d1));
       };
-      double hx = 0.;
-      hx += half(len(0, 1));
+      // lengths are >= +0: 0.0 + the first half-length is that half-length
+      double hx = half(len(0, 1));
       hx += half(len(3, 2));
-      double hy = 0.;
-      hy += half(len(1, 2));
+      double hy = half(len(1, 2));
       hy += half(len(0, 3));
       v.Hx[c] = hx;
       v.Hy[c] = hy;
@@ -429,7 +441,8 @@ struct EucCells {
       un0[k] = u0;
       un1[k] = u1;
       const double l0 = ldg(v.lpc, (2 * k) * P + c), l1 = ldg(v.lpc, (2 * k + 1) * P + c);
-      r2 = r2 + dot2(l0, l1, u0, u1);
+      const double t2 = dot2(l0, l1, u0, u1);
+      r2 = (k == 0) ? plus_zero(t2) : r2 + t2;
       const double du0 = u0 - v.uex[(2 * k) * P + c];
       const double du1 = u1 - v.uex[(2 * k + 1) * P + c];
       const double c00 = ldg(v.cmat, (3 * k) * P + c), c01 = ldg(v.cmat, (3 * k + 1) * P + c),
@@ -439,8 +452,8 @@ struct EucCells {
         const double mp = -v.pex[k * P + c];
         const double f0 = l0 * mp + dot2(m00, m01, du0, du1);
         const double f1 = l1 * mp + dot2(m01, m11, du0, du1);
-        r3a = r3a + f0;
-        r3b = r3b + f1;
+        r3a = (k == 0) ? plus_zero(f0) : r3a + f0;
+        r3b = (k == 0) ? plus_zero(f1) : r3b + f1;
       }
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
@@ -465,9 +478,10 @@ struct EucCells {
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
-        pr4[m] = pr4[m] + dot2(Fe0[k][m], Fe1[k][m], d0, d1);
-        fsa[m] = fsa[m] + Fe0[k][m];
-        fsb[m] = fsb[m] + Fe1[k][m];
+        const double t4 = dot2(Fe0[k][m], Fe1[k][m], d0, d1);
+        pr4[m] = (k == 0) ? plus_zero(t4) : pr4[m] + t4;
+        fsa[m] = (k == 0) ? plus_zero(Fe0[k][m]) : fsa[m] + Fe0[k][m];
+        fsb[m] = (k == 0) ? plus_zero(Fe1[k][m]) : fsb[m] + Fe1[k][m];
       }
     }
     // per-material corner-force sums for the next cycle's gradients
@@ -539,8 +553,8 @@ struct EucFinal {
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
       vn[m] = U[m * P];
-      volt += vn[m];
-      masset += U[(nb + m) * P];
+      volt = (m == 0) ? plus_zero(vn[m]) : volt + vn[m];  // 0.0 + x first
+      masset = (m == 0) ? plus_zero(U[(nb + m) * P]) : masset + U[(nb + m) * P];
     }
     double vnorm = 0.;
     const double r = qdiv(vol, volt);
@@ -548,7 +562,7 @@ struct EucFinal {
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
       vn[m] *= r;
-      vnorm += vn[m];
+      vnorm = (m == 0) ? plus_zero(vn[m]) : vnorm + vn[m];
     }
     double f[3], mf[3], sf = 0.;
 #pragma unroll
@@ -556,7 +570,7 @@ struct EucFinal {
       if (m >= nb) break;
       f[m] = qdiv(vn[m], vnorm);
       if (dlt(f[m], thr)) f[m] = 0.;
-      sf += f[m];
+      sf = (m == 0) ? plus_zero(f[m]) : sf + f[m];
     }
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
@@ -581,7 +595,7 @@ struct EucFinal {
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
       if (dlt(f[m], thr)) mf[m] = 0.;
-      fmt += mf[m];
+      fmt = (m == 0) ? plus_zero(mf[m]) : fmt + mf[m];
     }
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
@@ -593,7 +607,7 @@ struct EucFinal {
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
       if (dgt(f[m], thr)) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
-      dens += f[m] * dm[m];
+      dens = (m == 0) ? plus_zero(f[m] * dm[m]) : dens + f[m] * dm[m];
     }
     const double mv = dens * vol;
     const double un0 = qdiv(U[3 * nb * P], mv), un1 = qdiv(U[(3 * nb + 1) * P], mv);
@@ -615,7 +629,7 @@ struct EucFinal {
       rhom[m] = dm[m];
       em[m] = pe[m];
       em[m] += dec;
-      e += mf[m] * em[m];
+      e = (m == 0) ? plus_zero(mf[m] * em[m]) : e + mf[m] * em[m];
     }
 #pragma unroll
     for (int m = 0; m < 3; ++m) {

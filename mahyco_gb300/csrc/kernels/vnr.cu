@@ -161,8 +161,9 @@ struct LagNodes {
     if (i < v.ny && j > 0) { cells[k] = (long long)i * v.nx + j - 1; loc[k++] = 1; }
     if (i > 0 && j < v.nx) { cells[k] = (long long)(i - 1) * v.nx + j; loc[k++] = 3; }
     if (i > 0 && j > 0) { cells[k] = (long long)(i - 1) * v.nx + j - 1; loc[k++] = 2; }
-    double msum = 0.0;
-    for (int t = 0; t < k; ++t) msum = msum + v.cell_mass[cells[t]];
+    // sums from 0.0: first addition as plus_zero (k >= 1 cells)
+    double msum = plus_zero(v.cell_mass[cells[0]]);
+    for (int t = 1; t < k; ++t) msum = msum + v.cell_mass[cells[t]];
     const double m = div_pow2(msum, k);  // msum / k, k in {1, 2, 4}
     v.node_mass[p] = m;
 
@@ -178,18 +179,20 @@ struct LagNodes {
           const double C0 = ld(v.cqs, (2 * loc[t]) * v.pitch + c);
           const double C1 = ld(v.cqs, (2 * loc[t] + 1) * v.pitch + c);
           const double w = v.p[c] + v.q[c];
+          double t0, t1;
           if (!sym) {
-            r0 = r0 + w * C0;
-            r1 = r1 + w * C1;
+            t0 = w * C0;
+            t1 = w * C1;
           } else {
-            double d = 0.0;
-            d = d + C0 * sx;
+            double d = plus_zero(C0 * sx);
             d = d + C1 * sy;
             const double s2 = dbl(d);
             const double sv0 = sx * s2 - C0, sv1 = sy * s2 - C1;
-            r0 = r0 + w * (C0 + sv0);
-            r1 = r1 + w * (C1 + sv1);
+            t0 = w * (C0 + sv0);
+            t1 = w * (C1 + sv1);
           }
+          r0 = (t == 0) ? plus_zero(t0) : r0 + t0;
+          r1 = (t == 0) ? plus_zero(t1) : r1 + t1;
         }
       };
       const double u0x = ux, u0y = uy;
@@ -657,13 +660,13 @@ struct SweepGradT {
       // derived fluxes
       auto finish = [&](double* F, double ppv, double* out) {
         if (v.pb_complet == 1) {
-          double sfm = 0., sfv = 0.;
-          for (int m = 0; m < nb; m++) sfv += F[m];
+          double sfm = 0., sfv = plus_zero(F[0]);
+          for (int m = 1; m < nb; m++) sfv += F[m];
           if (dgt(fabs(sfv), v.threshold)) {
             for (int m = 0; m < nb; m++) {
               if (!vp) F[nb + m] = (F[nb + m] / sfv) * F[m];
               F[2 * nb + m] = (F[2 * nb + m] / sfv) * F[nb + m];
-              sfm += F[nb + m];
+              sfm = (m == 0) ? plus_zero(F[nb + m]) : sfm + F[nb + m];
             }
             if (euc)
               for (int k = 3 * nb; k < ncomp; ++k) F[k] = (F[k] / sfv) * sfm;
@@ -677,8 +680,8 @@ struct SweepGradT {
           for (int m = 0; m < nb; m++) {
             if (!vp) F[nb + m] = v.Phi[(nb + m) * P + c] * F[m];
             F[2 * nb + m] = v.Phi[(2 * nb + m) * P + c] * F[nb + m];
-            sfm += F[nb + m];
-            sfv += F[m];
+            sfm = (m == 0) ? plus_zero(F[nb + m]) : sfm + F[nb + m];
+            sfv = (m == 0) ? plus_zero(F[m]) : sfv + F[m];
           }
           if (euc)
             for (int k = 3 * nb; k < ncomp; ++k) F[k] = v.Phi[k * P + c] * sfm;
