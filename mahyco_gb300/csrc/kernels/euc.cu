@@ -157,7 +157,7 @@ struct EucCellPre {
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
-        const double t = v.fm[m * P + c] * pm[m];
+        const double t = mul_frac(v.fm[m * P + c], pm[m]);
         p = (m == 0) ? plus_zero(t) : p + t;  // 0.0 + t first
         snd = smax(snd, cm[m]);
       }
@@ -189,7 +189,7 @@ struct EucCellPre {
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
-        v.cmassm[m * P + c] = v.mfm[m * P + c] * cmass;
+        v.cmassm[m * P + c] = mul_frac(v.mfm[m * P + c], cmass);
       }
       const double u0 = v.uc[c], u1 = v.uc[P + c];
       const double un = sqrt(dot2(u0, u1, u0, u1));
@@ -274,7 +274,7 @@ struct EucNodes {
                             dot2(v.Fs[(2 * m) * P + c], v.Fs[(2 * m + 1) * P + c], d0, d1);
           const double pe = smax(smin(maxP[m], pr), minP[m]);
           v.peex[(k * nb + m) * P + c] = pe;
-          const double tp = v.fm[m * P + c] * pe;
+          const double tp = mul_frac(v.fm[m * P + c], pe);
           pt = (m == 0) ? plus_zero(tp) : pt + tp;
         }
         pe_tot[t] = pt;
@@ -507,7 +507,7 @@ struct EucCells {
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
       const double mf = v.mfm[m * P + c];
-      U[m] = v.fm[m * P + c] * vol;
+      U[m] = mul_frac(v.fm[m * P + c], vol);
       U[nb + m] = mf * vol * rhoL;
       U[2 * nb + m] = mf * vol * rhoL * peL[m];
     }
@@ -607,7 +607,8 @@ struct EucFinal {
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
       if (dgt(f[m], thr)) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
-      dens = (m == 0) ? plus_zero(f[m] * dm[m]) : dens + f[m] * dm[m];
+      const double fd = mul_frac(f[m], dm[m]);
+      dens = (m == 0) ? plus_zero(fd) : dens + fd;
     }
     const double mv = dens * vol;
     const double un0 = qdiv(U[3 * nb * P], mv), un1 = qdiv(U[(3 * nb + 1) * P], mv);
@@ -629,7 +630,8 @@ struct EucFinal {
       rhom[m] = dm[m];
       em[m] = pe[m];
       em[m] += dec;
-      e = (m == 0) ? plus_zero(mf[m] * em[m]) : e + mf[m] * em[m];
+      const double te = mul_frac(mf[m], em[m]);
+      e = (m == 0) ? plus_zero(te) : e + te;
     }
 #pragma unroll
     for (int m = 0; m < 3; ++m) {

@@ -249,6 +249,16 @@ HD double plus_zero(double x) {
   if (b == 0x8000000000000000ull) return 0.0;
   return is_nan(x) ? x + 0.0 : x;
 }
+// f * x for a volume or mass fraction f: in single-material cells the
+// fractions are exactly 1 or +0, and the product is x or the IEEE product's
+// signed zero (NaN for a non-finite x), decided on the integer pipe
+HD double mul_frac(double f, double x) {
+  const unsigned long long b = ubits(f);
+  if (b == 0x3ff0000000000000ull) return x;
+  if (b == 0ull && is_finite(x)) return from_bits(ubits(x) & ~kMag);
+  return f * x;
+}
+
 // x * n, with n = +1 or -1 (the outer normals of the Cartesian Euler mesh)
 // decided on the integer pipe: x or -x, exactly the IEEE products
 HD double mul_pm1(double x, double n) {

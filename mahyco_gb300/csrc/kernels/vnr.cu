@@ -324,7 +324,8 @@ struct LagCells {
       const double rm = v.rhom[m * P + c];
       rhom_new[m] = rm;
       if (dgt(f[m], thr)) rhom_new[m] = v.cmassm[m * P + c] / (f[m] * vol);
-      rho_new = (m == 0) ? plus_zero(f[m] * rhom_new[m]) : rho_new + f[m] * rhom_new[m];
+      const double fr = mul_frac(f[m], rhom_new[m]);
+      rho_new = (m == 0) ? plus_zero(fr) : rho_new + fr;
     }
     double e_new, q_new;
     if (v.sans_lagrange == 0) {
@@ -351,7 +352,7 @@ struct LagCells {
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
         const double qm_old = v.qm[m * P + c];
-        const double qm_new = f[m] * q_new;
+        const double qm_new = mul_frac(f[m], q_new);
         v.qm[m * P + c] = qm_new;
         const double rn = rhom_new[m], ro = v.rhom[m * P + c];
         em_new[m] = 0.;
@@ -371,7 +372,7 @@ struct LagCells {
           const double den = 1 + half(gamma_of(v, m) - 1.0) * rn * dvi;
           const double num = v.em[m * P + c] - (half(v.pm[m * P + c]) + pseudo) * dvi;
           em_new[m] = num / den;
-          e_new += mf[m] * em_new[m];
+          e_new += mul_frac(mf[m], em_new[m]);
           if (pos(v.energy_limit) && abs_gt(em_new[m], v.energy_limit)) bad = true;
         }
       }
@@ -424,9 +425,10 @@ struct LagCells {
   #pragma unroll
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
-      U[m] = f[m] * vol;
-      U[nb + m] = mf[m] * vol * rho_new;
-      U[2 * nb + m] = mf[m] * vol * rho_new * e_new;
+      U[m] = mul_frac(f[m], vol);
+      const double mv = mul_frac(mf[m], vol);  // (mf * vol) * rho_new ...
+      U[nb + m] = mv * rho_new;
+      U[2 * nb + m] = mv * rho_new * e_new;
     }
     U[3 * nb] = q_new * vol;  // reference slot 3*nbmat+3
     for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
@@ -1231,7 +1233,8 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   double dm[3] = {0., 0., 0.}, dens = 0.;
   for (int m = 0; m < nb; m++) {
     if (dgt(f[m], thr)) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
-    dens = (m == 0) ? plus_zero(f[m] * dm[m]) : dens + f[m] * dm[m];
+    const double fd = mul_frac(f[m], dm[m]);
+    dens = (m == 0) ? plus_zero(fd) : dens + fd;
   }
   double em[3] = {0., 0., 0.};
   for (int m = 0; m < nb; m++)
@@ -1241,9 +1244,12 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   double e = 0.;
   const double cmass = v.euler_volume * rho;
   v.cell_mass[c] = cmass;
-  for (int m = 0; m < nb; m++) v.cmassm[m * P + c] = mf[m] * cmass;
+  for (int m = 0; m < nb; m++) v.cmassm[m * P + c] = mul_frac(mf[m], cmass);
   v.q[c] = qdiv(U[3 * nb * P], vol);
-  for (int m = 0; m < nb; m++) e = (m == 0) ? plus_zero(mf[m] * em[m]) : e + mf[m] * em[m];
+  for (int m = 0; m < nb; m++) {
+    const double t = mul_frac(mf[m], em[m]);
+    e = (m == 0) ? plus_zero(t) : e + t;
+  }
   double rhom[3], emo[3];
   for (int m = 0; m < nb; m++) {
     rhom[m] = dm[m];
@@ -1278,7 +1284,10 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     }
   }
   double p = 0., cc = v.c[c];
-  for (int m = 0; m < nb; m++) p = (m == 0) ? plus_zero(f[m] * pm[m]) : p + f[m] * pm[m];
+  for (int m = 0; m < nb; m++) {
+    const double t = mul_frac(f[m], pm[m]);
+    p = (m == 0) ? plus_zero(t) : p + t;
+  }
   if (pos(rho)) {
     const double g0 = v.gamma[0];
     cc = sqrt(g0 * (g0 - 1.0) * e);

@@ -75,6 +75,8 @@ int main() {
     bad += !same(dbl(a), 2.0 * a);
     bad += !same(plus_zero(a), a + 0.0);
     for (int k = 0; k < 3; ++k) bad += !same(mul_012(k, a), (double)k * a);
+    for (double f : {1.0, 0.0, -0.0, 0.5, 0.25, 1e-300})
+      bad += !same(mul_frac(f, a), f * a);
     for (double n : {1.0, -1.0, 0.5, -2.0, 3.0, 0.0, -0.0})
       bad += !same(mul_pm1(a, n), a * n) + !same(mul_pm1(n, a), n * a);
     if (!std::isnan(a)) {
