@@ -613,14 +613,14 @@ struct SweepGradT {
       if (dirx) {
         fa_v = fnv_vertical(v, n0, n0 + v.nx + 1);          // left face
         fb_v = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);      // right face
-        Fa = ld(v.nout, 0 * P + c) * fa_v;
-        Fb = ld(v.nout, 1 * P + c) * fb_v;
+        Fa = mul_pm1(fa_v, ld(v.nout, 0 * P + c));
+        Fb = mul_pm1(fb_v, ld(v.nout, 1 * P + c));
         flen = half(ld(v.flv, i) + ld(v.flv, i));
       } else {
         fa_v = fnv_horizontal(v, n0, n0 + 1);               // bottom face
         fb_v = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);  // top face
-        Fa = ld(v.nout, 2 * P + c) * fa_v;
-        Fb = ld(v.nout, 3 * P + c) * fb_v;
+        Fa = mul_pm1(fa_v, ld(v.nout, 2 * P + c));
+        Fb = mul_pm1(fb_v, ld(v.nout, 3 * P + c));
         flen = half(ld(v.flh, j) + ld(v.flh, j));
       }
       const double fdual = half(fa_v + fb_v);
@@ -639,10 +639,11 @@ struct SweepGradT {
         if (nonneg((yp - y0) * (ym - y0))) {
           // "formule 16" (UtilesRemap-Impl.h:201-203): the reference replaces
           // every integral of this component by y0 * swept length, so the
-          // reconstruction is not built
-          fa_ = y0 * ppa;
-          fb_ = y0 * ppb;
-          fd_ = y0 * ppd;
+          // reconstruction is not built (y0, a volume fraction here, is
+          // mostly exactly 1 or 0: mul_frac)
+          fa_ = mul_frac(y0, ppa);
+          fb_ = mul_frac(y0, ppb);
+          fd_ = dual_k ? mul_frac(y0, ppd) : 0.;
         } else {
           const PPShape sh = pp_shape(plim, v.threshold, y0, yp, ym, hh, hp, hm, grad[k]);
           fa_ = (k < nint) ? pp_integral(sh, half(-hh), half(-hh) + ppa, hh, y0, yp, ym, ppa) : 0.;
@@ -680,8 +681,9 @@ struct SweepGradT {
         } else {
           double sfv = 0., sfm = 0.;
           for (int m = 0; m < nb; m++) {
-            if (!vp) F[nb + m] = v.Phi[(nb + m) * P + c] * F[m];
-            F[2 * nb + m] = v.Phi[(2 * nb + m) * P + c] * F[nb + m];
+            // an absent material's volume flux is exactly 0 (mul_frac)
+            if (!vp) F[nb + m] = mul_frac(F[m], v.Phi[(nb + m) * P + c]);
+            F[2 * nb + m] = mul_frac(F[nb + m], v.Phi[(2 * nb + m) * P + c]);
             sfm = (m == 0) ? plus_zero(F[nb + m]) : sfm + F[nb + m];
             sfv = (m == 0) ? plus_zero(F[m]) : sfv + F[m];
           }
