@@ -332,7 +332,9 @@ struct LagCells {
       const double rho_old = v.rho[c];
       const double irho_new = 1.0 / rho_new, irho_old = 1.0 / rho_old;
       const double tau = half(irho_new + irho_old);
-      const double divu_new = C.rdt_np1 * (irho_new - irho_old) / tau;
+      // qdiv: the density, hence the divergence, is unchanged where the
+      // flow has not arrived (0 / tau)
+      const double divu_new = qdiv(C.rdt_np1 * (irho_new - irho_old), tau);
       const double c_old = v.c[c];
       if (neg(v.divu[c])) {
         const double s0 = ld(v.s0, c);
@@ -371,7 +373,7 @@ struct LagCells {
           if (v.pseudo_centree == 0) pseudo = qm_new;
           const double den = 1 + half(gamma_of(v, m) - 1.0) * rn * dvi;
           const double num = v.em[m * P + c] - (half(v.pm[m * P + c]) + pseudo) * dvi;
-          em_new[m] = num / den;
+          em_new[m] = qdiv(num, den);  // den is exactly 1 at rest
           e_new += mul_frac(mf[m], em_new[m]);
           if (pos(v.energy_limit) && abs_gt(em_new[m], v.energy_limit)) bad = true;
         }
@@ -1167,11 +1169,12 @@ struct DualUpdate {
       v.UD1[p] = Un0;
       v.UD1[NP + p] = Un1;
       v.UD1[2 * NP + p] = Un2;
-      v.DPv[p] = Un0 / Un2;
-      v.DPv[NP + p] = Un1 / Un2;
+      // qdiv: momentum is exactly 0 wherever the flow has not arrived
+      v.DPv[p] = qdiv(Un0, Un2);
+      v.DPv[NP + p] = qdiv(Un1, Un2);
     } else {
       // remapVariables node part (vnr_remap/PhaseRemapFinal.cc:207-234)
-      const double ux = Un0 / Un2, uy = Un1 / Un2;
+      const double ux = qdiv(Un0, Un2), uy = qdiv(Un1, Un2);
       v.u[p] = ux;
       v.u[NP + p] = uy;
       v.speed[p] = sqrt(ux * ux + uy * uy);
