@@ -169,6 +169,7 @@ HD double mul_pow2m(double x) {
   const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
   if (e - (unsigned)(K + 1) < 0x7feu - (unsigned)K)  // K < e < 0x7ff
     return from_bits(b - ((unsigned long long)K << 52));
+  if ((b << 1) == 0ull) return x;  // +-0 * 2^-K = +-0
   return mul_pow2m_call<K>(x);
 }
 // Several numerators over one denominator, each result the IEEE quotient
@@ -241,6 +242,7 @@ HD double dbl(double x) {
   const unsigned long long b = ubits(x);
   const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
   if (e - 1u < 0x7fdu) return from_bits(b + (1ull << 52));  // 1 <= e <= 0x7fd
+  if ((b << 1) == 0ull) return x;  // 2 * +-0 = +-0
   return dbl_slow(x);
 }
 // x + 0.0 (turns -0 into +0; NaN through the FP64 addition)
