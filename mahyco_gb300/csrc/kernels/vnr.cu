@@ -538,6 +538,26 @@ struct FaceGrad {
 // Limited slopes and plateau-slope integrals of one sweep
 // (Remap::computeGradPhiFace{1,2} + computeGradPhi{1,2},
 // remap/PhaseRemap1.cc:22-323, remap/PhaseRemap2.cc:21-323).
+// The plateau-slope reconstruction of one component and its integrals over
+// the back / front swept lengths and the dual length (computeFluxPP,
+// remap/UtilesRemap-Impl.h:182-257).  Only cells where the component is not
+// at an extremum need it (the others take "formule 16"): kept out of line so
+// that the slope kernel carries neither its registers nor its code.
+struct PPFluxes {
+  double a, b, d;
+};
+__device__ __noinline__ PPFluxes pp_fluxes_call(int plim, double thr, double y0, double yp,
+                                                double ym, double hh, double hp, double hm,
+                                                double grad, double ppa, double ppb, double ppd,
+                                                bool do_ab, bool dual_k) {
+  const PPShape sh = pp_shape(plim, thr, y0, yp, ym, hh, hp, hm, grad);
+  PPFluxes r;
+  r.a = do_ab ? pp_integral(sh, half(-hh), half(-hh) + ppa, hh, y0, yp, ym, ppa) : 0.;
+  r.b = do_ab ? pp_integral(sh, half(hh) - ppb, half(hh), hh, y0, yp, ym, ppb) : 0.;
+  r.d = dual_k ? pp_integral(sh, 0., ppd, hh, y0, yp, ym, ppd) : 0.;
+  return r;
+}
+
 // PB: 2 = the run's option decides (batched launches), 0 / 1 = compiled
 // for runs without / with PenteBorne only (plain launches).
 template <int PB>
@@ -647,10 +667,11 @@ struct SweepGradT {
           fb_ = mul_frac(y0, ppb);
           fd_ = dual_k ? mul_frac(y0, ppd) : 0.;
         } else {
-          const PPShape sh = pp_shape(plim, v.threshold, y0, yp, ym, hh, hp, hm, grad[k]);
-          fa_ = (k < nint) ? pp_integral(sh, half(-hh), half(-hh) + ppa, hh, y0, yp, ym, ppa) : 0.;
-          fb_ = (k < nint) ? pp_integral(sh, half(hh) - ppb, half(hh), hh, y0, yp, ym, ppb) : 0.;
-          fd_ = dual_k ? pp_integral(sh, 0., ppd, hh, y0, yp, ym, ppd) : 0.;
+          const PPFluxes r = pp_fluxes_call(plim, v.threshold, y0, yp, ym, hh, hp, hm, grad[k],
+                                            ppa, ppb, ppd, k < nint, dual_k);
+          fa_ = r.a;
+          fb_ = r.b;
+          fd_ = r.d;
         }
         if (k < nint) {
           Fr[k] = fa_;
