@@ -1415,7 +1415,7 @@ __global__ void __launch_bounds__(kBX* kBY) k_o3_grad(RunView v, int sweep) { pl
 __global__ void __launch_bounds__(kBX* kBY) k_o3_ystar(RunView v, int sweep) { plain_items(v, O3Ystar{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) { plain_items(v, SweepGradT<0>{sweep}); }
 // six resident blocks (measured faster than the register-limited four or five)
-__global__ void __launch_bounds__(kBX* kBY, 6) k_sweep_grad_pb(RunView v, int sweep) { plain_items(v, SweepGradT<1>{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY, 8) k_sweep_grad_pb(RunView v, int sweep) { plain_items(v, SweepGradT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFaceT<2>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdate{sweep}); }
