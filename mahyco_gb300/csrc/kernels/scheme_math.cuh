@@ -345,9 +345,23 @@ HD double flux_limiter_pp(int id, double gp, double gm, double yp, double ym,
 // onto a breakpoint give the same constant).  Opposite signs give phi = 0
 // for both.  Anything else (NaN, infinities, other limiters) takes the
 // reference's two divisions.  The result is bit-identical in every case.
+// the generalised limiters out of line: runs use one limiter, and the
+// minmod / superBee kernels need not carry these registers
+#ifdef __CUDA_ARCH__
+static __device__ __noinline__ double flux_limiter_pp_call(int id, double gp, double gm,
+                                                           double yp, double ym, double h0,
+                                                           double hp, double hm) {
+  return flux_limiter_pp(id, gp, gm, yp, ym, h0, hp, hm);
+}
+#else
+static inline double flux_limiter_pp_call(int id, double gp, double gm, double yp, double ym,
+                                          double h0, double hp, double hm) {
+  return flux_limiter_pp(id, gp, gm, yp, ym, h0, hp, hm);
+}
+#endif
 HD double limit_grad1(int id, double gp, double gm, double yp, double ym,
                       double h0, double hp, double hm) {
-  if (id >= HYDRO_LIM_MINMODG) return flux_limiter_pp(id, gp, gm, yp, ym, h0, hp, hm);
+  if (id >= HYDRO_LIM_MINMODG) return flux_limiter_pp_call(id, gp, gm, yp, ym, h0, hp, hm);
   if ((id == HYDRO_LIM_MINMOD || id == HYDRO_LIM_SUPERBEE) && is_finite(gp) &&
       is_finite(gm)) {
     // every case needs at most one quotient: q = gp / gm gives phi(r1)

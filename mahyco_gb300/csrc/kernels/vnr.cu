@@ -1414,14 +1414,15 @@ __global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { 
 __global__ void __launch_bounds__(kBX* kBY) k_o3_grad(RunView v, int sweep) { plain_items(v, O3Grad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_ystar(RunView v, int sweep) { plain_items(v, O3Ystar{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) { plain_items(v, SweepGradT<0>{sweep}); }
-// six resident blocks (measured faster than the register-limited four or five)
+// eight resident blocks: the kernel waits on memory more than it computes
+// at rest; measured faster than the register-limited four to six
 __global__ void __launch_bounds__(kBX* kBY, 8) k_sweep_grad_pb(RunView v, int sweep) { plain_items(v, SweepGradT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFaceT<2>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdate{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY) k_final(RunView v) { plain_items(v, Final{}); }
+__global__ void __launch_bounds__(kBX* kBY, 10) k_final(RunView v) { plain_items(v, Final{}); }
 
 // Batched launches: a persistent grid walks the tile table; every thread of
 // a block works on the same tile (the final phase's block reduction relies
