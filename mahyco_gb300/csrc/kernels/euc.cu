@@ -415,10 +415,7 @@ struct EucCells {
     v.XcL[c] = r7a * sc;
     v.XcL[P + c] = r7b * sc;
     if (v.order > 1) {
-      auto len = [&](int a, int b) {
-        const double d0 = X[b][0] - X[a][0], d1 = X[b][1] - X[a][1];
-        return sqrt(dot2(d0, d1, d0, d1));
-      };
+      auto len = [&](int a, int b) { return face_len(X[b][0] - X[a][0], X[b][1] - X[a][1]); };
       // lengths are >= +0: 0.0 + the first half-length is that half-length
       double hx = half(len(0, 1));
       hx += half(len(3, 2));

@@ -210,6 +210,19 @@ HD double div_shared(const SharedDiv& S, double a) {
   const double q1 = fma_rn(fma_rn(-q0, S.b, a), S.y, q0);
   return fma_rn(fma_rn(-q1, S.b, a), S.y, q1);
 }
+// A face length as the reference forms it, sqrt(0.0 + a*a + b*b).  For an
+// axis-aligned face (one component exactly zero) it is |a| (or |b|): the
+// sum is the single square, and sqrt(RN(x*x)) = |x| for binary floating
+// point with correct rounding whenever x*x neither overflows nor
+// underflows (exponents within [-500, 500] here; checked on 2e8 values).
+HD double face_len(double a, double b) {
+  if (iszero(b) && div_safe_exp(a)) return fabs(a);
+  if (iszero(a) && div_safe_exp(b)) return fabs(b);
+  double r = a * a;  // 0.0 + a square (never -0) is the square
+  r = r + b * b;
+  return sqrt(r);
+}
+
 // qdiv's exact shortcuts (0 / d, x / 1, x / x), then div_shared
 HD double qdiv_shared(const SharedDiv& S, double n) {
   const unsigned long long nb = ubits(n);

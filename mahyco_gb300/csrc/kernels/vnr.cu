@@ -464,12 +464,7 @@ struct LagCells {
     v.XcL[P + c] = sc * r1;
     // Lagrangian face lengths -> HvLagrange for both sweep directions
     if (v.order > 1) {
-      auto len = [&](int a, int b) {
-        const double d0 = X[b][0] - X[a][0], d1 = X[b][1] - X[a][1];
-        double r = d0 * d0;  // 0.0 + a square (never -0) is the square
-        r = r + d1 * d1;
-        return sqrt(r);
-      };
+      auto len = [&](int a, int b) { return face_len(X[b][0] - X[a][0], X[b][1] - X[a][1]); };
       // lengths are >= +0: 0.0 + the first half-length is that half-length
       double hx = half(len(0, 1));  // bottom face
       hx += half(len(3, 2));        // top face

@@ -140,6 +140,25 @@ int main() {
     check_div(b * q, b);
   }
   if (dbad) printf("shared division: %ld mismatches of %ld\n", dbad, dn);
+  // face lengths: axis-aligned (one exact zero) and general, all exponents
+  long lbad2 = 0;
+  for (int i = 0; i < 2000000; ++i) {
+    unsigned long long ba = g(), bb = g();
+    double a, b;
+    memcpy(&a, &ba, 8);
+    memcpy(&b, &bb, 8);
+    if (i % 3 == 0) b = (g() & 1) ? 0.0 : -0.0;
+    if (i % 3 == 1) a = (g() & 1) ? 0.0 : -0.0;
+    if (i % 5 == 0) a = std::ldexp(1.0 + (double)(g() >> 11) * 0x1p-53, (int)(g() % 1200) - 600);
+    double r = 0.0;
+    r = r + a * a;
+    r = r + b * b;
+    if (!same(face_len(a, b), std::sqrt(r))) {
+      if (lbad2 < 5) printf("face_len(%a, %a) = %a, want %a\n", a, b, face_len(a, b), std::sqrt(r));
+      ++lbad2;
+    }
+  }
+  bad += lbad2;
   bad += dbad;
   // limiter on gradient pairs: specials, random, and ratios near breakpoints
   std::vector<std::pair<double, double>> pairs;
