@@ -192,7 +192,7 @@ struct EucCellPre {
         v.cmassm[m * P + c] = mul_frac(v.mfm[m * P + c], cmass);
       }
       const double u0 = v.uc[c], u1 = v.uc[P + c];
-      const double un = sqrt(dot2(u0, u1, u0, u1));
+      const double un = face_len(u0, u1);  // sqrt(dot(u, u))
       const double cdt = (v.projection == 1) ? V / (ldg(v.perim, c) * (un + snd))
                                              : V / (ldg(v.perim, c) * snd);
       if (!is_nan(cdt)) dtb = ord_bits(cdt);

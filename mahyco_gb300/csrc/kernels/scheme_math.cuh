@@ -216,6 +216,7 @@ HD double div_shared(const SharedDiv& S, double a) {
 // point with correct rounding whenever x*x neither overflows nor
 // underflows (exponents within [-500, 500] here; checked on 2e8 values).
 HD double face_len(double a, double b) {
+  if (iszero(a) && iszero(b)) return 0.0;  // sqrt(+0)
   if (iszero(b) && div_safe_exp(a)) return fabs(a);
   if (iszero(a) && div_safe_exp(b)) return fabs(b);
   double r = a * a;  // 0.0 + a square (never -0) is the square

@@ -1193,7 +1193,7 @@ struct DualUpdate {
       const double ux = qdiv(Un0, Un2), uy = qdiv(Un1, Un2);
       v.u[p] = ux;
       v.u[NP + p] = uy;
-      v.speed[p] = sqrt(ux * ux + uy * uy);
+      v.speed[p] = face_len(ux, uy);  // sqrt(ux*ux + uy*uy), |ux| when uy is 0
     }
   }
 };
@@ -1391,7 +1391,7 @@ __global__ void k_node_speed(RunView v) {
   if (i > v.ny || j > v.nx) return;
   const long long p = (long long)i * (v.nx + 1) + j;
   const double ux = v.u[p], uy = v.u[v.npitch + p];
-  v.speed[p] = sqrt(ux * ux + uy * uy);
+  v.speed[p] = face_len(ux, uy);  // sqrt(ux*ux + uy*uy)
 }
 
 
