@@ -940,6 +940,7 @@ struct SweepUpdate {
     // dual-method components: masses (A1) or volumes (A2)
     const int doff = (v.dual_method == 1) ? 0 : nb;
     double U[kMaxComp];
+    bool same = true;  // every component unchanged, bit for bit
     for (int k = 0; k < ncomp; ++k) {
       double red = 0.0;
       double F0 = 0., F1 = 0.;
@@ -951,7 +952,9 @@ struct SweepUpdate {
         F1 = coef[1] * v.phiF[k * FP + fidx[1]];
         red = has[0] ? red + F1 : plus_zero(F1);
       }
-      U[k] = Uin[k * P + c] - red;
+      const double uin = Uin[k * P + c];
+      U[k] = uin - red;
+      same = same && ubits(U[k]) == ubits(uin);
       Uout[k * P + c] = U[k];
       if (v.scheme != HYDRO_SCHEME_EUCCLHYD && v.dual_method != 2 && k >= doff &&
           k < doff + nb) {
@@ -967,7 +970,13 @@ struct SweepUpdate {
     }
     if (sweep == 1) {
       double* Phi = v.Phi;
-      if (v.pb == 1) {
+      // a VNR cell whose conserved values came through the sweep unchanged
+      // keeps the Phi the Lagrange kernel formed from exactly these values
+      // with the same formulas (the pseudo-viscosity slot is not updated
+      // here in either case)
+      const bool keep = same && v.scheme == HYDRO_SCHEME_VNR;
+      if (keep) {
+      } else if (v.pb == 1) {
         double sv = 0.;
         for (int m = 0; m < nb; m++) sv += U[m];
         double sm = 0.;
