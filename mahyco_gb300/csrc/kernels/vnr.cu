@@ -170,7 +170,20 @@ struct LagNodes {
     double ux = v.u[p], uy = v.u[v.npitch + p];
     if (v.sans_lagrange == 0) {
       const double dt = half(C.dt_np1 + C.dt_n);
-      const double s = dt / m;
+      // s = dt / m, formed only when a force is not exactly zero: with dt and
+      // m positive and of moderate size, s * (+-0) is +-0 itself (the force
+      // sums cancel exactly on a mesh at rest)
+      const bool s_easy = pos(dt) && pos(m) && div_safe_exp(dt) && div_safe_exp(m);
+      double s_val = 0.0;
+      bool s_have = false;
+      auto step = [&](double r) {
+        if (s_easy && iszero(r)) return r;
+        if (!s_have) {
+          s_val = dt / m;
+          s_have = true;
+        }
+        return s_val * r;
+      };
       auto force = [&](bool sym, double sx, double sy, double& r0, double& r1) {
         r0 = 0.0;
         r1 = 0.0;
@@ -199,15 +212,15 @@ struct LagNodes {
       double r0, r1;
       if (i > 0 && i < v.ny && j > 0 && j < v.nx) {
         force(false, 0., 0., r0, r1);
-        ux = u0x + s * r0;
-        uy = u0y + s * r1;
+        ux = u0x + step(r0);
+        uy = u0y + step(r1);
       }
       // sides in the reference's order: bottom, top, left, right
       if (i == 0) {
         if (v.bc_bottom == kBcSym) {
           force(true, 1.0, 0.0, r0, r1);
-          ux = u0x + s * r0;
-          uy = u0y + s * r1;
+          ux = u0x + step(r0);
+          uy = u0y + step(r1);
         } else if (v.bc_bottom == kBcImposed) {
           ux = v.v_bottom[0];
           uy = v.v_bottom[1];
@@ -216,8 +229,8 @@ struct LagNodes {
       if (i == v.ny) {
         if (v.bc_top == kBcSym) {
           force(true, 1.0, 0.0, r0, r1);
-          ux = u0x + s * r0;
-          uy = u0y + s * r1;
+          ux = u0x + step(r0);
+          uy = u0y + step(r1);
         } else if (v.bc_top == kBcImposed) {
           ux = v.v_top[0];
           uy = v.v_top[1];
@@ -226,8 +239,8 @@ struct LagNodes {
       if (j == 0) {
         if (v.bc_left == kBcSym) {
           force(true, 0.0, 1.0, r0, r1);
-          ux = u0x + s * r0;
-          uy = u0y + s * r1;
+          ux = u0x + step(r0);
+          uy = u0y + step(r1);
         } else if (v.bc_left == kBcImposed) {
           ux = v.v_left[0];
           uy = v.v_left[1];
@@ -236,8 +249,8 @@ struct LagNodes {
       if (j == v.nx) {
         if (v.bc_right == kBcSym) {
           force(true, 0.0, 1.0, r0, r1);
-          ux = u0x + s * r0;
-          uy = u0y + s * r1;
+          ux = u0x + step(r0);
+          uy = u0y + step(r1);
         } else if (v.bc_right == kBcImposed) {
           ux = v.v_right[0];
           uy = v.v_right[1];
