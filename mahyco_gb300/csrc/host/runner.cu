@@ -97,7 +97,7 @@ size_t layout(RunView& v, char* base) {
   v.xs = a.take<double>(v.nx + 1);
   v.ys = a.take<double>(v.ny + 1);
   if (v.scheme == HYDRO_SCHEME_EUCCLHYD) {
-    v.cqs = v.cflsq = v.s0 = v.sqs0 = nullptr;
+    v.cqs = v.cflsq = v.s0 = v.sqs0 = v.geo0 = nullptr;
     v.uc = a.take<double>(2 * P);
     v.uco = a.take<double>(2 * P);
     v.vg = a.take<double>(4 * P);
@@ -111,6 +111,7 @@ size_t layout(RunView& v, char* base) {
     v.perim = a.take<double>(P);
     v.evol = a.take<double>(P);
   } else {
+    v.geo0 = a.take<double>(5 * P);
     v.cqs = a.take<double>(8 * P);
     v.cflsq = a.take<double>(P);
     v.s0 = a.take<double>(P);

@@ -262,6 +262,17 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_cells_vnr(RunView v, int t, 
       const double nr = norm2(d0, d1);
       const_cast<double*>(v.nout)[q * P + c] = (q < 2 ? d0 : d1) / nr;
     }
+    // the Lagrangian geometry of the cell at rest, by the Lagrange kernel's
+    // own function from the Euler coordinates its nodes keep then
+    {
+      const CellGeom Gr = vnr_cell_geometry(X, v.order > 1);
+      double* g0 = const_cast<double*>(v.geo0);
+      g0[c] = Gr.vol;
+      g0[P + c] = Gr.xc0;
+      g0[2 * P + c] = Gr.xc1;
+      g0[3 * P + c] = Gr.hx;
+      g0[4 * P + c] = Gr.hy;
+    }
     // cell masses (computeCellMass, PhaseLagrange.cc:14-24)
     const double cmass = v.dx * v.dy * rho;
     if (v.sans_lagrange == 0) {

@@ -275,6 +275,63 @@ HD double mul_frac(double f, double x) {
   return f * x;
 }
 
+// Lagrangian geometry of a VNR cell from its four node positions
+// (updateCellPos, computeSubVol, vnr_remap/PhaseLagrange.cc:210-296; the
+// Lagrangian centroid, vnr_remap/PrepareRemap.cc:65-90; the face lengths
+// behind HvLagrange, remap/PhaseRemap1.cc:57-71): volume (sum of the four
+// sub-volumes around the node-averaged centre), centroid, and the widths
+// along x / y (order > 1).  Sums from 0.0 start with plus_zero.
+struct CellGeom {
+  double vol, xc0, xc1, hx, hy;
+};
+HD CellGeom vnr_cell_geometry(const double X[4][2], bool widths) {
+  CellGeom G;
+  double xc0 = plus_zero(X[0][0]), xc1 = plus_zero(X[0][1]);
+#pragma unroll
+  for (int k = 1; k < 4; ++k) {
+    xc0 = xc0 + X[k][0];
+    xc1 = xc1 + X[k][1];
+  }
+  xc0 = quarter(xc0);
+  xc1 = quarter(xc1);
+  double vol = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int km = (k + 3) & 3, kp = (k + 1) & 3;
+    const double x2a = half(X[km][0] + X[k][0]), x2b = half(X[km][1] + X[k][1]);
+    const double x4a = half(X[kp][0] + X[k][0]), x4b = half(X[kp][1] + X[k][1]);
+    const double c12 = xc0 * x2b - xc1 * x2a;
+    const double c23 = x2a * X[k][1] - x2b * X[k][0];
+    const double c34 = X[k][0] * x4b - X[k][1] * x4a;
+    const double c41 = x4a * xc1 - x4b * xc0;
+    const double t = half(c12 + c23 + c34 + c41);
+    vol = (k == 0) ? plus_zero(t) : vol + t;
+  }
+  G.vol = vol;
+  double r0 = 0.0, r1 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int kp = (k + 1) & 3;
+    const double cr = X[k][0] * X[kp][1] - X[k][1] * X[kp][0];
+    const double t0 = cr * (X[k][0] + X[kp][0]), t1 = cr * (X[k][1] + X[kp][1]);
+    r0 = (k == 0) ? plus_zero(t0) : r0 + t0;
+    r1 = (k == 0) ? plus_zero(t1) : r1 + t1;
+  }
+  const double sc = 1.0 / (6.0 * vol);
+  G.xc0 = sc * r0;
+  G.xc1 = sc * r1;
+  G.hx = G.hy = 0.0;
+  if (widths) {
+    auto len = [&](int a, int b) { return face_len(X[b][0] - X[a][0], X[b][1] - X[a][1]); };
+    // lengths are >= +0: 0.0 + the first half-length is that half-length
+    G.hx = half(len(0, 1));  // bottom face
+    G.hx += half(len(3, 2)); // top face
+    G.hy = half(len(1, 2));  // right face
+    G.hy += half(len(0, 3)); // left face
+  }
+  return G;
+}
+
 // x * n, with n = +1 or -1 (the outer normals of the Cartesian Euler mesh)
 // decided on the integer pipe: x or -x, exactly the IEEE products
 HD double mul_pm1(double x, double n) {

@@ -301,30 +301,29 @@ struct LagCells {
       X[k][0] = v.XL[nd[k]];
       X[k][1] = v.XL[NP + nd[k]];
     }
-    // centre and sub-volumes
-    // sums from 0.0: the first addition 0.0 + x is plus_zero(x) (integer
-    // pipe) here and below
-    double xc0 = plus_zero(X[0][0]), xc1 = plus_zero(X[0][1]);
-  #pragma unroll
-    for (int k = 1; k < 4; ++k) {
-      xc0 = xc0 + X[k][0];
-      xc1 = xc1 + X[k][1];
+    // Lagrangian geometry; a cell whose four nodes did not move (positions
+    // equal to the Euler coordinates, bit for bit) has the geometry the
+    // set-up stored for it, formed by the same function from the same
+    // numbers
+    bool rest = v.geo0 != nullptr;
+    if (rest) {
+      const unsigned long long x0 = ubits(ld(v.xs, j)), x1 = ubits(ld(v.xs, j + 1));
+      const unsigned long long y0 = ubits(ld(v.ys, i)), y1 = ubits(ld(v.ys, i + 1));
+      rest = ubits(X[0][0]) == x0 && ubits(X[0][1]) == y0 && ubits(X[1][0]) == x1 &&
+             ubits(X[1][1]) == y0 && ubits(X[2][0]) == x1 && ubits(X[2][1]) == y1 &&
+             ubits(X[3][0]) == x0 && ubits(X[3][1]) == y1;
     }
-    xc0 = quarter(xc0);
-    xc1 = quarter(xc1);
-    double vol = 0.0;
-  #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int km = (k + 3) & 3, kp = (k + 1) & 3;
-      const double x2a = half(X[km][0] + X[k][0]), x2b = half(X[km][1] + X[k][1]);
-      const double x4a = half(X[kp][0] + X[k][0]), x4b = half(X[kp][1] + X[k][1]);
-      const double c12 = xc0 * x2b - xc1 * x2a;
-      const double c23 = x2a * X[k][1] - x2b * X[k][0];
-      const double c34 = X[k][0] * x4b - X[k][1] * x4a;
-      const double c41 = x4a * xc1 - x4b * xc0;
-      const double t = half(c12 + c23 + c34 + c41);
-      vol = (k == 0) ? plus_zero(t) : vol + t;
+    CellGeom G;
+    if (rest) {
+      G.vol = ld(v.geo0, c);
+      G.xc0 = ld(v.geo0, P + c);
+      G.xc1 = ld(v.geo0, 2 * P + c);
+      G.hx = ld(v.geo0, 3 * P + c);
+      G.hy = ld(v.geo0, 4 * P + c);
+    } else {
+      G = vnr_cell_geometry(X, v.order > 1);
     }
+    const double vol = G.vol;
     const int nb = v.nbmat;
     const double thr = v.threshold;
     double f[3], mf[3], rhom_new[3];
@@ -462,29 +461,13 @@ struct LagCells {
     }
     v.vL[c] = vol;
     v.rL[c] = rho_new;
-    // Lagrangian centroid (PrepareRemap.cc:65-90)
-    double r0 = 0.0, r1 = 0.0;
-  #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int kp = (k + 1) & 3;
-      const double cr = X[k][0] * X[kp][1] - X[k][1] * X[kp][0];
-      const double t0 = cr * (X[k][0] + X[kp][0]), t1 = cr * (X[k][1] + X[kp][1]);
-      r0 = (k == 0) ? plus_zero(t0) : r0 + t0;
-      r1 = (k == 0) ? plus_zero(t1) : r1 + t1;
-    }
-    const double sc = 1.0 / (6.0 * vol);
-    v.XcL[c] = sc * r0;
-    v.XcL[P + c] = sc * r1;
-    // Lagrangian face lengths -> HvLagrange for both sweep directions
+    // Lagrangian centroid (PrepareRemap.cc:65-90) and the widths behind
+    // HvLagrange for both sweep directions
+    v.XcL[c] = G.xc0;
+    v.XcL[P + c] = G.xc1;
     if (v.order > 1) {
-      auto len = [&](int a, int b) { return face_len(X[b][0] - X[a][0], X[b][1] - X[a][1]); };
-      // lengths are >= +0: 0.0 + the first half-length is that half-length
-      double hx = half(len(0, 1));  // bottom face
-      hx += half(len(3, 2));        // top face
-      double hy = half(len(1, 2));  // right face
-      hy += half(len(0, 3));        // left face
-      v.Hx[c] = hx;
-      v.Hy[c] = hy;
+      v.Hx[c] = G.hx;
+      v.Hy[c] = G.hy;
     }
   }
 };
