@@ -240,6 +240,12 @@ int prepare_run(const hydro_spec& spec_in, PreparedRun& pr) {
   }
   v.threshold = spec->threshold;
   v.gamma_scalar = spec->gamma_scalar;
+  for (int m = 0; m < 3; ++m) {
+    v.gm1[m] = v.gamma[m] - 1.0;
+    v.hgm1[m] = v.gm1[m] * 0.5;
+  }
+  v.g0gm1 = v.gamma[0] * v.gm1[0];
+  v.hgs1 = (v.gamma_scalar + 1) * 0.5;
   v.energy_limit = spec->energy_limit;
   v.dx = spec->dx;
   v.dy = spec->dy;

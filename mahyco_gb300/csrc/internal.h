@@ -49,6 +49,10 @@ struct RunView {
   int pseudo_centree, sans_lagrange, projection, conservative;
   int eos[3];
   double threshold, gamma[3], gamma_scalar, energy_limit;
+  // per-run constants of the EOS expressions, formed once by the same IEEE
+  // operations the per-cell expressions perform: gamma[m] - 1.0,
+  // 0.5 * (gamma[m] - 1.0), gamma[0] * (gamma[0] - 1.0), 0.5 * (gamma_scalar + 1)
+  double gm1[3], hgm1[3], g0gm1, hgs1;
   double dx, dy, euler_volume, dt_min, final_time, cfl;
   long long max_iter;
 

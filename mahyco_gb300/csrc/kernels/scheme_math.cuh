@@ -275,6 +275,49 @@ HD double mul_frac(double f, double x) {
   return f * x;
 }
 
+// a + b, a - b and a * b with the exact shortcuts of zero operands decided on
+// the integer pipe (fields at rest are mostly zeros: velocities, fluxes,
+// slopes).  IEEE, round to nearest: x + (+-0) = x for every non-NaN x != 0;
+// two zeros sum to -0 only when both are -0; x - x = +0 for finite x; a zero
+// times a finite number is the zero of the xor of the signs.  Otherwise (and
+// whenever a NaN or an infinity could decide the result) the FP64
+// instruction runs.  Bit-identical to the plain operators.
+HD double addz(double a, double b) {
+  const unsigned long long ua = ubits(a), ub = ubits(b);
+  const unsigned long long ma = ua & kMag, mb = ub & kMag;
+  if (mb == 0 && ma <= kInfBits) return from_bits(ma == 0 ? (ua & ub) : ua);
+  if (ma == 0 && mb <= kInfBits) return b;
+  if ((ua ^ ub) == ~kMag && ma < kInfBits) return 0.0;  // a + (-a)
+  return a + b;
+}
+HD double subz(double a, double b) { return addz(a, -b); }
+HD double mulz(double a, double b) {
+  const unsigned long long ua = ubits(a), ub = ubits(b);
+  const unsigned long long ma = ua & kMag, mb = ub & kMag;
+  if ((ma == 0 && mb < kInfBits) || (mb == 0 && ma < kInfBits))
+    return from_bits((ua ^ ub) & ~kMag);
+  return a * b;
+}
+// a * b with the shortcuts of mulz and of a factor exactly 1 (1 * x = x for
+// every non-NaN x)
+HD double mul1z(double a, double b) {
+  constexpr unsigned long long kOne = 0x3ff0000000000000ull;
+  const unsigned long long ua = ubits(a), ub = ubits(b);
+  if (ub == kOne && (ua & kMag) <= kInfBits) return a;
+  if (ua == kOne && (ub & kMag) <= kInfBits) return b;
+  return mulz(a, b);
+}
+// (a * b) * c, the zero of c decided before a * b is formed: with |a| and
+// |b| below 2^511, a * b is finite (or a zero), and its product with a zero
+// c is the zero of the xor of the three signs.
+HD double mulz3(double a, double b, double c) {
+  constexpr unsigned long long kSafe = 0x5fe0000000000000ull;  // 2^511
+  const unsigned long long ua = ubits(a), ub = ubits(b), uc = ubits(c);
+  if ((uc & kMag) == 0 && (ua & kMag) < kSafe && (ub & kMag) < kSafe)
+    return from_bits((ua ^ ub ^ uc) & ~kMag);
+  return mulz(a * b, c);
+}
+
 // Lagrangian geometry of a VNR cell from its four node positions
 // (updateCellPos, computeSubVol, vnr_remap/PhaseLagrange.cc:210-296; the
 // Lagrangian centroid, vnr_remap/PrepareRemap.cc:65-90; the face lengths

@@ -60,6 +60,12 @@ int main() {
       bad += dge(a, b) != (a >= b);
       bad += !same(smin(a, b), ref_smin(a, b));
       bad += !same(smax(a, b), ref_smax(a, b));
+      bad += !same(addz(a, b), a + b);
+      bad += !same(subz(a, b), a - b);
+      bad += !same(mulz(a, b), a * b);
+      bad += !same(mul1z(a, b), a * b);
+      for (double c : {0.0, -0.0, 1.0, -3.5})
+        bad += !same(mulz3(a, b, c), (a * b) * c) + !same(mulz3(c, a, b), (c * a) * b);
     }
   for (double a : v) {
     bad += pos(a) != (a > 0.0);
@@ -74,6 +80,8 @@ int main() {
     bad += !same(quarter(a), a * 0.25);
     bad += !same(dbl(a), 2.0 * a);
     bad += !same(plus_zero(a), a + 0.0);
+    bad += !same(addz(a, -a), a + (-a)) + !same(subz(a, a), a - a);
+    bad += !same(addz(-a, a), (-a) + a) + !same(subz(-a, -a), (-a) - (-a));
     for (int k = 0; k < 3; ++k) bad += !same(mul_012(k, a), (double)k * a);
     for (double f : {1.0, 0.0, -0.0, 0.5, 0.25, 1e-300})
       bad += !same(mul_frac(f, a), f * a);
