@@ -24,9 +24,14 @@ namespace hydro {
 constexpr unsigned long long kMag = 0x7fffffffffffffffull;
 constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
 
+// The device reinterpretation is an opaque move: a plain bit cast lets the
+// optimizer recognise the tests below (x == 0, isnan, isfinite, ...) and turn
+// them back into FP64 comparisons, which run on the FP64 pipe.
 HD unsigned long long ubits(double x) {
 #ifdef __CUDA_ARCH__
-  return (unsigned long long)__double_as_longlong(x);
+  unsigned long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
 #else
   unsigned long long b;
   __builtin_memcpy(&b, &x, sizeof b);
