@@ -146,8 +146,8 @@ DV double cell_dt(const RunView& v, long long c, int i, int j) {
   // 0.0 + x = x for the first term (a speed is >= +0)
   double uc = quarter(ld(v.speed, nd[0]));
 #pragma unroll
-  for (int k = 1; k < 4; ++k) uc += quarter(ld(v.speed, nd[k]));
-  return ld(v.cflsq, c) / (uc + v.c[c]);
+  for (int k = 1; k < 4; ++k) uc = addz(uc, quarter(ld(v.speed, nd[k])));
+  return ld(v.cflsq, c) / addz(uc, v.c[c]);
 }
 
 // ------------------------------------------------------- Lagrange: nodes
@@ -197,7 +197,7 @@ struct LagNodes {
           const long long c = cells[t];
           const double C0 = ld(v.cqs, (2 * loc[t]) * v.pitch + c);
           const double C1 = ld(v.cqs, (2 * loc[t] + 1) * v.pitch + c);
-          const double w = v.p[c] + v.q[c];
+          const double w = addz(v.p[c], v.q[c]);
           double t0, t1;
           if (!sym) {
             t0 = w * C0;
@@ -218,15 +218,15 @@ struct LagNodes {
       double r0, r1;
       if (i > 0 && i < v.ny && j > 0 && j < v.nx) {
         force(false, 0., 0., r0, r1);
-        ux = u0x + step(r0);
-        uy = u0y + step(r1);
+        ux = addz(u0x, step(r0));
+        uy = addz(u0y, step(r1));
       }
       // sides in the reference's order: bottom, top, left, right
       if (i == 0) {
         if (v.bc_bottom == kBcSym) {
           force(true, 1.0, 0.0, r0, r1);
-          ux = u0x + step(r0);
-          uy = u0y + step(r1);
+          ux = addz(u0x, step(r0));
+          uy = addz(u0y, step(r1));
         } else if (v.bc_bottom == kBcImposed) {
           ux = v.v_bottom[0];
           uy = v.v_bottom[1];
@@ -235,8 +235,8 @@ struct LagNodes {
       if (i == v.ny) {
         if (v.bc_top == kBcSym) {
           force(true, 1.0, 0.0, r0, r1);
-          ux = u0x + step(r0);
-          uy = u0y + step(r1);
+          ux = addz(u0x, step(r0));
+          uy = addz(u0y, step(r1));
         } else if (v.bc_top == kBcImposed) {
           ux = v.v_top[0];
           uy = v.v_top[1];
@@ -245,8 +245,8 @@ struct LagNodes {
       if (j == 0) {
         if (v.bc_left == kBcSym) {
           force(true, 0.0, 1.0, r0, r1);
-          ux = u0x + step(r0);
-          uy = u0y + step(r1);
+          ux = addz(u0x, step(r0));
+          uy = addz(u0y, step(r1));
         } else if (v.bc_left == kBcImposed) {
           ux = v.v_left[0];
           uy = v.v_left[1];
@@ -255,8 +255,8 @@ struct LagNodes {
       if (j == v.nx) {
         if (v.bc_right == kBcSym) {
           force(true, 0.0, 1.0, r0, r1);
-          ux = u0x + step(r0);
-          uy = u0y + step(r1);
+          ux = addz(u0x, step(r0));
+          uy = addz(u0y, step(r1));
         } else if (v.bc_right == kBcImposed) {
           ux = v.v_right[0];
           uy = v.v_right[1];
@@ -280,8 +280,8 @@ struct LagNodes {
       v.u[p] = ux;
       v.u[v.npitch + p] = uy;
     }
-    v.XL[p] = ld(v.xs, j) + C.dt_np1 * ux;
-    v.XL[v.npitch + p] = ld(v.ys, i) + C.dt_np1 * uy;
+    v.XL[p] = addz(ld(v.xs, j), mulz(C.dt_np1, ux));
+    v.XL[v.npitch + p] = addz(ld(v.ys, i), mulz(C.dt_np1, uy));
   }
 };
 
@@ -343,7 +343,7 @@ struct LagCells {
       rhom_new[m] = rm;
       if (dgt(f[m], thr)) rhom_new[m] = v.cmassm[m * P + c] / (f[m] * vol);
       const double fr = mul_frac(f[m], rhom_new[m]);
-      rho_new = (m == 0) ? plus_zero(fr) : rho_new + fr;
+      rho_new = (m == 0) ? plus_zero(fr) : addz(rho_new, fr);
     }
     double e_new, q_new;
     if (v.sans_lagrange == 0) {
@@ -414,7 +414,7 @@ struct LagCells {
             em_new[m] = qdiv(num, den);  // den is exactly 1 at rest
           }
           const double te = mul_frac(mf[m], em_new[m]);
-          e_new = e_first ? plus_zero(te) : e_new + te;
+          e_new = e_first ? plus_zero(te) : addz(e_new, te);
           e_first = false;
           if (pos(v.energy_limit) && abs_gt(em_new[m], v.energy_limit)) bad = true;
         }
@@ -469,14 +469,14 @@ struct LagCells {
       if (m >= nb) break;
       U[m] = mul_frac(f[m], vol);
       const double mv = mul_frac(mf[m], vol);  // (mf * vol) * rho_new ...
-      U[nb + m] = mv * rho_new;
-      U[2 * nb + m] = mv * rho_new * e_new;
+      U[nb + m] = mulz(mv, rho_new);
+      U[2 * nb + m] = mulz(mulz(mv, rho_new), e_new);
     }
-    U[3 * nb] = q_new * vol;  // reference slot 3*nbmat+3
+    U[3 * nb] = mulz(q_new, vol);  // reference slot 3*nbmat+3
     for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
     if (v.pb == 1) {
       double sv = plus_zero(U[0]);
-      for (int m = 1; m < nb; ++m) sv += U[m];
+      for (int m = 1; m < nb; ++m) sv = addz(sv, U[m]);
       for (int m = 0; m < nb; ++m) {
         v.Phi[m * P + c] = qdiv(U[m], sv);
         v.Phi[(nb + m) * P + c] = nz(U[m]) ? qdiv(U[nb + m], U[m]) : 0.;
@@ -1331,21 +1331,21 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   double volt = plus_zero(vn[0]), masset = plus_zero(U[nb * P]);
   for (int m = 1; m < nb; m++) {
     vn[m] = U[m * P];
-    volt += vn[m];
-    masset += U[(nb + m) * P];
+    volt = addz(volt, vn[m]);
+    masset = addz(masset, U[(nb + m) * P]);
   }
   const double rv = qdiv(vol, volt);
-  vn[0] *= rv;
+  vn[0] = mul1z(vn[0], rv);
   double vnorm = plus_zero(vn[0]);
   for (int m = 1; m < nb; m++) {
-    vn[m] *= rv;
-    vnorm += vn[m];
+    vn[m] = mul1z(vn[m], rv);
+    vnorm = addz(vnorm, vn[m]);
   }
   double f[3], mf[3], sf = 0.;
   for (int m = 0; m < nb; m++) {
     f[m] = qdiv(vn[m], vnorm);
     if (dlt(f[m], thr)) f[m] = 0.;
-    sf = (m == 0) ? plus_zero(f[m]) : sf + f[m];
+    sf = (m == 0) ? plus_zero(f[m]) : addz(sf, f[m]);
   }
   for (int m = 0; m < nb; m++) f[m] = qdiv(f[m], sf);
   int matcell = 0, imatpure = -1;
@@ -1360,14 +1360,14 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   double fmt = 0.;
   for (int m = 0; m < nb; m++) {
     if (dlt(f[m], thr)) mf[m] = 0.;
-    fmt = (m == 0) ? plus_zero(mf[m]) : fmt + mf[m];
+    fmt = (m == 0) ? plus_zero(mf[m]) : addz(fmt, mf[m]);
   }
   for (int m = 0; m < nb; m++) mf[m] = qdiv(mf[m], fmt);
   double dm[3] = {0., 0., 0.}, dens = 0.;
   for (int m = 0; m < nb; m++) {
     if (dgt(f[m], thr)) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
     const double fd = mul_frac(f[m], dm[m]);
-    dens = (m == 0) ? plus_zero(fd) : dens + fd;
+    dens = (m == 0) ? plus_zero(fd) : addz(dens, fd);
   }
   double em[3] = {0., 0., 0.};
   for (int m = 0; m < nb; m++)
@@ -1381,7 +1381,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   v.q[c] = qdiv(U[3 * nb * P], vol);
   for (int m = 0; m < nb; m++) {
     const double t = mul_frac(mf[m], em[m]);
-    e = (m == 0) ? plus_zero(t) : e + t;
+    e = (m == 0) ? plus_zero(t) : addz(e, t);
   }
   double rhom[3], emo[3];
   for (int m = 0; m < nb; m++) {
@@ -1407,7 +1407,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   double pm[3], cm[3];
   for (int m = 0; m < nb; m++) {
     if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
-      pm[m] = gm1_of(v, m) * rhom[m] * emo[m];
+      pm[m] = mulz(mulz(gm1_of(v, m), rhom[m]), emo[m]);
     } else {
       pm[m] = v.pm[m * P + c];
       cm[m] = v.cm[m * P + c];
@@ -1418,7 +1418,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   double p = 0., cc = v.c[c];
   for (int m = 0; m < nb; m++) {
     const double t = mul_frac(f[m], pm[m]);
-    p = (m == 0) ? plus_zero(t) : p + t;
+    p = (m == 0) ? plus_zero(t) : addz(p, t);
   }
   if (pos(rho)) {
     cc = sqrt(v.g0gm1 * e);
