@@ -106,6 +106,10 @@ static inline double ddiv_call(double n, double d) { return n / d; }
 //   n = d, finite non-zero       -> 1
 // (uniform and single-material cells produce many of these); otherwise the
 // IEEE division.  Bit-identical to n / d (NaN results stay NaN).
+//   d = +-2^k (normal), n normal, quotient normal -> n with its exponent
+//                                   lowered by k and the sign xor-ed
+// (a power-of-two denominator only shifts the exponent; the cell volume of a
+// mesh with 2^-j spacing is one)
 HD double qdiv(double n, double d) {
   const unsigned long long nb = ubits(n);
   const unsigned long long db = ubits(d);
@@ -115,6 +119,12 @@ HD double qdiv(double n, double d) {
     return from_bits((nb ^ db) & 0x8000000000000000ull);
   if (db == 0x3ff0000000000000ull) return n;
   if (nb == db && dnz && dfin) return 1.0;
+  const long long en = (long long)((nb >> 52) & 0x7ffull), ed = (long long)((db >> 52) & 0x7ffull);
+  const long long er = en - ed + 1023;
+  if ((db & 0xfffffffffffffull) == 0 && ed != 0 && ed != 0x7ff && en != 0 && en != 0x7ff &&
+      er >= 1 && er <= 0x7fe)
+    return from_bits(((nb ^ db) & 0x8000000000000000ull) | ((unsigned long long)er << 52) |
+                     (nb & 0xfffffffffffffull));
   return ddiv_call(n, d);
 }
 

@@ -171,7 +171,6 @@ struct LagNodes {
     double msum = plus_zero(v.cell_mass[cells[0]]);
     for (int t = 1; t < k; ++t) msum = msum + v.cell_mass[cells[t]];
     const double m = div_pow2(msum, k);  // msum / k, k in {1, 2, 4}
-    v.node_mass[p] = m;
 
     double ux = v.u[p], uy = v.u[v.npitch + p];
     if (v.sans_lagrange == 0) {
@@ -280,6 +279,8 @@ struct LagNodes {
       v.u[p] = ux;
       v.u[v.npitch + p] = uy;
     }
+    // stored last: a store earlier would order the force loads behind it
+    v.node_mass[p] = m;
     v.XL[p] = addz(ld(v.xs, j), mulz(C.dt_np1, ux));
     v.XL[v.npitch + p] = addz(ld(v.ys, i), mulz(C.dt_np1, uy));
   }
@@ -311,7 +312,14 @@ struct LagCells {
     // equal to the Euler coordinates, bit for bit) has the geometry the
     // set-up stored for it, formed by the same function from the same
     // numbers
+    // the stored geometry is loaded with the positions (its use waits on the
+    // comparison below, its latency does not)
+    double g0v[5] = {0., 0., 0., 0., 0.};
     bool rest = v.geo0 != nullptr;
+    if (rest) {
+  #pragma unroll
+      for (int q = 0; q < 5; ++q) g0v[q] = ld(v.geo0, q * P + c);
+    }
     if (rest) {
       const unsigned long long x0 = ubits(ld(v.xs, j)), x1 = ubits(ld(v.xs, j + 1));
       const unsigned long long y0 = ubits(ld(v.ys, i)), y1 = ubits(ld(v.ys, i + 1));
@@ -321,51 +329,79 @@ struct LagCells {
     }
     CellGeom G;
     if (rest) {
-      G.vol = ld(v.geo0, c);
-      G.xc0 = ld(v.geo0, P + c);
-      G.xc1 = ld(v.geo0, 2 * P + c);
-      G.hx = ld(v.geo0, 3 * P + c);
-      G.hy = ld(v.geo0, 4 * P + c);
+      G.vol = g0v[0];
+      G.xc0 = g0v[1];
+      G.xc1 = g0v[2];
+      G.hx = g0v[3];
+      G.hy = g0v[4];
     } else {
       G = vnr_cell_geometry(X, v.order > 1);
     }
     const double vol = G.vol;
     const int nb = v.nbmat;
     const double thr = v.threshold;
-    double f[3], mf[3], rhom_new[3];
+    double f[3], mf[3], rhom_new[3], rho_o[3], em_o[3], pm_o[3], qm_o[3];
     double rho_new = 0.;
+    // every value read before the first store (the stores would otherwise
+    // order the later loads behind them)
+    const double rho_old = v.rho[c], divu_old = v.divu[c], c_old = v.c[c];
+  #pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      em_o[m] = v.em[m * P + c];
+      pm_o[m] = v.pm[m * P + c];
+      qm_o[m] = v.qm[m * P + c];
+    }
   #pragma unroll
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
       f[m] = v.fm[m * P + c];
       mf[m] = v.mfm[m * P + c];
       const double rm = v.rhom[m * P + c];
+      rho_o[m] = rm;
       rhom_new[m] = rm;
-      if (dgt(f[m], thr)) rhom_new[m] = v.cmassm[m * P + c] / (f[m] * vol);
+      if (dgt(f[m], thr)) rhom_new[m] = qdiv(v.cmassm[m * P + c], mul_frac(f[m], vol));
       const double fr = mul_frac(f[m], rhom_new[m]);
       rho_new = (m == 0) ? plus_zero(fr) : addz(rho_new, fr);
     }
     double e_new, q_new;
     if (v.sans_lagrange == 0) {
-      const double rho_old = v.rho[c];
-      const double irho_old = 1.0 / rho_old;
-      // a density that came through the Lagrange phase bit for bit unchanged
-      // (a cell at rest) has the old reciprocal, and the difference of the
-      // two is then +0 (x - x, x finite)
-      const bool same_rho = ubits(rho_new) == ubits(rho_old) && is_finite(irho_old);
-      const double irho_new = same_rho ? irho_old : ddiv_call(1.0, rho_new);
-      const double tau = half(irho_new + irho_old);
-      // qdiv: the density, hence the divergence, is unchanged where the
-      // flow has not arrived (0 / tau)
-      const double divu_new = qdiv(C.rdt_np1 * (same_rho ? 0.0 : irho_new - irho_old), tau);
-      const double c_old = v.c[c];
-      if (neg(v.divu[c])) {
-        const double s0 = ld(v.s0, c);
-        q_new = 1.0 / tau *
-                (-half(ld(v.sqs0, c)) * c_old * divu_new +
-                 v.hgs1 * s0 * divu_new * divu_new);
-      } else {
+      const double rdt = C.rdt_np1;
+      // A density that came through the Lagrange phase bit for bit unchanged,
+      // positive and within [2^-1000, 2^1001) (so 1/rho is a positive finite
+      // normal number), with the previous divergence >= 0: the new
+      // divergence is rdt * (1/rho - 1/rho) / tau = rdt * (+0) / tau = +0
+      // (rdt and tau = 1/rho positive and finite), q is 0, and a material
+      // whose old and new densities are the cell's has equal reciprocals.
+      // 1/rho itself is then formed only if something else needs it.
+      const unsigned long long eo = ubits(rho_old) >> 52;  // sign and exponent
+      const bool rest = ubits(rho_new) == ubits(rho_old) && eo >= 23 && eo <= 2023 &&
+                        !neg(divu_old) && pos(rdt) && is_finite(rdt);
+      double irho_old = 0., irho_new = 0.;
+      bool have_irho = false;
+      double divu_new;
+      if (rest) {
+        divu_new = 0.0;
         q_new = 0.0;
+      } else {
+        irho_old = 1.0 / rho_old;
+        // a density unchanged has the old reciprocal, and the difference of
+        // the two is then +0 (x - x, x finite)
+        const bool same_rho = ubits(rho_new) == ubits(rho_old) && is_finite(irho_old);
+        irho_new = same_rho ? irho_old : ddiv_call(1.0, rho_new);
+        have_irho = true;
+        const double tau = half(irho_new + irho_old);
+        // qdiv: the density, hence the divergence, is unchanged where the
+        // flow has not arrived (0 / tau)
+        divu_new = qdiv(rdt * (same_rho ? 0.0 : irho_new - irho_old), tau);
+        if (neg(divu_old)) {
+          const double s0 = ld(v.s0, c);
+          q_new = 1.0 / tau *
+                  (-half(ld(v.sqs0, c)) * c_old * divu_new +
+                   v.hgs1 * s0 * divu_new * divu_new);
+        } else {
+          q_new = 0.0;
+        }
       }
       if (dgt(q_new, C.pmax_prev)) q_new = C.pmax_prev;
       v.divu[c] = divu_new;
@@ -377,24 +413,34 @@ struct LagCells {
   #pragma unroll
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
-        const double qm_old = v.qm[m * P + c];
+        const double qm_old = qm_o[m];
         const double qm_new = mul_frac(f[m], q_new);
         v.qm[m * P + c] = qm_new;
-        const double rn = rhom_new[m], ro = v.rhom[m * P + c];
+        const double rn = rhom_new[m], ro = rho_o[m];
         em_new[m] = 0.;
         if (dgt(rn, thr) && dgt(ro, thr)) {
           // 1/rho_m: in a pure cell the material density is the cell's,
-          // bit for bit, and so is its reciprocal
-          double irn, iro;
-          if (ubits(rn) == ubits(rho_new)) irn = irho_new;
-          else irn = 1.0 / rn;
-          if (ubits(ro) == ubits(rho_old)) iro = irho_old;
-          else iro = 1.0 / ro;
-          const double em_old = v.em[m * P + c], pm_old = v.pm[m * P + c];
+          // bit for bit, and so is its reciprocal (at rest both are 1/rho_old)
+          const bool rn_cell = ubits(rn) == ubits(rho_new), ro_cell = ubits(ro) == ubits(rho_old);
+          double irn = 0., iro = 0.;
+          bool eq_inv;
+          if (rest && rn_cell && ro_cell) {
+            eq_inv = true;  // both 1 / rho_old, finite; not formed
+          } else {
+            if (!have_irho && (rn_cell || ro_cell)) {
+              irho_old = ddiv_call(1.0, rho_old);
+              irho_new = irho_old;  // rest: rho_new == rho_old
+              have_irho = true;
+            }
+            irn = rn_cell ? irho_new : ddiv_call(1.0, rn);
+            iro = ro_cell ? irho_old : ddiv_call(1.0, ro);
+            eq_inv = ubits(irn) == ubits(iro) && is_finite(irn);
+          }
+          const double em_old = em_o[m], pm_old = pm_o[m];
           constexpr unsigned long long kBig = 0x7fd0000000000000ull;   // 2^1022
           constexpr unsigned long long kSafe = 0x5fe0000000000000ull;  // 2^511
           const double hg = hgm1_of(v, m);
-          if (ubits(irn) == ubits(iro) && is_finite(irn) && nz(em_old) && !is_nan(em_old) &&
+          if (eq_inv && nz(em_old) && !is_nan(em_old) &&
               (ubits(pm_old) & kMag) < kBig &&
               (v.pseudo_centree != 0 || (ubits(qm_new) & kMag) < kBig) &&
               (ubits(hg) & kMag) < kSafe && (ubits(rn) & kMag) < kSafe) {
@@ -404,7 +450,7 @@ struct LagCells {
             // em, den = 1 + (a zero) = 1 and em / 1 = em
             em_new[m] = em_old;
           } else {
-            const double dvi = irn - iro;
+            const double dvi = eq_inv ? 0.0 : irn - iro;  // x - x = +0 (finite x)
             double pseudo = 0.;
             if ((v.pseudo_centree == 1) && pos((qm_new + qm_old) * dvi))
               pseudo = half(qm_new + qm_old);
@@ -860,12 +906,33 @@ struct SweepFaceT {
         const double xf = dirx ? ld(v.xs, j) : ld(v.ys, i);
         const long long cu = pos(fnv * dxl) ? cb : cf;
         const double s = plus_zero(xf - v.XcL[ax * P + cu]);
-        for (int k = 0; k < ncomp; ++k)
-          out[k * FP] = v.Phi[k * P + cu] + s * v.gP[k * P + cu];
+        // four components at a time, loads ahead of the stores
+        for (int k0 = 0; k0 < ncomp; k0 += 4) {
+          double a[4], g[4];
+  #pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int k = k0 + t;
+            a[t] = (k < ncomp) ? v.Phi[k * P + cu] : 0.;
+            g[t] = (k < ncomp) ? v.gP[k * P + cu] : 0.;
+          }
+  #pragma unroll
+          for (int t = 0; t < 4; ++t)
+            if (k0 + t < ncomp) out[(k0 + t) * FP] = a[t] + s * g[t];
+        }
       } else {
         const long long av = dirx ? cb : cf, ar = dirx ? cf : cb;
-        for (int k = 0; k < ncomp; ++k)
-          out[k * FP] = v.dPAv[k * P + av] - v.dPAr[k * P + ar];
+        for (int k0 = 0; k0 < ncomp; k0 += 4) {
+          double a[4], b[4];
+  #pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int k = k0 + t;
+            a[t] = (k < ncomp) ? v.dPAv[k * P + av] : 0.;
+            b[t] = (k < ncomp) ? v.dPAr[k * P + ar] : 0.;
+          }
+  #pragma unroll
+          for (int t = 0; t < 4; ++t)
+            if (k0 + t < ncomp) out[(k0 + t) * FP] = a[t] - b[t];
+        }
       }
     } else {
       // order 3: six cells along the sweep, "minus" side first, clamped
@@ -984,42 +1051,58 @@ struct SweepUpdate {
     double U[kMaxComp];
     bool same = true;  // every component unchanged, bit for bit
     const bool cfin = is_finite(coef[0]) && is_finite(coef[1]);
-    for (int k = 0; k < ncomp; ++k) {
-      const double q0 = has[0] ? v.phiF[k * FP + fidx[0]] : 0.;
-      const double q1 = has[1] ? v.phiF[k * FP + fidx[1]] : 0.;
-      const double uin = Uin[k * P + c];
-      double F0 = 0., F1 = 0.;
-      if (cfin && iszero(q0) && iszero(q1) && !is_nan(uin)) {
-        // nothing crosses either face: each flux coef * q is the zero of
-        // sign(coef) xor sign(q), their sum from 0.0 is +0, and uin - +0 is
-        // uin
-        if (has[0]) F0 = from_bits((ubits(coef[0]) ^ ubits(q0)) & ~kMag);
-        if (has[1]) F1 = from_bits((ubits(coef[1]) ^ ubits(q1)) & ~kMag);
-        U[k] = uin;
-      } else {
-        double red = 0.0;
-        if (has[0]) {
-          F0 = coef[0] * q0;
-          red = plus_zero(F0);  // 0.0 + F0
-        }
-        if (has[1]) {
-          F1 = coef[1] * q1;
-          red = has[0] ? red + F1 : plus_zero(F1);
-        }
-        U[k] = uin - red;
+    const bool dual_share = v.scheme != HYDRO_SCHEME_EUCCLHYD && v.dual_method != 2;
+    const double rl = (dual_share && v.dual_method == 1) ? v.rL[c] : 0.;
+    const double vl = (sweep == 1 && v.pb != 1) ? v.vL[c] : 0.;
+    // components four at a time: the loads of a group are issued together,
+    // ahead of the group's stores (which would otherwise order each
+    // component's loads behind the previous component's stores)
+    for (int k0 = 0; k0 < ncomp; k0 += 4) {
+      double qa[4], qb[4], ui[4];
+  #pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int k = k0 + t;
+        qa[t] = (k < ncomp && has[0]) ? v.phiF[k * FP + fidx[0]] : 0.;
+        qb[t] = (k < ncomp && has[1]) ? v.phiF[k * FP + fidx[1]] : 0.;
+        ui[t] = (k < ncomp) ? Uin[k * P + c] : 0.;
       }
-      same = same && ubits(U[k]) == ubits(uin);
-      Uout[k * P + c] = U[k];
-      if (v.scheme != HYDRO_SCHEME_EUCCLHYD && v.dual_method != 2 && k >= doff &&
-          k < doff + nb) {
-        // the cell's share of the nodal mass flux (UtilesDualRemap.cc A1
-        // :10-233, A2 :401-644): the two face fluxes times their outer
-        // normals, summed; every node this cell feeds uses the same value
-        // (its two sums differ only in the order of the terms, and IEEE
-        // addition commutes)
-        double w = mul_pm1(F0, nrm[0]) + mul_pm1(F1, nrm[1]);
-        if (v.dual_method == 1) w = v.rL[c] * w;
-        v.FFd[(k - doff) * P + c] = w;
+  #pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int k = k0 + t;
+        if (k >= ncomp) break;
+        const double q0 = qa[t], q1 = qb[t], uin = ui[t];
+        double F0 = 0., F1 = 0.;
+        if (cfin && iszero(q0) && iszero(q1) && !is_nan(uin)) {
+          // nothing crosses either face: each flux coef * q is the zero of
+          // sign(coef) xor sign(q), their sum from 0.0 is +0, and uin - +0 is
+          // uin
+          if (has[0]) F0 = from_bits((ubits(coef[0]) ^ ubits(q0)) & ~kMag);
+          if (has[1]) F1 = from_bits((ubits(coef[1]) ^ ubits(q1)) & ~kMag);
+          U[k] = uin;
+        } else {
+          double red = 0.0;
+          if (has[0]) {
+            F0 = coef[0] * q0;
+            red = plus_zero(F0);  // 0.0 + F0
+          }
+          if (has[1]) {
+            F1 = coef[1] * q1;
+            red = has[0] ? red + F1 : plus_zero(F1);
+          }
+          U[k] = uin - red;
+        }
+        same = same && ubits(U[k]) == ubits(uin);
+        Uout[k * P + c] = U[k];
+        if (dual_share && k >= doff && k < doff + nb) {
+          // the cell's share of the nodal mass flux (UtilesDualRemap.cc A1
+          // :10-233, A2 :401-644): the two face fluxes times their outer
+          // normals, summed; every node this cell feeds uses the same value
+          // (its two sums differ only in the order of the terms, and IEEE
+          // addition commutes)
+          double w = mul_pm1(F0, nrm[0]) + mul_pm1(F1, nrm[1]);
+          if (v.dual_method == 1) w = rl * w;
+          v.FFd[(k - doff) * P + c] = w;
+        }
       }
     }
     if (sweep == 1) {
@@ -1046,7 +1129,7 @@ struct SweepUpdate {
         if (v.scheme == HYDRO_SCHEME_EUCCLHYD)
           for (int k = 3 * nb; k < ncomp; ++k) Phi[k * P + c] = qdiv(U[k], sm);
       } else {
-        const double vl = v.vL[c];
+        // vl: the Lagrangian volume, read with the inputs
         const SharedDiv Sv = shared_div(vl);  // one denominator, ncomp quotients
         for (int k = 0; k < ncomp; ++k) Phi[k * P + c] = qdiv_shared(Sv, U[k]);
       }
@@ -1324,15 +1407,35 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   const double thr = v.threshold;
   const double* U = v.UL + c;  // second sweep output
   const double vol = v.euler_volume;
+  // every value read up front, before the first store (stores would order
+  // the later loads behind them): the remapped volumes, masses and energies,
+  // the pseudo-viscosity, the sound speed kept for rho <= 0, and the dt
+  // candidate's inputs
+  double vn[3], Um[3], Ue[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    if (m >= nb) break;
+    vn[m] = U[m * P];
+    Um[m] = U[(nb + m) * P];
+    Ue[m] = U[(2 * nb + m) * P];
+  }
+  const double Uq = U[3 * nb * P];
+  const double c_in = v.c[c];
+  double spd[4] = {0., 0., 0., 0.}, cflsq = 0.;
+  if (v.sans_lagrange == 0) {
+    const long long n0 = (long long)i * (v.nx + 1) + j;
+    spd[0] = ld(v.speed, n0);
+    spd[1] = ld(v.speed, n0 + 1);
+    spd[2] = ld(v.speed, n0 + v.nx + 2);
+    spd[3] = ld(v.speed, n0 + v.nx + 1);
+    cflsq = ld(v.cflsq, c);
+  }
   // every sum below starts from 0.0 in the reference: its first addition
   // 0.0 + x is plus_zero(x), on the integer pipe (materials 0 .. nb-1, nb >= 1)
-  double vn[3];
-  vn[0] = U[0];
-  double volt = plus_zero(vn[0]), masset = plus_zero(U[nb * P]);
+  double volt = plus_zero(vn[0]), masset = plus_zero(Um[0]);
   for (int m = 1; m < nb; m++) {
-    vn[m] = U[m * P];
     volt = addz(volt, vn[m]);
-    masset = addz(masset, U[(nb + m) * P]);
+    masset = addz(masset, Um[m]);
   }
   const double rv = qdiv(vol, volt);
   vn[0] = mul1z(vn[0], rv);
@@ -1356,7 +1459,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     }
   v.mixte[c] = (matcell > 1) ? 1 : 0;
   v.pure[c] = (matcell > 1) ? -1 : imatpure;
-  for (int m = 0; m < nb; m++) mf[m] = qdiv(U[(nb + m) * P], masset);
+  for (int m = 0; m < nb; m++) mf[m] = qdiv(Um[m], masset);
   double fmt = 0.;
   for (int m = 0; m < nb; m++) {
     if (dlt(f[m], thr)) mf[m] = 0.;
@@ -1365,20 +1468,20 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   for (int m = 0; m < nb; m++) mf[m] = qdiv(mf[m], fmt);
   double dm[3] = {0., 0., 0.}, dens = 0.;
   for (int m = 0; m < nb; m++) {
-    if (dgt(f[m], thr)) dm[m] = qdiv(U[(nb + m) * P], vn[m]);
+    if (dgt(f[m], thr)) dm[m] = qdiv(Um[m], vn[m]);
     const double fd = mul_frac(f[m], dm[m]);
     dens = (m == 0) ? plus_zero(fd) : addz(dens, fd);
   }
   double em[3] = {0., 0., 0.};
   for (int m = 0; m < nb; m++)
-    if (dgt(f[m], thr) && nz(U[(nb + m) * P]))
-      em[m] = qdiv(U[(2 * nb + m) * P], U[(nb + m) * P]);
+    if (dgt(f[m], thr) && nz(Um[m]))
+      em[m] = qdiv(Ue[m], Um[m]);
   const double rho = dens;
   double e = 0.;
   const double cmass = v.euler_volume * rho;
   v.cell_mass[c] = cmass;
   for (int m = 0; m < nb; m++) v.cmassm[m * P + c] = mul_frac(mf[m], cmass);
-  v.q[c] = qdiv(U[3 * nb * P], vol);
+  v.q[c] = qdiv(Uq, vol);
   for (int m = 0; m < nb; m++) {
     const double t = mul_frac(mf[m], em[m]);
     e = (m == 0) ? plus_zero(t) : addz(e, t);
@@ -1415,7 +1518,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
       e = 0.;
     }
   }
-  double p = 0., cc = v.c[c];
+  double p = 0., cc = c_in;
   for (int m = 0; m < nb; m++) {
     const double t = mul_frac(f[m], pm[m]);
     p = (m == 0) ? plus_zero(t) : addz(p, t);
@@ -1447,7 +1550,12 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   }
   // reductions feeding the next cycle
   if (v.sans_lagrange == 0) {
-    const double d = cell_dt(v, c, i, j);
+    // dt candidate (Vnr::computeDeltaT, VnrRemap.cc:26-46) with this
+    // cell's new sound speed
+    double uc = quarter(spd[0]);
+  #pragma unroll
+    for (int k = 1; k < 4; ++k) uc = addz(uc, quarter(spd[k]));
+    const double d = cflsq / addz(uc, cc);
     if (!is_nan(d)) dtb = ord_bits(d) < dtb ? ord_bits(d) : dtb;
   }
   if (!is_nan(p)) pb = ord_bits(p) > pb ? ord_bits(p) : pb;
@@ -1514,7 +1622,7 @@ __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
 }
 
 __global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
-__global__ void __launch_bounds__(kBX* kBY) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
+__global__ void __launch_bounds__(kBX* kBY, 6) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { plain_items(v, FaceGrad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_grad(RunView v, int sweep) { plain_items(v, O3Grad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_ystar(RunView v, int sweep) { plain_items(v, O3Ystar{sweep}); }
