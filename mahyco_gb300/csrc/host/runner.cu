@@ -97,7 +97,8 @@ size_t layout(RunView& v, char* base) {
   v.xs = a.take<double>(v.nx + 1);
   v.ys = a.take<double>(v.ny + 1);
   if (v.scheme == HYDRO_SCHEME_EUCCLHYD) {
-    v.cqs = v.cflsq = v.s0 = v.sqs0 = v.geo0 = nullptr;
+    v.cqs = v.cflsq = v.s0 = v.sqs0 = nullptr;
+    v.geo0 = a.take<double>(5 * P);
     v.uc = a.take<double>(2 * P);
     v.uco = a.take<double>(2 * P);
     v.vg = a.take<double>(4 * P);

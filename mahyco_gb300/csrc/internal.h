@@ -93,8 +93,8 @@ struct RunView {
   double* phiF;       // ncomp face planes
   double* FFd;        // nbmat planes: each cell's share of the nodal mass
                       // fluxes of the sweep (A1 / A2 dual methods)
-  const double* geo0; // VNR: 5 cell planes, the Lagrangian geometry of the
-                      // cell at rest (volume, centroid x / y, widths x / y)
+  const double* geo0; // 5 cell planes, the Lagrangian geometry of the cell
+                      // at rest (volume, centroid x / y, widths x / y)
   double* o3g;        // order 3: ncomp cell planes, each cell's limited-free
                       // gradient along the sweep (eval_grad); null otherwise
                       // and in batched launches, which work per face

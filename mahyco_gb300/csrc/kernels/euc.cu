@@ -52,6 +52,16 @@ DV double dot2(double a0, double a1, double b0, double b1) {
   return r;
 }
 DV double cross2(double a0, double a1, double b0, double b1) { return a0 * b1 - a1 * b0; }
+// dot2 is exactly +0 when one vector is two zeros and the other finite
+// (plus_zero of a signed zero, plus a signed zero)
+DV bool dot2_zero(double a0, double a1, double b0, double b1) {
+  return (iszero(a0) && iszero(a1) && is_finite(b0) && is_finite(b1)) ||
+         (iszero(b0) && iszero(b1) && is_finite(a0) && is_finite(a1));
+}
+// x + dot2(a, b), with x + (+0) = plus_zero(x) where the product is +0
+DV double add_dot2(double x, double a0, double a1, double b0, double b1) {
+  return dot2_zero(a0, a1, b0, b1) ? plus_zero(x) : x + dot2(a0, a1, b0, b1);
+}
 
 // block-wide min of ordered encodings, one atomic per block
 DV void block_min(unsigned long long dtv, Ctrl* C) {
@@ -170,13 +180,26 @@ struct EucCellPre {
         const long long n0 = (long long)i * (v.nx + 1) + j;
         const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
         double r14[4] = {0.0, 0.0, 0.0, 0.0};
+        double cu[4][2], cl[4][2];
+        bool still = true;  // every corner velocity a zero, every l finite
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const double u0 = v.u[nd[k]], u1 = v.u[NP + nd[k]];
-          const double l0 = ldg(v.lpc, (2 * k) * P + c), l1 = ldg(v.lpc, (2 * k + 1) * P + c);
-          const double t[4] = {u0 * l0, u0 * l1, u1 * l0, u1 * l1};
+          cu[k][0] = v.u[nd[k]];
+          cu[k][1] = v.u[NP + nd[k]];
+          cl[k][0] = ldg(v.lpc, (2 * k) * P + c);
+          cl[k][1] = ldg(v.lpc, (2 * k + 1) * P + c);
+          still = still && iszero(cu[k][0]) && iszero(cu[k][1]) && is_finite(cl[k][0]) &&
+                  is_finite(cl[k][1]);
+        }
+        // then every product is a signed zero and each sum from 0.0 is +0
+        if (!still) {
 #pragma unroll
-          for (int q = 0; q < 4; ++q) r14[q] = (k == 0) ? plus_zero(t[q]) : r14[q] + t[q];
+          for (int k = 0; k < 4; ++k) {
+            const double u0 = cu[k][0], u1 = cu[k][1], l0 = cl[k][0], l1 = cl[k][1];
+            const double t[4] = {u0 * l0, u0 * l1, u1 * l0, u1 * l1};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) r14[q] = (k == 0) ? plus_zero(t[q]) : r14[q] + t[q];
+          }
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) v.vg[q * P + c] = qdiv(r14[q], V);
@@ -270,8 +293,8 @@ struct EucNodes {
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
           if (m >= nb) break;
-          const double pr = v.pm[m * P + c] +
-                            dot2(v.Fs[(2 * m) * P + c], v.Fs[(2 * m + 1) * P + c], d0, d1);
+          const double pr = add_dot2(v.pm[m * P + c], v.Fs[(2 * m) * P + c],
+                                     v.Fs[(2 * m + 1) * P + c], d0, d1);
           const double pe = smax(smin(maxP[m], pr), minP[m]);
           v.peex[(k * nb + m) * P + c] = pe;
           const double tp = mul_frac(v.fm[m * P + c], pe);
@@ -279,9 +302,8 @@ struct EucNodes {
         }
         pe_tot[t] = pt;
         v.pex[k * P + c] = pt;
-        const double mv0 = dot2(v.vg[c], v.vg[P + c], d0, d1);
-        const double mv1 = dot2(v.vg[2 * P + c], v.vg[3 * P + c], d0, d1);
-        const double vt0 = v.uc[c] + mv0, vt1 = v.uc[P + c] + mv1;
+        const double vt0 = add_dot2(v.uc[c], v.vg[c], v.vg[P + c], d0, d1);
+        const double vt1 = add_dot2(v.uc[P + c], v.vg[2 * P + c], v.vg[3 * P + c], d0, d1);
         ue0[t] = smax(smin(maxVx, vt0), minVx);
         ue1[t] = smax(smin(maxVy, vt1), minVy);
         v.uex[(2 * k) * P + c] = ue0[t];
@@ -314,10 +336,14 @@ struct EucNodes {
       const double m00 = ldg(v.cmat, (3 * k) * P + c) * s;
       const double m01 = ldg(v.cmat, (3 * k + 1) * P + c) * s;
       const double m11 = ldg(v.cmat, (3 * k + 2) * P + c) * s;
-      const double mv0 = dot2(m00, m01, ue0[t], ue1[t]);
-      const double mv1 = dot2(m01, m11, ue0[t], ue1[t]);
       const double l0 = ldg(v.lpc, (2 * k) * P + c), l1 = ldg(v.lpc, (2 * k + 1) * P + c);
-      const double g0 = mv0 + l0 * pe_tot[t], g1 = mv1 + l1 * pe_tot[t];
+      // mv + l * pe, with (+0) + y = plus_zero(y) where mv = dot2(m, ue) is +0
+      const double g0 = dot2_zero(m00, m01, ue0[t], ue1[t])
+                            ? plus_zero(l0 * pe_tot[t])
+                            : dot2(m00, m01, ue0[t], ue1[t]) + l0 * pe_tot[t];
+      const double g1 = dot2_zero(m01, m11, ue0[t], ue1[t])
+                            ? plus_zero(l1 * pe_tot[t])
+                            : dot2(m01, m11, ue0[t], ue1[t]) + l1 * pe_tot[t];
       if (t == 0) {  // sums from 0.0: 0.0 + x as plus_zero
         G[0] = plus_zero(g0);
         G[1] = plus_zero(g1);
@@ -365,12 +391,29 @@ struct EucNodes {
     } else if (bot) {
       bc_velocity(v.bc_bottom, v.v_bottom[0], v.v_bottom[1], Mp, G, u0, u1);
     } else {
-      bc_velocity(202, 0.0, 0.0, Mp, G, u0, u1);
+      // inverse(Mp) . G: with G two zeros the result is dot2(i, G) = +0 as
+      // long as the inverse is finite: |Mp| < 2^500 and |det| >= 2^-500
+      // bound it by 2^1000, so the reciprocal and the products are not
+      // formed
+      constexpr unsigned long long kLo = 523ull << 52, kHi = 1523ull << 52;
+      bool gz = iszero(G[0]) && iszero(G[1]) && (ubits(Mp[0]) & kMag) < kHi &&
+                (ubits(Mp[1]) & kMag) < kHi && (ubits(Mp[2]) & kMag) < kHi &&
+                (ubits(Mp[3]) & kMag) < kHi;
+      if (gz) {
+        const double det = Mp[0] * Mp[3] - Mp[1] * Mp[2];
+        gz = (ubits(det) & kMag) >= kLo;  // finite: |Mp| < 2^500
+      }
+      if (gz) {
+        u0 = 0.0;
+        u1 = 0.0;
+      } else {
+        bc_velocity(202, 0.0, 0.0, Mp, G, u0, u1);
+      }
     }
     v.u[p] = u0;
     v.u[NP + p] = u1;
-    v.XL[p] = X0 + u0 * C.dt_n;
-    v.XL[NP + p] = X1 + u1 * C.dt_n;
+    v.XL[p] = addz(X0, mulz(u0, C.dt_n));
+    v.XL[NP + p] = addz(X1, mulz(u1, C.dt_n));
   }
 };
 
@@ -393,38 +436,38 @@ struct EucCells {
       X[k][0] = v.XL[nd[k]];
       X[k][1] = v.XL[NP + nd[k]];
     }
-    double r6 = 0.0;
+    // Lagrangian geometry; a cell whose four nodes kept their Euler
+    // positions (bit for bit) has the geometry the set-up formed with the
+    // same function from the same numbers (loaded with the positions).
+    // The geometry is stored at the end: a store here would order every
+    // later load behind it.
+    double g0v[5];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int kp = (k + 1) & 3;
-      const double t = cross2(X[k][0], X[k][1], X[kp][0], X[kp][1]);
-      r6 = (k == 0) ? plus_zero(t) : r6 + t;
+    for (int q = 0; q < 5; ++q) g0v[q] = ldg(v.geo0, q * P + c);
+    const unsigned long long x0 = ubits(ldg(v.xs, j)), x1 = ubits(ldg(v.xs, j + 1));
+    const unsigned long long y0 = ubits(ldg(v.ys, i)), y1 = ubits(ldg(v.ys, i + 1));
+    const bool rest = ubits(X[0][0]) == x0 && ubits(X[0][1]) == y0 && ubits(X[1][0]) == x1 &&
+                      ubits(X[1][1]) == y0 && ubits(X[2][0]) == x1 && ubits(X[2][1]) == y1 &&
+                      ubits(X[3][0]) == x0 && ubits(X[3][1]) == y1;
+    CellGeom G;
+    if (rest) {
+      G.vol = g0v[0];
+      G.xc0 = g0v[1];
+      G.xc1 = g0v[2];
+      G.hx = g0v[3];
+      G.hy = g0v[4];
+    } else {
+      G = euc_cell_geometry(X, v.order > 1);
     }
-    const double vol = half(r6);
-    v.vL[c] = vol;
-    double r7a = 0.0, r7b = 0.0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int kp = (k + 1) & 3;
-      const double cr = cross2(X[k][0], X[k][1], X[kp][0], X[kp][1]);
-      const double ta = (X[k][0] + X[kp][0]) * cr, tb = (X[k][1] + X[kp][1]) * cr;
-      r7a = (k == 0) ? plus_zero(ta) : r7a + ta;
-      r7b = (k == 0) ? plus_zero(tb) : r7b + tb;
-    }
-    const double sc = 1.0 / (6.0 * vol);
-    v.XcL[c] = r7a * sc;
-    v.XcL[P + c] = r7b * sc;
-    if (v.order > 1) {
-      auto len = [&](int a, int b) { return face_len(X[b][0] - X[a][0], X[b][1] - X[a][1]); };
-      // lengths are >= +0: 0.0 + the first half-length is that half-length
-      double hx = half(len(0, 1));
-      hx += half(len(3, 2));
-      double hy = half(len(1, 2));
-      hy += half(len(0, 3));
-      v.Hx[c] = hx;
-      v.Hy[c] = hy;
-    }
-    // sub-cell forces of the cell's corners with the new node velocities
+    const double vol = G.vol;
+    // sub-cell forces of the cell's corners with the new node velocities.
+    // Zero shortcuts (where the mesh is at rest the node velocities and
+    // their differences are zeros): dot2(a, b) with b0, b1 zeros and a0, a1
+    // finite is +0 (plus_zero of a signed zero, plus a signed zero), so
+    // x + dot2 is plus_zero(x) (x + 0.0), and a product c * s with |c| and
+    // |s| under 2^511 is finite without being formed.
+    constexpr unsigned long long kSafe = 0x5fe0000000000000ull;  // 2^511
+    auto small = [](double x) { return (ubits(x) & kMag) < kSafe; };
     const double rho = v.rho[c], snd = v.c[c];
     const double s = rho * snd;
     double se[3];
@@ -438,55 +481,79 @@ struct EucCells {
       un0[k] = u0;
       un1[k] = u1;
       const double l0 = ldg(v.lpc, (2 * k) * P + c), l1 = ldg(v.lpc, (2 * k + 1) * P + c);
-      const double t2 = dot2(l0, l1, u0, u1);
-      r2 = (k == 0) ? plus_zero(t2) : r2 + t2;
-      const double du0 = u0 - v.uex[(2 * k) * P + c];
-      const double du1 = u1 - v.uex[(2 * k + 1) * P + c];
+      const bool uz = iszero(u0) && iszero(u1);
+      const bool t2z = uz && is_finite(l0) && is_finite(l1);  // dot2(l, u) = +0
+      const double t2 = t2z ? 0.0 : dot2(l0, l1, u0, u1);
+      r2 = (k == 0) ? plus_zero(t2) : (t2z ? plus_zero(r2) : r2 + t2);
+      const double ux0 = v.uex[(2 * k) * P + c], ux1 = v.uex[(2 * k + 1) * P + c];
+      // velocity differences; any zero difference gives the same dot2, so
+      // two zeros minus two zeros need not be formed
+      double du0 = 0.0, du1 = 0.0;
+      bool duz = uz && iszero(ux0) && iszero(ux1);
+      if (!duz) {
+        du0 = u0 - ux0;
+        du1 = u1 - ux1;
+        duz = iszero(du0) && iszero(du1);
+      }
       const double c00 = ldg(v.cmat, (3 * k) * P + c), c01 = ldg(v.cmat, (3 * k + 1) * P + c),
                    c11 = ldg(v.cmat, (3 * k + 2) * P + c);
+      const bool cz = duz && small(c00) && small(c01) && small(c11);
       {
-        const double m00 = c00 * s, m01 = c01 * s, m11 = c11 * s;
         const double mp = -v.pex[k * P + c];
-        const double f0 = l0 * mp + dot2(m00, m01, du0, du1);
-        const double f1 = l1 * mp + dot2(m01, m11, du0, du1);
+        double f0, f1;
+        if (cz && small(s)) {
+          f0 = plus_zero(l0 * mp);
+          f1 = plus_zero(l1 * mp);
+        } else {
+          const double m00 = c00 * s, m01 = c01 * s, m11 = c11 * s;
+          f0 = l0 * mp + dot2(m00, m01, du0, du1);
+          f1 = l1 * mp + dot2(m01, m11, du0, du1);
+        }
         r3a = (k == 0) ? plus_zero(f0) : r3a + f0;
         r3b = (k == 0) ? plus_zero(f1) : r3b + f1;
       }
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
-        const double m00 = c00 * se[m], m01 = c01 * se[m], m11 = c11 * se[m];
         const double mp = -v.peex[(k * nb + m) * P + c];
-        Fe0[k][m] = l0 * mp + dot2(m00, m01, du0, du1);
-        Fe1[k][m] = l1 * mp + dot2(m01, m11, du0, du1);
+        if (cz && small(se[m])) {
+          Fe0[k][m] = plus_zero(l0 * mp);
+          Fe1[k][m] = plus_zero(l1 * mp);
+        } else {
+          const double m00 = c00 * se[m], m01 = c01 * se[m], m11 = c11 * se[m];
+          Fe0[k][m] = l0 * mp + dot2(m00, m01, du0, du1);
+          Fe1[k][m] = l1 * mp + dot2(m01, m11, du0, du1);
+        }
       }
     }
     const double dt = C.dt_n;
     const double cmass = v.cell_mass[c];
-    const double rhoL = 1 / (1 / rho + dt / cmass * r2);
+    // (dt / cmass) * r2: a zero r2 times a finite quotient (|dt| < 2^500,
+    // |cmass| >= 2^-500) is the zero of the xor of the three signs
+    constexpr unsigned long long kLo = 523ull << 52, kHi = 1523ull << 52;  // 2^-500, 2^500
+    const bool qfin = (ubits(dt) & kMag) < kHi && (ubits(cmass) & kMag) >= kLo &&
+                      is_finite(cmass);
+    const double dr2 = (iszero(r2) && qfin) ? from_bits((ubits(dt) ^ ubits(cmass) ^ ubits(r2)) & ~kMag)
+                                            : dt / cmass * r2;
+    const double rhoL = 1 / addz(1 / rho, dr2);
     const double uc0 = v.uc[c], uc1 = v.uc[P + c];
-    const double uL0 = uc0 + r3a * dt / cmass;
-    const double uL1 = uc1 + r3b * dt / cmass;
-    const double mid0 = half(uc0 + uL0), mid1 = half(uc1 + uL1);
+    const double uL0 = addz(uc0, qdiv(mulz(r3a, dt), cmass));
+    const double uL1 = addz(uc1, qdiv(mulz(r3b, dt), cmass));
+    const double mid0 = half(addz(uc0, uL0)), mid1 = half(addz(uc1, uL1));
     double pr4[3] = {0.0, 0.0, 0.0}, fsa[3] = {0.0, 0.0, 0.0}, fsb[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const double d0 = un0[k] - mid0, d1 = un1[k] - mid1;
+      const double d0 = subz(un0[k], mid0), d1 = subz(un1[k], mid1);
+      const bool dz = iszero(d0) && iszero(d1);
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         if (m >= nb) break;
-        const double t4 = dot2(Fe0[k][m], Fe1[k][m], d0, d1);
-        pr4[m] = (k == 0) ? plus_zero(t4) : pr4[m] + t4;
+        const bool t4z = dz && is_finite(Fe0[k][m]) && is_finite(Fe1[k][m]);  // dot2 = +0
+        const double t4 = t4z ? 0.0 : dot2(Fe0[k][m], Fe1[k][m], d0, d1);
+        pr4[m] = (k == 0) ? plus_zero(t4) : (t4z ? plus_zero(pr4[m]) : pr4[m] + t4);
         fsa[m] = (k == 0) ? plus_zero(Fe0[k][m]) : fsa[m] + Fe0[k][m];
         fsb[m] = (k == 0) ? plus_zero(Fe1[k][m]) : fsb[m] + Fe1[k][m];
       }
-    }
-    // per-material corner-force sums for the next cycle's gradients
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-      if (m >= nb) break;
-      v.Fs[(2 * m) * P + c] = fsa[m];
-      v.Fs[(2 * m + 1) * P + c] = fsb[m];
     }
     double peL[3];
     const double thr = v.threshold;
@@ -495,7 +562,17 @@ struct EucCells {
       if (m >= nb) break;
       peL[m] = 0.;
       const double f = v.fm[m * P + c], cmm = v.cmassm[m * P + c];
-      if (dgt(f, thr) && nz(cmm)) peL[m] = v.em[m * P + c] + f * dt / cmm * pr4[m];
+      if (dgt(f, thr) && nz(cmm)) {
+        // ((f * dt) / cmm) * pr4: a zero pr4 times a finite quotient (|f| and
+        // |dt| below 2^250, |cmm| >= 2^-500: under 2^1000) is a signed zero
+        constexpr unsigned long long kMid = 1273ull << 52;  // 2^250
+        const double em = v.em[m * P + c];
+        const bool pz = iszero(pr4[m]) && (ubits(f) & kMag) < kMid && (ubits(dt) & kMag) < kMid &&
+                        (ubits(cmm) & kMag) >= kLo && is_finite(cmm);
+        const double w = pz ? from_bits((ubits(f) ^ ubits(dt) ^ ubits(cmm) ^ ubits(pr4[m])) & ~kMag)
+                            : f * dt / cmm * pr4[m];
+        peL[m] = addz(em, w);
+      }
     }
     // ULagrange and Phi
     const int ncomp = v.ncomp;
@@ -505,11 +582,11 @@ struct EucCells {
       if (m >= nb) break;
       const double mf = v.mfm[m * P + c];
       U[m] = mul_frac(v.fm[m * P + c], vol);
-      U[nb + m] = mf * vol * rhoL;
-      U[2 * nb + m] = mf * vol * rhoL * peL[m];
+      U[nb + m] = mulz(mulz(mf, vol), rhoL);
+      U[2 * nb + m] = mulz(mulz(mulz(mf, vol), rhoL), peL[m]);
     }
-    U[3 * nb] = vol * rhoL * uL0;
-    U[3 * nb + 1] = vol * rhoL * uL1;
+    U[3 * nb] = mulz(vol * rhoL, uL0);
+    U[3 * nb + 1] = mulz(vol * rhoL, uL1);
     if (v.conservative == 1) U[3 * nb + 2] = 0.5 * vol * rhoL * (uL0 * uL0 + uL1 * uL1);
     for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
     if (v.pb == 1) {
@@ -529,6 +606,21 @@ struct EucCells {
     } else {
       const SharedDiv Sv = shared_div(vol);  // one denominator, ncomp quotients
       for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv_shared(Sv, U[k]);
+    }
+    // per-material corner-force sums for the next cycle's gradients, and
+    // the Lagrangian geometry (volume, centroid, HvLagrange widths)
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      v.Fs[(2 * m) * P + c] = fsa[m];
+      v.Fs[(2 * m + 1) * P + c] = fsb[m];
+    }
+    v.vL[c] = vol;
+    v.XcL[c] = G.xc0;
+    v.XcL[P + c] = G.xc1;
+    if (v.order > 1) {
+      v.Hx[c] = G.hx;
+      v.Hy[c] = G.hy;
     }
   }
 };

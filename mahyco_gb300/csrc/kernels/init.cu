@@ -425,6 +425,17 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_cells_euc(RunView v, int t, 
     r13 = r13 + nrm(d);
   }
   const_cast<double*>(v.perim)[c] = r13;
+  // the Lagrangian geometry of the cell at rest, by the Lagrange kernel's
+  // own function from the Euler coordinates its nodes keep then
+  {
+    const CellGeom Gr = euc_cell_geometry(X, v.order > 1);
+    double* g0 = const_cast<double*>(v.geo0);
+    g0[c] = Gr.vol;
+    g0[P + c] = Gr.xc0;
+    g0[2 * P + c] = Gr.xc1;
+    g0[3 * P + c] = Gr.hx;
+    g0[4 * P + c] = Gr.hy;
+  }
   // initCellInternalEnergy, initCellVelocity, initDensity (Init.cc
   // :194-675); init_variant 3 of BiTriplePoint scales the regions to a 7 x 3
   // domain and gives material 3 density 0.125

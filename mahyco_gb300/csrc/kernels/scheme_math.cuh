@@ -390,6 +390,44 @@ HD CellGeom vnr_cell_geometry(const double X[4][2], bool widths) {
   return G;
 }
 
+// Lagrangian geometry of an Eucclhyd cell from its four node positions
+// (computeLagrangeVolumeAndCenterOfGravity, eucclhyd_remap/PhaseLagrange.cc
+// :671-716; the face lengths behind HvLagrange, remap/PhaseRemap1.cc:57-71):
+// volume (half the shoelace sum), centroid, widths along x / y (order > 1).
+HD CellGeom euc_cell_geometry(const double X[4][2], bool widths) {
+  CellGeom G;
+  double r6 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int kp = (k + 1) & 3;
+    const double t = X[k][0] * X[kp][1] - X[k][1] * X[kp][0];
+    r6 = (k == 0) ? plus_zero(t) : r6 + t;
+  }
+  G.vol = half(r6);
+  double r7a = 0.0, r7b = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int kp = (k + 1) & 3;
+    const double cr = X[k][0] * X[kp][1] - X[k][1] * X[kp][0];
+    const double ta = (X[k][0] + X[kp][0]) * cr, tb = (X[k][1] + X[kp][1]) * cr;
+    r7a = (k == 0) ? plus_zero(ta) : r7a + ta;
+    r7b = (k == 0) ? plus_zero(tb) : r7b + tb;
+  }
+  const double sc = 1.0 / (6.0 * G.vol);
+  G.xc0 = r7a * sc;
+  G.xc1 = r7b * sc;
+  G.hx = G.hy = 0.0;
+  if (widths) {
+    auto len = [&](int a, int b) { return face_len(X[b][0] - X[a][0], X[b][1] - X[a][1]); };
+    // lengths are >= +0: 0.0 + the first half-length is that half-length
+    G.hx = half(len(0, 1));
+    G.hx += half(len(3, 2));
+    G.hy = half(len(1, 2));
+    G.hy += half(len(0, 3));
+  }
+  return G;
+}
+
 // x * n, with n = +1 or -1 (the outer normals of the Cartesian Euler mesh)
 // decided on the integer pipe: x or -x, exactly the IEEE products
 HD double mul_pm1(double x, double n) {

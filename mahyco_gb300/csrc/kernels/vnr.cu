@@ -967,13 +967,37 @@ struct SweepFaceT {
         // interior face: gradients and interpolated values from O3Grad /
         // O3Ystar, only the parabola and its interval here
         O3Face F;
-        o3_face_dt(F, h, vdt);
+        bool have_F = false;
         const long long fst = dirx ? 1 : v.nx;  // face stride along the axis
+        // A face that does not move: its normal velocity is exactly zero, so
+        // (without PenteBorne) the sweep update multiplies its value by a
+        // zero coefficient, and the flux is a zero whatever the value, as
+        // long as it is finite.  It is: with vdt = +-0, dt finite and a
+        // positive finite upwind width, Q1 = Q2 = +-0 and the value is the
+        // interpolated one clamped into a finite interval, once the seven
+        // inputs below are finite and under 2^1000 (no sum or the factor 6
+        // overflows).  The value itself is then not formed: 0 is stored
+        // (the product's zero may differ in sign, which no later sum sees).
+        constexpr unsigned long long kMod = 2023ull << 52;  // 2^1000
+        const bool still = v.pb == 0 && iszero(fnv) && is_finite(C.dt_n) && pos(h[2]) &&
+                           is_finite(h[2]);
         for (int k = 0; k < ncomp; ++k) {
           const double ys[3] = {v.o3y[k * FP + fidx - fst], v.o3y[k * FP + fidx],
                                 v.o3y[k * FP + fidx + fst]};
-          out[k * FP] = o3_tail(F, ys, o3_value(v, sweep, k, cs[1]), o3_value(v, sweep, k, cs[2]),
-                                o3_value(v, sweep, k, cs[3]), o3_value(v, sweep, k, cs[4]));
+          const double y1 = o3_value(v, sweep, k, cs[1]), ym = o3_value(v, sweep, k, cs[2]);
+          const double yp = o3_value(v, sweep, k, cs[3]), y4 = o3_value(v, sweep, k, cs[4]);
+          if (still && ((ubits(ys[0]) & kMag) < kMod) && ((ubits(ys[1]) & kMag) < kMod) &&
+              ((ubits(ys[2]) & kMag) < kMod) && ((ubits(y1) & kMag) < kMod) &&
+              ((ubits(ym) & kMag) < kMod) && ((ubits(yp) & kMag) < kMod) &&
+              ((ubits(y4) & kMag) < kMod)) {
+            out[k * FP] = 0.0;
+            continue;
+          }
+          if (!have_F) {
+            o3_face_dt(F, h, vdt);
+            have_F = true;
+          }
+          out[k * FP] = o3_tail(F, ys, y1, ym, yp, y4);
         }
       } else {
         const O3Face F = o3_face(h, vdt);
