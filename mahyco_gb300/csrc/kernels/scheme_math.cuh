@@ -811,15 +811,17 @@ HD O3Face o3_face(const double* h, double vdt) {
   return F;
 }
 // eval_grad with its coefficients
+// (zero shortcuts: a uniform row of values gives zero differences)
 HD double o3_grad(double G0, double A, double B, double ym, double y0, double yp) {
-  return G0 * (A * (yp - y0) + B * (y0 - ym));
+  return mulz(G0, addz(mulz(A, subz(yp, y0)), mulz(B, subz(y0, ym))));
 }
 // eval_ystar with its coefficients T (o3_ystar_coef) at the face between
 // ym | yp, from the gradients of the cells on its minus / plus side
 HD double o3_ystar(const double* T, double ym, double yp, double grm, double grp) {
-  const double tmp1 = T[0] * (yp - ym);
-  const double tmp2 = T[1] * grp + T[2] * grm;
-  return ym + T[3] * (yp - ym) + T[4] * (tmp1 + tmp2);
+  const double dy = subz(yp, ym);
+  const double tmp1 = mulz(T[0], dy);
+  const double tmp2 = addz(mulz(T[1], grp), mulz(T[2], grm));
+  return addz(addz(ym, mulz(T[3], dy)), mulz(T[4], addz(tmp1, tmp2)));
 }
 // the face value from the interpolated values ys of the faces at -1, 0, +1
 // and the cell values y1 | ym | yp | y4 (ComputeFluxOrdre3's parabola and
