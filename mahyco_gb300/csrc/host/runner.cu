@@ -98,6 +98,7 @@ size_t layout(RunView& v, char* base) {
   v.ys = a.take<double>(v.ny + 1);
   if (v.scheme == HYDRO_SCHEME_EUCCLHYD) {
     v.cqs = v.cflsq = v.s0 = v.sqs0 = nullptr;
+    v.sarg = nullptr;
     v.geo0 = a.take<double>(5 * P);
     v.uc = a.take<double>(2 * P);
     v.uco = a.take<double>(2 * P);
@@ -113,6 +114,7 @@ size_t layout(RunView& v, char* base) {
     v.evol = a.take<double>(P);
   } else {
     v.geo0 = a.take<double>(5 * P);
+    v.sarg = a.take<double>(P);
     v.cqs = a.take<double>(8 * P);
     v.cflsq = a.take<double>(P);
     v.s0 = a.take<double>(P);

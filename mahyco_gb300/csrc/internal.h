@@ -28,6 +28,10 @@ constexpr int kBcPeriodic = 203;
 // energies, pseudo-viscosity.  Slot k of the device arrays maps to reference
 // slot ref_slot(k).
 constexpr int kMaxComp = 13;
+// marker of the sound-speed argument plane: a NaN payload that arithmetic
+// never produces (the hardware's NaNs are the default one), so no energy
+// compares equal to it
+constexpr unsigned long long kNoRoot = 0x7ff4000000000001ull;
 
 // Device-side view of one run: sizes, options and raw device pointers.
 // All cell arrays are SoA planes of `pitch` doubles (pitch >= nc, multiple
@@ -93,6 +97,9 @@ struct RunView {
   double* phiF;       // ncomp face planes
   double* FFd;        // nbmat planes: each cell's share of the nodal mass
                       // fluxes of the sweep (A1 / A2 dual methods)
+  double* sarg;       // VNR: 1 cell plane, the energy e from which the sound
+                      // speed in c was formed as sqrt(gamma0 (gamma0 - 1) e),
+                      // or kNoRoot where c came otherwise
   const double* geo0; // 5 cell planes, the Lagrangian geometry of the cell
                       // at rest (volume, centroid x / y, widths x / y)
   double* o3g;        // order 3: ncomp cell planes, each cell's limited-free

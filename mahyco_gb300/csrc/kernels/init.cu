@@ -273,6 +273,7 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_cells_vnr(RunView v, int t, 
       g0[3 * P + c] = Gr.hx;
       g0[4 * P + c] = Gr.hy;
     }
+    v.sarg[c] = from_bits(kNoRoot);  // the initial sound speed is not a root of e
     // cell masses (computeCellMass, PhaseLagrange.cc:14-24)
     const double cmass = v.dx * v.dy * rho;
     if (v.sans_lagrange == 0) {

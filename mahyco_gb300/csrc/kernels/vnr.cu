@@ -345,6 +345,7 @@ struct LagCells {
     // every value read before the first store (the stores would otherwise
     // order the later loads behind them)
     const double rho_old = v.rho[c], divu_old = v.divu[c], c_old = v.c[c];
+    const double sarg_old = v.sarg[c];
   #pragma unroll
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
@@ -485,8 +486,13 @@ struct LagCells {
       // sound speeds, replaced by the mixture's when rho > 0 (then the
       // materials' values are not needed)
       double cc = c_old;
+      double sarg_new = from_bits(kNoRoot);
       if (pos(rho_new)) {
-        cc = sqrt(v.g0gm1 * e_new);
+        // c_old is sqrt(g0 (g0 - 1) e) of the energy in sarg: the same energy
+        // (bit for bit) gives the same root
+        cc = (ubits(e_new) == ubits(sarg_old) && !is_nan(e_new)) ? c_old
+                                                                 : sqrt(v.g0gm1 * e_new);
+        sarg_new = e_new;
       } else {
         for (int m = 0; m < nb; ++m) {
           if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
@@ -499,6 +505,7 @@ struct LagCells {
       for (int m = 0; m < nb; ++m)
         if (eos_of(v, m) == HYDRO_EOS_VOID) e_new += mf[m] * em_new[m];
       v.c[c] = cc;
+      v.sarg[c] = sarg_new;
     } else {
       // no Lagrange phase (advection cases): energy and q are carried over
       e_new = v.e[c];
@@ -1444,7 +1451,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     Ue[m] = U[(2 * nb + m) * P];
   }
   const double Uq = U[3 * nb * P];
-  const double c_in = v.c[c];
+  const double c_in = v.c[c], sarg_in = v.sarg[c];
   double spd[4] = {0., 0., 0., 0.}, cflsq = 0.;
   if (v.sans_lagrange == 0) {
     const long long n0 = (long long)i * (v.nx + 1) + j;
@@ -1547,8 +1554,12 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     const double t = mul_frac(f[m], pm[m]);
     p = (m == 0) ? plus_zero(t) : addz(p, t);
   }
+  double sarg_out = from_bits(kNoRoot);
   if (pos(rho)) {
-    cc = sqrt(v.g0gm1 * e);
+    // c_in is sqrt(g0 (g0 - 1) e') of the energy e' in sarg: the same
+    // energy (bit for bit) gives the same root
+    cc = (ubits(e) == ubits(sarg_in) && !is_nan(e)) ? c_in : sqrt(v.g0gm1 * e);
+    sarg_out = e;
   } else {
     for (int m = 0; m < nb; m++) {
       if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
@@ -1565,6 +1576,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   v.e[c] = e;
   v.p[c] = p;
   v.c[c] = cc;
+  v.sarg[c] = sarg_out;
   for (int m = 0; m < nb; m++) {
     v.fm[m * P + c] = f[m];
     v.mfm[m * P + c] = mf[m];
