@@ -87,9 +87,11 @@ size_t layout(RunView& v, char* base) {
   v.FFd = a.take<double>(nb * P);
   if (v.order == 3) {
     v.o3g = a.take<double>(nc * P);
+    v.o3c = a.take<double>(16 * P);
     v.o3y = a.take<double>(nc * FP);
   } else {
     v.o3g = v.o3y = nullptr;
+    v.o3c = nullptr;
   }
   v.DPv = a.take<double>(2 * NP);
   v.gD = a.take<double>(2 * NP);

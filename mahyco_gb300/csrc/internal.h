@@ -105,6 +105,10 @@ struct RunView {
   double* o3g;        // order 3: ncomp cell planes, each cell's limited-free
                       // gradient along the sweep (eval_grad); null otherwise
                       // and in batched launches, which work per face
+  const double* o3c;  // order 3: 16 cell planes, the width-only coefficients
+                      // of the mesh at rest, per sweep axis (x: planes 0-7,
+                      // y: 8-15): eval_grad's G0, A, B of each cell, then
+                      // eval_ystar's T0..T4 of the face below / left of it
   double* o3y;        // order 3: ncomp face planes, the interpolated value
                       // at each inner face (eval_ystar)
   double* DPv;        // 2 node planes: nodal velocity after sweep 1

@@ -555,6 +555,38 @@ __global__ void kd_init_rows_euc(RunView v) {
 
 }  // namespace
 
+// Order-3 coefficients of the mesh at rest: eval_grad's and eval_ystar's
+// coefficients depend on the cell widths along the sweep only; with the
+// widths of the cells at rest (the stored rest geometry) they are formed here
+// once, by the functions the order-3 kernels use, for both sweep axes.
+__global__ void __launch_bounds__(kBX* kBY) kd_init_o3c(RunView v) {
+  const long long j = blockIdx.x * kBX + threadIdx.x;
+  const long long i = blockIdx.y * kBY + threadIdx.y;
+  if (i >= v.ny || j >= v.nx) return;
+  const long long c = i * v.nx + j, P = v.pitch;
+  double* o = const_cast<double*>(v.o3c);
+  for (int ax = 0; ax < 2; ++ax) {
+    const double* Hr = v.geo0 + (3 + ax) * P;
+    const int q = ax == 0 ? (int)j : (int)i, n = ax == 0 ? v.nx : v.ny;
+    const long long st = ax == 0 ? 1 : v.nx;
+    double* oa = o + 8 * ax * P;
+    {
+      const long long cm = q > 0 ? c - st : c, cp = q < n - 1 ? c + st : c;
+      double G0, A, B;
+      o3_grad_coef(Hr[cm], Hr[c], Hr[cp], G0, A, B);
+      oa[c] = G0;
+      oa[P + c] = A;
+      oa[2 * P + c] = B;
+    }
+    if (q >= 1) {
+      const long long cm = c - st, cmm = q > 1 ? cm - st : cm, cpp = q < n - 1 ? c + st : c;
+      double T[5];
+      o3_ystar_coef(Hr[cmm], Hr[cm], Hr[c], Hr[cpp], T);
+      for (int t = 0; t < 5; ++t) oa[(3 + t) * P + c] = T[t];
+    }
+  }
+}
+
 // Queues the device initialisation of a run whose arena is zeroed and whose
 // control block holds the ordered encoding of +DBL_MAX in dt_min_bits.
 // Returns the number of kernels.
@@ -566,12 +598,14 @@ int launch_device_init(const RunView& v, int test_case, int init_variant, cudaSt
     kd_init_cells_euc<<<cg, blk, 0, s>>>(v, test_case, init_variant);
     const int n = (v.nx > v.ny ? v.nx : v.ny) + 1;
     kd_init_rows_euc<<<(n + 127) / 128, 128, 0, s>>>(v);
-    return 2;
+    if (v.o3c) kd_init_o3c<<<cg, blk, 0, s>>>(v);
+    return v.o3c ? 3 : 2;
   }
   kd_init_cells_vnr<<<cg, blk, 0, s>>>(v, test_case, init_variant);
   kd_init_nodes_vnr<<<ng, blk, 0, s>>>(v, test_case, init_variant);
   kd_init_finish_vnr<<<1, 1, 0, s>>>(v);
-  return 3;
+  if (v.o3c) kd_init_o3c<<<cg, blk, 0, s>>>(v);
+  return v.o3c ? 4 : 3;
 }
 
 }  // namespace hydro

@@ -841,7 +841,18 @@ struct O3Grad {
     // neighbours clamped at the ends, as the face stencil clamps them
     const long long cm = q > 0 ? c - st : c, cp = q < n - 1 ? c + st : c;
     double G0, A, B;
-    o3_grad_coef(H[cm], H[c], H[cp], G0, A, B);
+    // widths equal (bit for bit) to the rest widths: the coefficients formed
+    // from those at set-up
+    const double* Hr = v.geo0 + (dirx ? 3 : 4) * P;
+    const double* oc = v.o3c ? v.o3c + (dirx ? 0 : 8) * P : nullptr;
+    if (oc && ubits(H[cm]) == ubits(ld(Hr, cm)) && ubits(H[c]) == ubits(ld(Hr, c)) &&
+        ubits(H[cp]) == ubits(ld(Hr, cp))) {
+      G0 = ld(oc, c);
+      A = ld(oc, P + c);
+      B = ld(oc, 2 * P + c);
+    } else {
+      o3_grad_coef(H[cm], H[c], H[cp], G0, A, B);
+    }
     for (int k = 0; k < v.ncomp; ++k)
       v.o3g[k * P + c] = o3_grad(G0, A, B, o3_value(v, sweep, k, cm),
                                  o3_value(v, sweep, k, c), o3_value(v, sweep, k, cp));
@@ -864,7 +875,17 @@ struct O3Ystar {
     const long long cmm = q > 1 ? cm - st : cm;            // left(q-1)
     const long long cpp = q < n - 1 ? c + st : c;          // right(q)
     double T[5];
-    o3_ystar_coef(H[cmm], H[cm], H[c], H[cpp], T);
+    // widths equal (bit for bit) to the rest widths: the coefficients formed
+    // from those at set-up
+    const double* Hr = v.geo0 + (dirx ? 3 : 4) * P;
+    const double* oc = v.o3c ? v.o3c + (dirx ? 3 : 11) * P : nullptr;
+    if (oc && ubits(H[cmm]) == ubits(ld(Hr, cmm)) && ubits(H[cm]) == ubits(ld(Hr, cm)) &&
+        ubits(H[c]) == ubits(ld(Hr, c)) && ubits(H[cpp]) == ubits(ld(Hr, cpp))) {
+  #pragma unroll
+      for (int t = 0; t < 5; ++t) T[t] = ld(oc, t * P + c);
+    } else {
+      o3_ystar_coef(H[cmm], H[cm], H[c], H[cpp], T);
+    }
     const long long f = dirx ? (long long)i * (v.nx + 1) + j : c;
     for (int k = 0; k < v.ncomp; ++k)
       v.o3y[k * FP + f] = o3_ystar(T, o3_value(v, sweep, k, cm), o3_value(v, sweep, k, c),
@@ -1001,7 +1022,12 @@ struct SweepFaceT {
             continue;
           }
           if (!have_F) {
-            o3_face_dt(F, h, vdt);
+            // vdt through a volatile move: the divisions below cannot be
+            // formed ahead of this branch (inline, the optimizer would hoist
+            // them out of the loop and form them for every face)
+            double vdt_b;
+            asm volatile("mov.b64 %0, %1;" : "=d"(vdt_b) : "d"(vdt));
+            o3_face_dt(F, h, vdt_b);
             have_F = true;
           }
           out[k * FP] = o3_tail(F, ys, y1, ym, yp, y4);
