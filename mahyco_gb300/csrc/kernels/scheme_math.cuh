@@ -209,7 +209,13 @@ HD SharedDiv shared_div(double b) {
   SharedDiv S;
   S.b = b;
   S.ok = div_safe_exp(b);
-  S.y = S.ok ? 1.0 / b : 0.0;
+  // the reciprocal of a power of two (within these exponents) is the power
+  // of two with the negated exponent, exactly 1.0 / b
+  const unsigned long long bb = ubits(b);
+  if (S.ok && (bb & 0xfffffffffffffull) == 0)
+    S.y = from_bits((bb & 0x8000000000000000ull) | ((2046ull - ((bb >> 52) & 0x7ffull)) << 52));
+  else
+    S.y = S.ok ? 1.0 / b : 0.0;
   return S;
 }
 HD double fma_rn(double a, double b, double c) {
@@ -249,6 +255,14 @@ HD double qdiv_shared(const SharedDiv& S, double n) {
     return from_bits((nb ^ db) & 0x8000000000000000ull);
   if (db == 0x3ff0000000000000ull) return n;
   if (nb == db && dnz && dfin) return 1.0;
+  // a power-of-two denominator only shifts the exponent (normal operands
+  // and quotient)
+  const long long en = (long long)((nb >> 52) & 0x7ffull), ed = (long long)((db >> 52) & 0x7ffull);
+  const long long er = en - ed + 1023;
+  if ((db & 0xfffffffffffffull) == 0 && ed != 0 && ed != 0x7ff && en != 0 && en != 0x7ff &&
+      er >= 1 && er <= 0x7fe)
+    return from_bits(((nb ^ db) & 0x8000000000000000ull) | ((unsigned long long)er << 52) |
+                     (nb & 0xfffffffffffffull));
   return div_shared(S, n);
 }
 
@@ -811,17 +825,31 @@ HD O3Face o3_face(const double* h, double vdt) {
   return F;
 }
 // eval_grad with its coefficients
-// (zero shortcuts: a uniform row of values gives zero differences)
+// A uniform row (the three values equal bit for bit, finite) has zero
+// differences: A * (+0) + B * (+0) is the zero -0 only when A and B are both
+// negative, times G0 (finite coefficients) the zero of the xor with G0's
+// sign.  One coarse test, so that the arithmetic is branched over rather
+// than issued under a predicate.
 HD double o3_grad(double G0, double A, double B, double ym, double y0, double yp) {
-  return mulz(G0, addz(mulz(A, subz(yp, y0)), mulz(B, subz(y0, ym))));
+  const unsigned long long b0 = ubits(y0);
+  if (ubits(ym) == b0 && ubits(yp) == b0 && is_finite(y0) && is_finite(G0) && is_finite(A) &&
+      is_finite(B))
+    return from_bits(((ubits(A) & ubits(B)) ^ ubits(G0)) & ~kMag);
+  return G0 * (A * (yp - y0) + B * (y0 - ym));
 }
 // eval_ystar with its coefficients T (o3_ystar_coef) at the face between
 // ym | yp, from the gradients of the cells on its minus / plus side
+// Equal values (bit for bit, finite, ym non-zero) and zero gradients with
+// finite coefficients: every term after ym is a signed zero, and ym plus
+// zeros is ym.  One coarse test, as in o3_grad.
 HD double o3_ystar(const double* T, double ym, double yp, double grm, double grp) {
-  const double dy = subz(yp, ym);
-  const double tmp1 = mulz(T[0], dy);
-  const double tmp2 = addz(mulz(T[1], grp), mulz(T[2], grm));
-  return addz(addz(ym, mulz(T[3], dy)), mulz(T[4], addz(tmp1, tmp2)));
+  if (ubits(yp) == ubits(ym) && nz(ym) && is_finite(ym) && iszero(grm) && iszero(grp) &&
+      is_finite(T[0]) && is_finite(T[1]) && is_finite(T[2]) && is_finite(T[3]) &&
+      is_finite(T[4]))
+    return ym;
+  const double tmp1 = T[0] * (yp - ym);
+  const double tmp2 = T[1] * grp + T[2] * grm;
+  return ym + T[3] * (yp - ym) + T[4] * (tmp1 + tmp2);
 }
 // the face value from the interpolated values ys of the faces at -1, 0, +1
 // and the cell values y1 | ym | yp | y4 (ComputeFluxOrdre3's parabola and

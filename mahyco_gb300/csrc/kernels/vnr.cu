@@ -820,6 +820,30 @@ struct SweepGradT {
 // inner face) and read by SweepFace for faces whose six-cell stencil is not
 // clamped at the ends of the row / column (the two faces next to each end
 // compute everything themselves).  Same arithmetic, same values.
+// The parabola and its interval (o3_tail) and the face's time-step
+// coefficients behind calls: inline, the compiler issues them under a
+// predicate for every component, also where the face does not move.
+struct O3Dt {
+  double Q1, Q2, R1, R2;
+  bool fwd;
+};
+__device__ __noinline__ O3Dt o3_dt_call(double h2, double h3, double vdt) {
+  const double h[4] = {0., 0., h2, h3};
+  O3Face F;
+  o3_face_dt(F, h, vdt);
+  return O3Dt{F.Q1, F.Q2, F.R1, F.R2, F.fwd};
+}
+__device__ __noinline__ double o3_tail_call(O3Dt d, double ys0, double ys1, double ys2,
+                                            double y1, double ym, double yp, double y4) {
+  O3Face F;
+  F.Q1 = d.Q1;
+  F.Q2 = d.Q2;
+  F.R1 = d.R1;
+  F.R2 = d.R2;
+  F.fwd = d.fwd;
+  const double ys[3] = {ys0, ys1, ys2};
+  return o3_tail(F, ys, y1, ym, yp, y4);
+}
 DV double o3_value(const RunView& v, int sweep, int k, long long c) {
   // the component value the order-3 reconstruction works on: U / vLagrange,
   // which is what Phi holds without PenteBorne (same division)
@@ -994,7 +1018,7 @@ struct SweepFaceT {
       if (v.o3g && q >= 2 && q <= n - 2) {
         // interior face: gradients and interpolated values from O3Grad /
         // O3Ystar, only the parabola and its interval here
-        O3Face F;
+        O3Dt F;
         bool have_F = false;
         const long long fst = dirx ? 1 : v.nx;  // face stride along the axis
         // A face that does not move: its normal velocity is exactly zero, so
@@ -1022,15 +1046,10 @@ struct SweepFaceT {
             continue;
           }
           if (!have_F) {
-            // vdt through a volatile move: the divisions below cannot be
-            // formed ahead of this branch (inline, the optimizer would hoist
-            // them out of the loop and form them for every face)
-            double vdt_b;
-            asm volatile("mov.b64 %0, %1;" : "=d"(vdt_b) : "d"(vdt));
-            o3_face_dt(F, h, vdt_b);
+            F = o3_dt_call(h[2], h[3], vdt);
             have_F = true;
           }
-          out[k * FP] = o3_tail(F, ys, y1, ym, yp, y4);
+          out[k * FP] = o3_tail_call(F, ys[0], ys[1], ys[2], y1, ym, yp, y4);
         }
       } else {
         const O3Face F = o3_face(h, vdt);
@@ -1122,6 +1141,32 @@ struct SweepUpdate {
         qa[t] = (k < ncomp && has[0]) ? v.phiF[k * FP + fidx[0]] : 0.;
         qb[t] = (k < ncomp && has[1]) ? v.phiF[k * FP + fidx[1]] : 0.;
         ui[t] = (k < ncomp) ? Uin[k * P + c] : 0.;
+      }
+      // a group whose face values are all zeros: each component keeps its
+      // value (see below), decided once so that the arithmetic is branched
+      // over rather than issued under a predicate
+      bool group_still = cfin;
+  #pragma unroll
+      for (int t = 0; t < 4; ++t)
+        if (k0 + t < ncomp) group_still = group_still && iszero(qa[t]) && iszero(qb[t]) && !is_nan(ui[t]);
+      if (group_still) {
+  #pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int k = k0 + t;
+          if (k >= ncomp) break;
+          U[k] = ui[t];
+          Uout[k * P + c] = ui[t];
+          if (dual_share && k >= doff && k < doff + nb) {
+            // the signed-zero fluxes times the normals, summed: -0 only when
+            // both terms are -0
+            const double F0 = has[0] ? from_bits((ubits(coef[0]) ^ ubits(qa[t])) & ~kMag) : 0.;
+            const double F1 = has[1] ? from_bits((ubits(coef[1]) ^ ubits(qb[t])) & ~kMag) : 0.;
+            double w = from_bits(ubits(mul_pm1(F0, nrm[0])) & ubits(mul_pm1(F1, nrm[1])));
+            if (v.dual_method == 1) w = rl * w;
+            v.FFd[(k - doff) * P + c] = w;
+          }
+        }
+        continue;
       }
   #pragma unroll
       for (int t = 0; t < 4; ++t) {

@@ -63,6 +63,7 @@ int main() {
       bad += !same(addz(a, b), a + b);
       bad += !same(subz(a, b), a - b);
       bad += !same(mulz(a, b), a * b);
+      bad += !same(qdiv(a, b), a / b);
       bad += !same(mul1z(a, b), a * b);
       for (double c : {0.0, -0.0, 1.0, -3.5})
         bad += !same(mulz3(a, b, c), (a * b) * c) + !same(mulz3(c, a, b), (c * a) * b);
@@ -93,6 +94,28 @@ int main() {
         bad += !same(flux_limiter_q(id, a), ref_flux_limiter(id, a));
     }
   }
+  // qdiv by powers of two: every exponent, numerators from the value list and
+  // random patterns (quotients across the subnormal and overflow edges)
+  for (int e = -1074; e <= 1023; ++e) {
+    const double d = std::ldexp(1.0, e);
+    for (double a : v) {
+      bad += !same(qdiv(a, d), a / d) + !same(qdiv(a, -d), a / -d);
+    }
+  }
+  // order-3 gradient / interpolated value on uniform rows (the coarse
+  // shortcut) and near-uniform ones, against the plain expressions
+  for (double y : v)
+    for (double a : {0.0, -0.0, 1.5, -2.25, 1e-300, 3e200}) {
+      const double G0 = a, A = -a * 0.5 + 0.25, B = a * 3.0 - 1.0;
+      bad += !same(o3_grad(G0, A, B, y, y, y), G0 * (A * (y - y) + B * (y - y)));
+      bad += !same(o3_grad(G0, -A, -B, y, y, y), G0 * (-A * (y - y) + -B * (y - y)));
+      const double T[5] = {a, -a, A, B, G0};
+      for (double g : {0.0, -0.0, 1.0})
+        for (double g2 : {0.0, -0.0}) {
+          const double t1 = T[0] * (y - y), t2 = T[1] * g2 + T[2] * g;
+          bad += !same(o3_ystar(T, y, y, g, g2), y + T[3] * (y - y) + T[4] * (t1 + t2));
+        }
+    }
   // exponent helpers: every significand pattern class near and below the
   // smallest normal exponents, both signs
   long pbad = 0, pn = 0;
@@ -125,6 +148,12 @@ int main() {
   };
   for (double a : v)
     for (double b : v) check_div(a, b);
+  // power-of-two denominators (exact reciprocal, exponent-shift quotients)
+  for (int e = -1074; e <= 1023; e += 3)
+    for (double a : v) {
+      check_div(a, std::ldexp(1.0, e));
+      check_div(a, -std::ldexp(1.0, e));
+    }
   for (int i = 0; i < 3000000; ++i) {
     unsigned long long ba = g(), bb = g();
     double a, b;
