@@ -101,6 +101,7 @@ size_t layout(RunView& v, char* base) {
   if (v.scheme == HYDRO_SCHEME_EUCCLHYD) {
     v.cqs = v.cflsq = v.s0 = v.sqs0 = nullptr;
     v.sarg = nullptr;
+    v.nsym = nullptr;
     v.geo0 = a.take<double>(5 * P);
     v.uc = a.take<double>(2 * P);
     v.uco = a.take<double>(2 * P);
@@ -117,6 +118,7 @@ size_t layout(RunView& v, char* base) {
   } else {
     v.geo0 = a.take<double>(5 * P);
     v.sarg = a.take<double>(P);
+    v.nsym = a.take<unsigned char>(NP);
     v.cqs = a.take<double>(8 * P);
     v.cflsq = a.take<double>(P);
     v.s0 = a.take<double>(P);

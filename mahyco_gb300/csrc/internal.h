@@ -97,6 +97,9 @@ struct RunView {
   double* phiF;       // ncomp face planes
   double* FFd;        // nbmat planes: each cell's share of the nodal mass
                       // fluxes of the sweep (A1 / A2 dual methods)
+  const unsigned char* nsym;  // VNR: per node, 1 where the corner normals of
+                      // its four cells cancel exactly in the force sum's
+                      // order (both components), 0 otherwise
   double* sarg;       // VNR: 1 cell plane, the energy e from which the sound
                       // speed in c was formed as sqrt(gamma0 (gamma0 - 1) e),
                       // or kNoRoot where c came otherwise

@@ -32,6 +32,7 @@ constexpr int kBX = 32, kBY = 4;  // 2D cell / node tiles
 #define DV __device__ __forceinline__
 
 DV double ld(const double* p, long long i) { return __ldg(p + i); }
+DV unsigned ld_u8(const unsigned char* p, long long i) { return __ldg(p + i); }
 
 // Per-material options read by select rather than by a dynamic index, so a
 // RunView copied into registers (batched launches) is never spilled whole to
@@ -216,7 +217,23 @@ struct LagNodes {
       const double u0x = ux, u0y = uy;
       double r0, r1;
       if (i > 0 && i < v.ny && j > 0 && j < v.nx) {
-        force(false, 0., 0., r0, r1);
+        // one pressure in the four cells around a node whose corner normals
+        // cancel exactly (nsym, set up with the derivation): the sum is +0
+        // without the products
+        bool zero = false;
+        if (ld_u8(v.nsym, p)) {
+          const unsigned long long w0 = ubits(addz(v.p[cells[0]], v.q[cells[0]]));
+          constexpr unsigned long long kMod = 1523ull << 52;  // 2^500
+          zero = (w0 & kMag) < kMod;
+          for (int t = 1; t < 4 && zero; ++t)
+            zero = ubits(addz(v.p[cells[t]], v.q[cells[t]])) == w0;
+        }
+        if (zero) {
+          r0 = 0.0;
+          r1 = 0.0;
+        } else {
+          force(false, 0., 0., r0, r1);
+        }
         ux = addz(u0x, step(r0));
         uy = addz(u0y, step(r1));
       }
@@ -680,6 +697,27 @@ struct SweepGradT {
     double ppa = 0., ppb = 0., ppd = 0., flen = 0.;
     if (pb == 1) {
       const long long n0 = (long long)i * (v.nx + 1) + j;
+      // the four node velocities along the sweep all zeros (and dt finite):
+      // each face velocity is plus_zero(half(+-0 + +-0)) = +0, so every
+      // swept length below is a zero and the cell takes the no-flux exit
+      // without forming them
+      {
+        const long long NP = v.npitch, o = dirx ? 0 : NP;
+        const unsigned long long z = ubits(v.u[o + n0]) | ubits(v.u[o + n0 + 1]) |
+                                     ubits(v.u[o + n0 + v.nx + 1]) | ubits(v.u[o + n0 + v.nx + 2]);
+        if ((z & kMag) == 0 && is_finite(C.dt_n)) {
+          for (int k = 0; k < ncomp; ++k) {
+            v.dPAr[k * P + c] = 0.0;
+            v.dPAv[k * P + c] = 0.0;
+          }
+          if (cfd) {
+            const double fl = dirx ? half(ld(v.flv, i) + ld(v.flv, i)) : half(ld(v.flh, j) + ld(v.flh, j));
+            const double zf = 0.0 * fl;
+            for (int m = 0; m < nb; ++m) v.DPF[m * P + c] = zf;
+          }
+          return;
+        }
+      }
       double Fa, Fb, fa_v, fb_v;
       if (dirx) {
         fa_v = fnv_vertical(v, n0, n0 + v.nx + 1);          // left face
