@@ -839,14 +839,21 @@ HD double o3_grad(double G0, double A, double B, double ym, double y0, double yp
 }
 // eval_ystar with its coefficients T (o3_ystar_coef) at the face between
 // ym | yp, from the gradients of the cells on its minus / plus side
-// Equal values (bit for bit, finite, ym non-zero) and zero gradients with
-// finite coefficients: every term after ym is a signed zero, and ym plus
-// zeros is ym.  One coarse test, as in o3_grad.
+// Equal values (bit for bit, finite) and zero gradients with finite
+// coefficients: every term after ym is a signed zero, so the value is ym
+// when ym is not zero; for a zero ym it is the zero the sign rules give
+// (x + y of two zeros is -0 only when both are -0, a zero product has the
+// xor of the signs).  One coarse test, as in o3_grad.
 HD double o3_ystar(const double* T, double ym, double yp, double grm, double grp) {
-  if (ubits(yp) == ubits(ym) && nz(ym) && is_finite(ym) && iszero(grm) && iszero(grp) &&
+  if (ubits(yp) == ubits(ym) && is_finite(ym) && iszero(grm) && iszero(grp) &&
       is_finite(T[0]) && is_finite(T[1]) && is_finite(T[2]) && is_finite(T[3]) &&
-      is_finite(T[4]))
-    return ym;
+      is_finite(T[4])) {
+    if (nz(ym)) return ym;
+    // yp - ym = +0; T3 (+0) has T3's sign; T0 (+0) + (T1 grp + T2 grm)
+    const unsigned long long t2 = (ubits(T[1]) ^ ubits(grp)) & (ubits(T[2]) ^ ubits(grm));
+    const unsigned long long z2 = ubits(T[4]) ^ (ubits(T[0]) & t2);
+    return from_bits(ubits(ym) & ubits(T[3]) & z2 & ~kMag);
+  }
   const double tmp1 = T[0] * (yp - ym);
   const double tmp2 = T[1] * grp + T[2] * grm;
   return ym + T[3] * (yp - ym) + T[4] * (tmp1 + tmp2);

@@ -110,6 +110,12 @@ int main() {
       bad += !same(o3_grad(G0, A, B, y, y, y), G0 * (A * (y - y) + B * (y - y)));
       bad += !same(o3_grad(G0, -A, -B, y, y, y), G0 * (-A * (y - y) + -B * (y - y)));
       const double T[5] = {a, -a, A, B, G0};
+      const double T2[5] = {-a, a, -A, -B, -G0};
+      for (double g : {0.0, -0.0})
+        for (double g2 : {0.0, -0.0}) {
+          const double t1 = T2[0] * (y - y), t2 = T2[1] * g2 + T2[2] * g;
+          bad += !same(o3_ystar(T2, y, y, g, g2), y + T2[3] * (y - y) + T2[4] * (t1 + t2));
+        }
       for (double g : {0.0, -0.0, 1.0})
         for (double g2 : {0.0, -0.0}) {
           const double t1 = T[0] * (y - y), t2 = T[1] * g2 + T[2] * g;
