@@ -336,16 +336,6 @@ HD double mul1z(double a, double b) {
   if (ua == kOne && (ub & kMag) <= kInfBits) return b;
   return mulz(a, b);
 }
-// (a * b) * c, the zero of c decided before a * b is formed: with |a| and
-// |b| below 2^511, a * b is finite (or a zero), and its product with a zero
-// c is the zero of the xor of the three signs.
-HD double mulz3(double a, double b, double c) {
-  constexpr unsigned long long kSafe = 0x5fe0000000000000ull;  // 2^511
-  const unsigned long long ua = ubits(a), ub = ubits(b), uc = ubits(c);
-  if ((uc & kMag) == 0 && (ua & kMag) < kSafe && (ub & kMag) < kSafe)
-    return from_bits((ua ^ ub ^ uc) & ~kMag);
-  return mulz(a * b, c);
-}
 
 // Lagrangian geometry of a VNR cell from its four node positions
 // (updateCellPos, computeSubVol, vnr_remap/PhaseLagrange.cc:210-296; the

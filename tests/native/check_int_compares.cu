@@ -65,8 +65,6 @@ int main() {
       bad += !same(mulz(a, b), a * b);
       bad += !same(qdiv(a, b), a / b);
       bad += !same(mul1z(a, b), a * b);
-      for (double c : {0.0, -0.0, 1.0, -3.5})
-        bad += !same(mulz3(a, b, c), (a * b) * c) + !same(mulz3(c, a, b), (c * a) * b);
     }
   for (double a : v) {
     bad += pos(a) != (a > 0.0);
