@@ -1779,7 +1779,8 @@ __global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) {
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdate{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
+// ten resident blocks: where nodes are quiet the kernel waits on memory
+__global__ void __launch_bounds__(kBX* kBY, 10) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY, 10) k_final(RunView v) { plain_items(v, Final{}); }
 
 // Batched launches: a persistent grid walks the tile table; every thread of
