@@ -133,7 +133,14 @@ DV void cell_eos(const RunView& v, int m, long long c, double& pm, double& cm) {
   const int eos = eosm(v, m);
   if (eos == HYDRO_EOS_PERFECT_GAS) {
     pm = (g - 1.0) * rm * em;
-    cm = pos(rm) ? sqrt(g * pm / rm) : 1.e-20;
+    if (pos(rm)) {
+      // the volatile barrier keeps the division and the root inside this
+      // branch (a select would form them for absent materials too)
+      asm volatile("");
+      cm = sqrt(g * pm / rm);
+    } else {
+      cm = 1.e-20;
+    }
   } else if (eos == HYDRO_EOS_VOID) {
     pm = 0.;
     cm = 1.e-20;
