@@ -1538,6 +1538,10 @@ struct DualUpdate {
 // computeEOS + computePressionMoyenne (PhaseLagrange.cc:392-485), and the
 // next cycle's dt candidate (VnrRemap.cc:14-50) and max pressure
 // (PhaseLagrange.cc:55-61).
+// material loops unrolled to the three possible materials (the arrays they
+// index stay in registers instead of local memory); iterations m >= nbmat do
+// nothing
+#define MAT_LOOP(m, first) _Pragma("unroll") for (int m = (first); m < 3; ++m) if (m < nb)
 __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
                                            int j, unsigned long long& dtb,
                                            unsigned long long& pb) {
@@ -1573,65 +1577,65 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   // every sum below starts from 0.0 in the reference: its first addition
   // 0.0 + x is plus_zero(x), on the integer pipe (materials 0 .. nb-1, nb >= 1)
   double volt = plus_zero(vn[0]), masset = plus_zero(Um[0]);
-  for (int m = 1; m < nb; m++) {
+  MAT_LOOP(m, 1) {
     volt = addz(volt, vn[m]);
     masset = addz(masset, Um[m]);
   }
   const double rv = qdiv(vol, volt);
   vn[0] = mul1z(vn[0], rv);
   double vnorm = plus_zero(vn[0]);
-  for (int m = 1; m < nb; m++) {
+  MAT_LOOP(m, 1) {
     vn[m] = mul1z(vn[m], rv);
     vnorm = addz(vnorm, vn[m]);
   }
   double f[3], mf[3], sf = 0.;
-  for (int m = 0; m < nb; m++) {
+  MAT_LOOP(m, 0) {
     f[m] = qdiv(vn[m], vnorm);
     if (dlt(f[m], thr)) f[m] = 0.;
     sf = (m == 0) ? plus_zero(f[m]) : addz(sf, f[m]);
   }
-  for (int m = 0; m < nb; m++) f[m] = qdiv(f[m], sf);
+  MAT_LOOP(m, 0) f[m] = qdiv(f[m], sf);
   int matcell = 0, imatpure = -1;
-  for (int m = 0; m < nb; m++)
+  MAT_LOOP(m, 0)
     if (pos(f[m])) {
       matcell++;
       imatpure = m;
     }
   v.mixte[c] = (matcell > 1) ? 1 : 0;
   v.pure[c] = (matcell > 1) ? -1 : imatpure;
-  for (int m = 0; m < nb; m++) mf[m] = qdiv(Um[m], masset);
+  MAT_LOOP(m, 0) mf[m] = qdiv(Um[m], masset);
   double fmt = 0.;
-  for (int m = 0; m < nb; m++) {
+  MAT_LOOP(m, 0) {
     if (dlt(f[m], thr)) mf[m] = 0.;
     fmt = (m == 0) ? plus_zero(mf[m]) : addz(fmt, mf[m]);
   }
-  for (int m = 0; m < nb; m++) mf[m] = qdiv(mf[m], fmt);
+  MAT_LOOP(m, 0) mf[m] = qdiv(mf[m], fmt);
   double dm[3] = {0., 0., 0.}, dens = 0.;
-  for (int m = 0; m < nb; m++) {
+  MAT_LOOP(m, 0) {
     if (dgt(f[m], thr)) dm[m] = qdiv(Um[m], vn[m]);
     const double fd = mul_frac(f[m], dm[m]);
     dens = (m == 0) ? plus_zero(fd) : addz(dens, fd);
   }
   double em[3] = {0., 0., 0.};
-  for (int m = 0; m < nb; m++)
+  MAT_LOOP(m, 0)
     if (dgt(f[m], thr) && nz(Um[m]))
       em[m] = qdiv(Ue[m], Um[m]);
   const double rho = dens;
   double e = 0.;
   const double cmass = v.euler_volume * rho;
   v.cell_mass[c] = cmass;
-  for (int m = 0; m < nb; m++) v.cmassm[m * P + c] = mul_frac(mf[m], cmass);
+  MAT_LOOP(m, 0) v.cmassm[m * P + c] = mul_frac(mf[m], cmass);
   v.q[c] = qdiv(Uq, vol);
-  for (int m = 0; m < nb; m++) {
+  MAT_LOOP(m, 0) {
     const double t = mul_frac(mf[m], em[m]);
     e = (m == 0) ? plus_zero(t) : addz(e, t);
   }
   double rhom[3], emo[3];
-  for (int m = 0; m < nb; m++) {
+  MAT_LOOP(m, 0) {
     rhom[m] = dm[m];
     emo[m] = em[m];
   }
-  for (int m = 0; m < nb; m++) {
+  MAT_LOOP(m, 0) {
     if (neg(em[m]) || neg(dm[m])) {
       rhom[m] = 0.;
       emo[m] = 0.;
@@ -1648,7 +1652,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   // mean-pressure step when rho <= 0 (otherwise the mixture's replaces the
   // maximum), and nothing else reads it: it is formed only then.
   double pm[3], cm[3];
-  for (int m = 0; m < nb; m++) {
+  MAT_LOOP(m, 0) {
     if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
       pm[m] = mulz(mulz(gm1_of(v, m), rhom[m]), emo[m]);
     } else {
@@ -1659,7 +1663,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     }
   }
   double p = 0., cc = c_in;
-  for (int m = 0; m < nb; m++) {
+  MAT_LOOP(m, 0) {
     const double t = mul_frac(f[m], pm[m]);
     p = (m == 0) ? plus_zero(t) : addz(p, t);
   }
@@ -1670,7 +1674,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     cc = (ubits(e) == ubits(sarg_in) && !is_nan(e)) ? c_in : sqrt(v.g0gm1 * e);
     sarg_out = e;
   } else {
-    for (int m = 0; m < nb; m++) {
+    MAT_LOOP(m, 0) {
       if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
         const double g = gamma_of(v, m);
         cm[m] = sqrt(g * (g - 1.0) * emo[m]);
@@ -1679,14 +1683,14 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
       cc = smax(cc, cm[m]);
     }
   }
-  for (int m = 0; m < nb; m++)
+  MAT_LOOP(m, 0)
     if (eos_of(v, m) == HYDRO_EOS_VOID) e += mf[m] * emo[m];
   v.rho[c] = rho;
   v.e[c] = e;
   v.p[c] = p;
   v.c[c] = cc;
   v.sarg[c] = sarg_out;
-  for (int m = 0; m < nb; m++) {
+  MAT_LOOP(m, 0) {
     v.fm[m * P + c] = f[m];
     v.mfm[m * P + c] = mf[m];
     v.rhom[m * P + c] = rhom[m];
@@ -1781,7 +1785,7 @@ __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep)
 __global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
 // ten resident blocks: where nodes are quiet the kernel waits on memory
 __global__ void __launch_bounds__(kBX* kBY, 10) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY, 10) k_final(RunView v) { plain_items(v, Final{}); }
+__global__ void __launch_bounds__(kBX* kBY, 8) k_final(RunView v) { plain_items(v, Final{}); }
 
 // Batched launches: a persistent grid walks the tile table; every thread of
 // a block works on the same tile (the final phase's block reduction relies
