@@ -120,6 +120,61 @@ int main() {
           bad += !same(o3_ystar(T, y, y, g, g2), y + T[3] * (y - y) + T[4] * (t1 + t2));
         }
     }
+  // the node force cancellation the node kernel relies on: with one pressure
+  // w in the four cells, ((w c0 + w c1) + w c2) + w c3 (first addition from
+  // 0.0) is +0 when c1 = -c0, c3 = -c2, or c1 = c0, c2 = c3 = -c0, for
+  // |w|, |c| < 2^500
+  {
+    long fbad = 0;
+    auto rnd = [&](int emax) {
+      unsigned long long b = g();
+      const unsigned long long e = 1023 - emax + g() % (2 * emax);
+      b = (b & 0x800fffffffffffffull) | (e << 52);
+      double x;
+      memcpy(&x, &b, 8);
+      return x;
+    };
+    auto fsum = [](double w, double c0, double c1, double c2, double c3) {
+      double r = plus_zero(w * c0);
+      r = r + w * c1;
+      r = r + w * c2;
+      return r + w * c3;
+    };
+    for (int i = 0; i < 2000000; ++i) {
+      const double w = (i % 97 == 0) ? 0.0 : rnd(499), a = rnd(499), b = rnd(499);
+      const double z = (i % 89 == 0) ? -0.0 : a;
+      fbad += !same(fsum(w, z, -z, b, -b), 0.0) || (std::signbit(fsum(w, z, -z, b, -b)));
+      fbad += !same(fsum(w, z, z, -z, -z), 0.0) || (std::signbit(fsum(w, z, z, -z, -z)));
+    }
+    if (fbad) printf("force cancellation: %ld mismatches\n", fbad);
+    bad += fbad;
+  }
+  // the order-3 face value of a face that does not move (vdt = +-0, finite
+  // positive upwind width, inputs finite below 2^1000) is finite, so its
+  // product with the zero sweep coefficient is a zero
+  {
+    long obad = 0;
+    auto rnd = [&](int emax) {
+      unsigned long long b = g();
+      const unsigned long long e = 1023 - emax + g() % (2 * emax);
+      b = (b & 0x800fffffffffffffull) | (e << 52);
+      double x;
+      memcpy(&x, &b, 8);
+      return (g() % 13 == 0) ? 0.0 : x;
+    };
+    for (int i = 0; i < 1000000; ++i) {
+      const double h[4] = {0., 0., std::fabs(rnd(900)) + 1e-300, (i % 5 == 0) ? 0.0 : std::fabs(rnd(900))};
+      const double vdt = (i & 1) ? 0.0 : -0.0;
+      if (!(h[2] > 0.0)) continue;
+      O3Face F;
+      o3_face_dt(F, h, vdt);
+      const double ys[3] = {rnd(999), rnd(999), rnd(999)};
+      const double y = o3_tail(F, ys, rnd(999), rnd(999), rnd(999), rnd(999));
+      obad += !std::isfinite(y);
+    }
+    if (obad) printf("still order-3 faces: %ld non-finite values\n", obad);
+    bad += obad;
+  }
   // exponent helpers: every significand pattern class near and below the
   // smallest normal exponents, both signs
   long pbad = 0, pn = 0;
