@@ -175,6 +175,39 @@ int main() {
     if (obad) printf("still order-3 faces: %ld non-finite values\n", obad);
     bad += obad;
   }
+  // the dual update of a quiet node (no mass flux, velocities +0 at the node
+  // and its neighbours, zero slopes at the node, positions below 2^1022, dt
+  // finite): the new conserved value is the old one with a zero made +0
+  {
+    long qbad = 0;
+    auto rnd = [&](int emax) {
+      unsigned long long b = g();
+      const unsigned long long e = 1023 - emax + g() % (2 * emax);
+      b = (b & 0x800fffffffffffffull) | (e << 52);
+      double x;
+      memcpy(&x, &b, 8);
+      return x;
+    };
+    for (int i = 0; i < 1000000; ++i) {
+      const double Fm = 0.0, Fp = 0.0, dp = 0.0, dn = 0.0;
+      const double gp = (i & 1) ? 0.0 : -0.0, dt = rnd(300);
+      const double xp = rnd(1020), xn = (i % 7 == 0) ? 0.0 : rnd(1020);
+      const int order2 = i % 3;
+      double Ui = (i % 5 == 0) ? ((i & 2) ? -0.0 : 0.0) : rnd(1000);
+      if (i % 11 == 0) Ui = INFINITY;
+      // the kernel's expressions (minus side and plus side, one component)
+      const double u = half(dn + dp);
+      const double dxm = xp - xn, sdm = pos(u) ? dxm : -dxm;
+      const double um = dp + mul_012(order2, half(gp) * (sdm - dt * u));
+      const double dxp = xn - xp, sdp = pos(u) ? dxp : -dxp;
+      const double up = dp + mul_012(order2, half(gp) * (sdp - dt * u));
+      const double Un = Ui + Fm * um - Fp * up;
+      const double want = iszero(Ui) ? 0.0 : Ui;
+      qbad += !same(Un, want) || (iszero(Un) && std::signbit(Un));
+    }
+    if (qbad) printf("quiet dual update: %ld mismatches\n", qbad);
+    bad += qbad;
+  }
   // exponent helpers: every significand pattern class near and below the
   // smallest normal exponents, both signs
   long pbad = 0, pn = 0;
