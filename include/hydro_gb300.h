@@ -230,11 +230,18 @@ int hydro_serve_stop(hydro_ctx* ctx, int drain);
  * Vnr::computeDeltaT with the remap on).  For callers that may not call
  * cudaMalloc/cudaFree because their own pool owns the device memory.  Inputs:
  * node velocity planes d_u, d_v ((nx+1)*(ny+1) each), cell sound speed d_c
- * (nx*ny), the current dt_n; output: one double at d_dt_out.  Its scratch is
- * a fixed 32 KiB device array inside the library, so at most 1,048,576 cells
- * are accepted (larger meshes return an error).  The first call on a device
- * looks up that array's address and should come before any stream capture.
- * Calls that overlap on the GPU share the scratch and race. */
+ * (nx*ny), the current dt_n; output: one double at d_dt_out.  It models the
+ * remapped run only: cfl 0.05 and the sub-volumes of the Euler mesh, whose
+ * nodes sit at (dx*j, dy*i) from the origin as the reference's mesh
+ * generator places them (a run without remap uses cfl 0.1 and its moved
+ * sub-volumes, which this function does not take).  Its scratch is a fixed
+ * 32 KiB device array inside the library, so at most 1,048,576 cells are
+ * accepted (larger meshes return an error).  The first call on a device
+ * looks up that array's address in the device's primary context (the one
+ * the CUDA runtime uses) and keeps it for the life of the process: call it
+ * with that context current, make the first call before any stream capture,
+ * and do not call it after resetting the device.  Calls that overlap on the
+ * GPU share the scratch and race. */
 int hydro_vnr_dt_noalloc(int nx, int ny, double dx, double dy,
                          const double* d_u, const double* d_v,
                          const double* d_c, double dt_n, double* d_dt_out,

@@ -12,9 +12,11 @@
 // restore).
 //
 // File: header (magic, format version, sizeof(hydro_spec), arena bytes, a
-// hash of the layout, a hash of the arena contents), the hydro_spec, then
-// the arena bytes.  The layout hash ties a file to the library's layout; the
-// content hash rejects truncated or corrupted files.
+// hash of the layout, a hash of the arena contents, a hash of the options),
+// the hydro_spec, then the arena bytes.  The layout hash ties a file to the
+// library's layout; the content and option hashes reject truncated or
+// corrupted files (a damaged option would otherwise resume the run with
+// another scheme, limiter or end time).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -28,7 +30,7 @@ namespace hydro {
 namespace {
 
 constexpr char kMagic[8] = {'H', 'G', 'B', '3', 'C', 'K', 'P', 'T'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;
 constexpr size_t kChunk = 64u << 20;
 
 struct Header {
@@ -38,7 +40,8 @@ struct Header {
   uint64_t arena_bytes;
   uint64_t layout_hash;
   uint64_t data_hash;
-  uint64_t reserved[3];
+  uint64_t spec_hash;
+  uint64_t reserved[2];
 };
 
 // FNV-1a over 64-bit words (tail bytes zero-padded)
@@ -118,6 +121,11 @@ int hydro_run_checkpoint(hydro_run* r, const char* path) {
   h.spec_bytes = sizeof(hydro_spec);
   h.arena_bytes = r->arena_bytes;
   h.layout_hash = layout_hash(r->v, r->arena_bytes);
+  {
+    Hash hs;
+    hs.add(&r->spec, sizeof(hydro_spec));
+    h.spec_hash = hs.h;
+  }
   if (std::fwrite(&h, sizeof h, 1, out.f) != 1 ||
       std::fwrite(&r->spec, sizeof(hydro_spec), 1, out.f) != 1)
     return fail(-41, "checkpoint: write failed");
@@ -166,6 +174,11 @@ int hydro_run_restore(hydro_ctx* ctx, const char* path, hydro_run** out) {
     return fail(-43, "restore: checkpoint format version not supported");
   if (std::fread(&spec, sizeof spec, 1, in.f) != 1)
     return fail(-43, "restore: truncated checkpoint");
+  {
+    Hash hs;
+    hs.add(&spec, sizeof spec);
+    if (hs.h != h.spec_hash) return fail(-46, "restore: checkpoint options corrupted");
+  }
   PreparedRun pr;
   if (int rc = prepare_run(spec, pr)) return rc;
   if (pr.bytes != h.arena_bytes || layout_hash(pr.v, pr.bytes) != h.layout_hash)

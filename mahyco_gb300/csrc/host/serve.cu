@@ -156,9 +156,25 @@ void worker_main(ServeState* S) {
     }
     if (!runs.empty() && !rc) rc = batch_done_flags(ctx, &done);
     if (rc) {
+      // runs released by the user are no longer listed anywhere: free them
+      // here; requests still being prepared or on the device will never
+      // finish, so their pollers get a failed completion (the resident runs
+      // stay listed and are freed with the server)
+      for (auto* r : frees) hydro_run_destroy(r);
       std::lock_guard<std::mutex> lk(S->mu);
       S->error = rc;
       S->error_msg = hydro_last_error();
+      const auto now = Clock::now();
+      auto post_failed = [&](const ServeRequest& q) {
+        hydro_serve_done d{};
+        d.req_id = q.id;
+        d.status = -1;
+        d.latency_s = secs(q.submitted, now);
+        S->done.push_back(d);
+        S->st.failed += 1;
+      };
+      for (const auto& q : preparing) post_failed(q);
+      for (const auto& q : S->resident) post_failed(q);
       S->stop = true;
       S->cv.notify_all();
       break;

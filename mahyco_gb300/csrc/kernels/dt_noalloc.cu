@@ -120,7 +120,9 @@ k_dt_final(int nblocks, double dt_n, const unsigned long long* scratch,
 }
 
 // Device address of g_dt_scratch, looked up once per device (with that
-// device current) on the first call made on it.
+// device current) on the first call made on it, in the device's primary
+// context (the CUDA runtime's); it stays valid until that context is reset,
+// after which the function must not be called (documented in the header).
 constexpr int kMaxDevices = 64;
 unsigned long long* g_scratch_ptr[kMaxDevices];
 std::mutex g_scratch_mu;

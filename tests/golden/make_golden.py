@@ -14,14 +14,16 @@ Cases: every deck of the reference's test suite that uses the remap
 and the three-material triple point with one exponent per material.
 Eucclhyd fixtures hold cell_velocity instead of the VNR-only fields.
 
-Needs the reference sources (default /root/reference); run from the repo root:
-  make -f oracle/Makefile.ref REF=/root/reference -j8
-  python tests/golden/make_golden.py [--ref /root/reference]
+Needs the reference sources, given by --ref or MAHYCO_REFERENCE; run from
+the repo root:
+  make -f oracle/Makefile.ref REF=<reference tree> -j8
+  python tests/golden/make_golden.py --ref <reference tree>
 """
 from __future__ import annotations
 
 import argparse
 import json
+import os
 import subprocess
 import sys
 import tempfile
@@ -73,9 +75,12 @@ def save(case: str, spec: M.HydroSpec, meta: dict, fields: dict) -> None:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("MAHYCO_REFERENCE"),
+                    help="reference source tree (or set MAHYCO_REFERENCE)")
     ap.add_argument("--only", default="")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("the reference source tree is needed: --ref or MAHYCO_REFERENCE")
     tests = Path(a.ref) / "tests"
     if not DUMP.exists():
         sys.exit("oracle/_ref/mahyco_dump missing: make -f oracle/Makefile.ref")

@@ -12,13 +12,14 @@ remap on, VNR or Eucclhyd), stores in tests/golden/vtk_digests.json:
 The drop-in driver's test runs each deck and compares its output directory
 with these digests, file by file.  Needs the reference sources; run from the
 repo root:
-  python tests/golden/make_vtk_digests.py [--ref /root/reference]
+  python tests/golden/make_vtk_digests.py --ref <reference tree>
 """
 from __future__ import annotations
 
 import argparse
 import hashlib
 import json
+import os
 import sys
 import tempfile
 from pathlib import Path
@@ -37,8 +38,11 @@ def digest(path: Path):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("MAHYCO_REFERENCE"),
+                    help="reference source tree (or set MAHYCO_REFERENCE)")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("the reference source tree is needed: --ref or MAHYCO_REFERENCE")
     cases = {}
     with tempfile.TemporaryDirectory() as tmp:
         for d in sorted((Path(a.ref) / "tests").iterdir()):

@@ -136,6 +136,15 @@ def test_damaged_or_foreign_files_are_rejected(M, tmp_path):
     bad.write_bytes(bytes(flip))
     with pytest.raises(RuntimeError, match="corrupted"):
         M.Run.restore(bad)
+    # one option byte changed (the limiter id, after the 64-byte header):
+    # the options carry their own hash, so the run does not resume with
+    # another scheme
+    opt = tmp_path / "option.ckpt"
+    flip = bytearray(data)
+    flip[64 + M.HydroSpec.limiter.offset] ^= 0x01
+    opt.write_bytes(bytes(flip))
+    with pytest.raises(RuntimeError, match="options corrupted"):
+        M.Run.restore(opt)
     short = tmp_path / "short.ckpt"
     short.write_bytes(bytes(data[: len(data) - 4096]))
     with pytest.raises(RuntimeError, match="truncated"):
