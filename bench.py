@@ -6,21 +6,25 @@ Default workload (the single large instance): bi-material Sod along Y on a
 Lagrange scheme, order-2 remap, Superbee limiter with PenteBorne (pure),
 A1 dual mass flux, 200 cycles, FP64.  One "step" is one full cycle
 (Lagrange + two directional remap sweeps + dual remap + remap final) over
-all 4,194,304 cells.  The state (~1.9 GB) is far larger than L2, so every
+all 4,194,304 cells.  The state (~3.9 GB) is far larger than L2, so every
 cycle streams it from HBM.
 
-  value      device time (CUDA events on the run's stream) of K cycles,
-             state resident in HBM
-  e2e        the same work through the C ABI with host buffers: run
-             creation from the options (the initial state is built on the
-             device; the host uploads the 128-byte control block), K cycles,
-             fetch of the final fields (device->host)
+  value      device time (CUDA events on the run's stream) of the last K
+             cycles of the configured 200-cycle window (cycles 200-K+1..200,
+             the first 200-K advanced untimed), state resident in HBM
+  e2e        the whole 200-cycle job through the C ABI with host buffers:
+             run creation from the options (the initial state is built on
+             the device; the host uploads the 128-byte control block), 200
+             cycles, fetch of the final fields (device->host)
+  developed  the same deck advanced untimed until most nodes move (the
+             flow developed), then K cycles timed: the regime where the
+             exact at-rest shortcuts are taken almost nowhere
   roofline   the dominant kernel's algorithmic bytes / measured launch time
              against the measured HBM copy bandwidth, plus its FP64 rate
-             against the measured FP64 FMA throughput (the kernels are FP64
-             instruction bound on GB300)
+             against the measured FP64 FMA throughput
   cpu_baseline  the C restatement of the reference (oracle/port, OpenMP on
              all host cores) on a bounded sample of the same workload
+  summary    the headline figures of every record, last on the line
 
   --impl reference   times the reference's CPU algorithm (the C restatement;
                      the reference's own build cannot exist on this host) on
@@ -37,6 +41,8 @@ import sys
 import tempfile
 import time
 from pathlib import Path
+
+import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 CTRL_BYTES = 128  # the run's control block, the one host->device copy of creation
@@ -62,15 +68,28 @@ def workload_spec(M, n: int = 2048, cycles: int = 200):
     return s
 
 
-WORKLOAD = {
-    "workload": "bi-material Sod Y, 2048x2048 cells, 50/50 mixed interface row, "
-                "VNR + order-2 remap, superBee + PenteBorne pure, A1 dual flux, "
-                "200 cycles",
-    "mesh": [2048, 2048], "nbmat": 2, "cycles": 200, "scheme": "VNR",
-    "projection_order": 2, "limiter": "superBee", "pente_borne": "pure",
-    "dual_mass_flux": "A1", "state_bytes": None,
-    "l2": "state (~1.9 GB) >> L2 (129 MB): every cycle streams it from HBM",
-}
+CYCLES = 200  # the configured window of the large single instance
+
+
+def timed_window(K: int, W: int) -> tuple[int, int]:
+    """(untimed cycles before the timed ones, run length): the K timed
+    cycles end the configured window; with K + W above it the window is
+    extended so that W warm-up cycles still come first."""
+    adv = CYCLES - K if K + W <= CYCLES else W
+    return adv, max(CYCLES, adv + K)
+
+
+def workload_config(K: int, W: int, n: int = 2048) -> dict:
+    adv, length = timed_window(K, W)
+    return {
+        "workload": f"bi-material Sod Y, {n}x{n} cells, 50/50 mixed interface row, "
+                    "VNR + order-2 remap, superBee + PenteBorne pure, A1 dual flux, "
+                    f"{CYCLES} cycles",
+        "mesh": [n, n], "nbmat": 2, "cycles": CYCLES, "scheme": "VNR",
+        "projection_order": 2, "limiter": "superBee", "pente_borne": "pure",
+        "dual_mass_flux": "A1",
+        "l2": "state (~3.9 GB) >> L2 (129 MB): every cycle streams it from HBM",
+    }
 
 
 # Algorithmic (compulsory) bytes per unit of each kernel: every input plane
@@ -192,20 +211,23 @@ def cpu_baseline(spec_fn, budget_s: float = 25.0) -> dict:
 
 
 def run_reference(args) -> None:
+    """The reference's CPU algorithm (the C restatement, bit for bit the
+    reference) on all host cores: W warm-up cycles, then K timed cycles of
+    the same deck (time-capped)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     import mahyco_gb300 as M
     from oracle import port
-    spec = workload_spec(M, 2048, 200)
+    K, W = args.steps, args.warmup
+    spec = workload_spec(M, args.mesh, CYCLES + K + W)
     cores = port.num_threads()
     run = port.PortRun(spec)
-    for _ in range(min(args.warmup, 1)):
-        run.step(1)
+    run.step(W)
     budget = 150.0
     n, t0 = 0, time.perf_counter()
-    while n < args.steps:
+    while n < K:
         run.step(1)
         n += 1
         if time.perf_counter() - t0 > budget:
@@ -214,14 +236,17 @@ def run_reference(args) -> None:
     val = spec.nx * spec.ny * n / el
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT,
-        "n_gpus": args.gpus, "steps": n, "warmup": min(args.warmup, 1),
+        "n_gpus": args.gpus, "steps": n, "warmup": W,
         "ms_per_step": 1e3 * el / n, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(WORKLOAD, form="cpu"),
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic initial state)",
+        "config": workload_config(K, W, args.mesh), "form": "cpu",
+        "window": [W + 1, W + n],
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{n} cycles of the 2048x2048 workload on "
-                                   f"{cores} OpenMP threads (time-capped at "
-                                   f"{budget:.0f} s)"},
+                         "sample": f"cycles {W + 1}..{W + n} of the {args.mesh}x{args.mesh} "
+                                   f"workload after {W} warm-up cycles, on {cores} OpenMP "
+                                   f"threads (time-capped at {budget:.0f} s; the port does "
+                                   "the reference's full arithmetic on every cell, its "
+                                   "per-cycle cost barely depends on the cycle)"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -241,47 +266,50 @@ BATCH_WORKLOAD = {
 def bench_batch(M, ctx, args, local: int) -> dict:
     """The mixed batch: plain path (each run through its own CUDA graph, one
     after another) against the batched path (one persistent launch per phase
-    for all 512 runs), on the same runs at nearby cycles."""
+    for all 512 runs), each on its own copy of the same runs, timed over the
+    same cycles (WARM untimed cycles first: the batch autotunes in 11 of
+    them)."""
     from mahyco_gb300.workloads import batch_mix
+    import torch
     mix = batch_mix(args.batch_n)
     cells = sum(i.cells for i in mix)
+    K, WARM = args.batch_steps, 14
+    # plain path: every run's own 8-cycle graph, runs enqueued back to back,
+    # events on the context's stream around the K cycles of all of them
+    plain_runs = [M.Run(i.spec(M), ctx) for i in mix]
+    for r in plain_runs:
+        r.enqueue(WARM)
+    for r in plain_runs:
+        r.sync()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    launches0 = sum(r.kernel_launches for r in plain_runs)
+    with Clocks(local) as clk_plain:
+        ev0.record(ext)
+        for r in plain_runs:
+            r.enqueue(K)
+        ev1.record(ext)
+        ev1.synchronize()
+    plain_ms = ev0.elapsed_time(ev1)
+    plain_launches = sum(r.kernel_launches for r in plain_runs) - launches0
+    plain_val = cells * K / (plain_ms * 1e-3)
+    plain_density = [r.fetch("density") for r in plain_runs[:8]]
+    for r in plain_runs:
+        r.close()
+    # batched path on a fresh copy of the same runs
     t0 = time.perf_counter()
     runs = [M.Run(i.spec(M), ctx) for i in mix]
     create_s = time.perf_counter() - t0
     state = sum(r.device_bytes for r in runs)
-    import ctypes
-    lib = M.lib()
-    stream = ctypes.c_void_p(ctx.stream)
-    # plain path: warm (graph capture) then K2 cycles of every run, enqueued
-    # back to back, timed with events on the context's stream
-    K2 = 8
-    for r in runs:
-        r.enqueue(1)
-    for r in runs:
-        r.sync()
-    import torch
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
-    launches0 = sum(r.kernel_launches for r in runs)
-    with Clocks(local) as clk_plain:
-        ev0.record(ext)
-        for r in runs:
-            r.enqueue(K2)
-        ev1.record(ext)
-        ev1.synchronize()
-    plain_ms = ev0.elapsed_time(ev1)
-    plain_launches = sum(r.kernel_launches for r in runs) - launches0
-    plain_val = cells * K2 / (plain_ms * 1e-3)
-    # batched path: tuning cycles + warm-up, then K timed cycles
     batch = M.Batch(runs, ctx)
-    batch.step(11 + 3)  # 11 tuning cycles (10 candidates + warm-up), 3 warm
-    K = args.batch_steps
+    batch.step(WARM)  # 11 tuning cycles (10 candidates + warm-up), 3 warm
     b0 = batch.kernel_launches
     with Clocks(local) as clk_batch:
         bms = batch.timed(K)
     b_launches = batch.kernel_launches - b0
     bval = cells * K / (bms * 1e-3)
+    same = all(np.array_equal(a, r.fetch("density")) for a, r in zip(plain_density, runs))
     prof = batch.profile(2)
     kinds = {k: v for k, v in prof.items() if v[1] > 0}
     t1 = time.perf_counter()
@@ -295,13 +323,16 @@ def bench_batch(M, ctx, args, local: int) -> dict:
         r.close()
     return {
         "value": bval, "unit": UNIT, "ms_per_step": bms / K, "steps": K,
+        "timed_cycles": [WARM + 1, WARM + K],
         "gpu_launches": b_launches,
-        "plain_mix": {"value": plain_val, "unit": UNIT, "ms_per_step": plain_ms / K2,
-                      "steps": K2, "gpu_launches": plain_launches,
+        "plain_mix": {"value": plain_val, "unit": UNIT, "ms_per_step": plain_ms / K,
+                      "steps": K, "timed_cycles": [WARM + 1, WARM + K],
+                      "gpu_launches": plain_launches,
                       "clocks": clk_plain.summary(),
                       "how": "each run's own CUDA graph (8 cycles), runs enqueued "
-                             "one after another, events around the sweep"},
+                             "one after another, events around the K cycles of all"},
         "speedup_vs_plain_mix": bval / plain_val,
+        "plain_equals_batched_at_window_end": same,
         "cells": cells, "state_bytes": state, "create_s": create_s,
         "finish_s": finish_s, "fetch_bytes": fetched, "runs_left": left,
         "cycles_done": [min(cyc), max(cyc)], "runs_in_error": errs,
@@ -323,9 +354,13 @@ SERVE_WORKLOAD = {
 
 def bench_serve(M, args, local: int) -> dict:
     """Continuous batching under Poisson arrivals: per rate, n requests are
-    submitted at their arrival times; latency is submission -> retirement;
-    throughput is the cell-updates of all requests over first arrival ->
-    last retirement."""
+    submitted at their arrival times; latency is submission -> retirement,
+    split into the admission wait (submission -> admission against the HBM
+    budget and the slots) and the time resident on the device (placement ->
+    retirement); throughput is the cell-updates of all requests over first
+    arrival -> last retirement.  The first rate is below the server's
+    capacity (about 7 requests/s of this mix), so its latencies are service
+    times rather than queue drain."""
     from mahyco_gb300.workloads import request_stream
     rates = [float(x) for x in args.serve_rates.split(",") if x]
     out = []
@@ -354,15 +389,20 @@ def bench_serve(M, args, local: int) -> dict:
         st = srv.stats()
         srv.stop(drain=False)
         ctx.close()
-        ls = sorted(d.latency_s for d in lat)
         work = sum(d.cells * d.cycles for d in lat)
 
-        def pct(q):
-            return ls[min(len(ls) - 1, int(q * len(ls)))] if ls else None
+        def pct(vals, q):
+            vals = sorted(vals)
+            return vals[min(len(vals) - 1, int(q * len(vals)))] if vals else None
         out.append({
             "rate_req_s": lam, "requests": len(reqs), "completed": len(lat),
             "failed": sum(1 for d in lat if d.status < 0),
-            "p50_latency_s": pct(0.50), "p99_latency_s": pct(0.99),
+            "p50_latency_s": pct([d.latency_s for d in lat], 0.50),
+            "p99_latency_s": pct([d.latency_s for d in lat], 0.99),
+            "p50_wait_s": pct([d.wait_s for d in lat], 0.50),
+            "p99_wait_s": pct([d.wait_s for d in lat], 0.99),
+            "p50_resident_s": pct([d.resident_s for d in lat], 0.50),
+            "p99_resident_s": pct([d.resident_s for d in lat], 0.99),
             "cell_updates": work, "wall_s": wall,
             "value": work / wall if wall > 0 else None, "unit": UNIT,
             "peak_resident": st["peak_resident"], "peak_bytes": st["peak_bytes"],
@@ -454,6 +494,140 @@ def bench_euc(M, ctx, args, local: int) -> dict:
     return out
 
 
+def roofline_of(M, kinds: dict, spec, regime: str, local: int) -> dict:
+    """Roofline of the dominant kernel of a per-kernel profile: algorithmic
+    bytes per launch over its mean CUDA-event launch time against the
+    measured HBM bandwidth; DRAM traffic and FP64 flops per unit from the
+    committed ncu counters of the same regime ("kernels": the benchmark's
+    early cycles, "developed": the developed flow), scaled by the units."""
+    n = spec.nx
+    cells = spec.nx * spec.ny
+    dom = max(kinds, key=lambda k: kinds[k][0])
+    dom_ms, dom_n = kinds[dom]
+    per_launch_ms = dom_ms / dom_n
+    node_kernel = dom in ("k_lag_nodes", "k_dual_grad", "k_dual_update")
+    units = (n + 1) * (spec.ny + 1) if node_kernel else cells
+    alg = algorithmic_bytes(dom, spec.nbmat, bool(spec.pb)) * units
+    achieved = alg / (per_launch_ms * 1e-3) / 1e9
+    peaks = load_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    prof_file = ROOT / "profiles" / "kernel_counters_bisod_vnr.json"
+    traffic, fp64 = None, None
+    fp64_peak = M.fp64_peak_tflops(local)
+    if prof_file.exists():
+        pj = json.loads(prof_file.read_text())
+        table = pj.get(regime, {})
+        table = table.get("kernels", table)
+        kp = table.get(dom) or table.get(dom + "_pb", {})
+        if "dram_bytes_per_unit" in kp:
+            traffic = kp["dram_bytes_per_unit"] * units
+        if "fp64_flops_per_unit" in kp:
+            fl = kp["fp64_flops_per_unit"] * units
+            ach = fl / (per_launch_ms * 1e-3) / 1e12
+            fp64 = {"achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                    "frac": ach / fp64_peak, "flops_per_launch": fl,
+                    "pipe_busy_pct_ncu": kp.get("fp64_pipe_pct"),
+                    "peak_source": "measured DFMA chain (hydro_fp64_peak)"}
+    if fp64 is None:
+        fp64 = {"achieved": None, "peak": fp64_peak, "unit": "TFLOP/s",
+                "peak_source": "measured DFMA chain (hydro_fp64_peak)"}
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+            "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+            "algorithmic_bytes_per_launch": alg, "launch_ms": per_launch_ms,
+            "counters": f"profiles/kernel_counters_bisod_vnr.json [{regime}]",
+            "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"
+            if not peaks.get("fallback") else "of fallback",
+            "fp64": fp64}
+
+
+def path_traffic(kinds: dict, spec, regime: str, ms_per_cycle: float) -> dict | None:
+    """Whole-cycle DRAM bytes per cell from the committed counters of every
+    kernel of the cycle (launches per cycle from the profile), against the
+    compulsory state traffic 2 S(m) per cell-update (80 + 56 m bytes of
+    persistent VNR state, read and written once)."""
+    prof_file = ROOT / "profiles" / "kernel_counters_bisod_vnr.json"
+    if not prof_file.exists():
+        return None
+    pj = json.loads(prof_file.read_text())
+    table = pj.get(regime, {})
+    table = table.get("kernels", table)
+    cells = spec.nx * spec.ny
+    nodes = (spec.nx + 1) * (spec.ny + 1)
+    cycles = max(v[1] for k, v in kinds.items() if k in ("k_lag_cells", "k_final"))
+    per_cell = 0.0
+    for k, (ms, cnt) in kinds.items():
+        kp = table.get(k) or table.get(k + "_pb")
+        if not kp:
+            continue
+        units = nodes if k in ("k_lag_nodes", "k_dual_grad", "k_dual_update") else cells
+        per_cell += kp["dram_bytes_per_unit"] * units * (cnt / cycles) / cells
+    compulsory = 2 * (80 + 56 * spec.nbmat)
+    peaks = load_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    gbs = compulsory * cells / (ms_per_cycle * 1e-3) / 1e9
+    return {"dram_bytes_per_cell": round(per_cell, 1), "compulsory_bytes_per_cell": compulsory,
+            "over_compulsory": round(per_cell / compulsory, 2),
+            "compulsory_gbs": gbs, "path_hbm_frac": gbs / hbm,
+            "counters": f"profiles/kernel_counters_bisod_vnr.json [{regime}]"}
+
+
+def port_developed(M, spec_fn, budget_s: float = 12.0) -> dict:
+    """The C restatement in a developed flow: the same deck on 256^2,
+    advanced until the waves cross most of the mesh, then timed per cycle
+    (its work per cell grows once the cells leave the at-rest extrema)."""
+    from oracle import port
+    spec = spec_fn(256, 2400)
+    run = port.PortRun(spec)
+    run.step(1800)
+    u = run.fetch("node_velocity").reshape(-1, 2)
+    moving = float(np.mean((u[:, 0] != 0) | (u[:, 1] != 0)))
+    n, t0 = 0, time.perf_counter()
+    while n < 40 and time.perf_counter() - t0 < budget_s:
+        run.step(1)
+        n += 1
+    el = time.perf_counter() - t0
+    run.close()
+    cores = port.num_threads()
+    return {"value": spec.nx * spec.ny * n / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} cycles (1801..{1800 + n}) of the same deck on 256x256, "
+                      f"{100 * moving:.0f}% of the nodes moving, {cores} OpenMP threads, "
+                      f"{el:.1f} s"}
+
+
+def bench_developed(M, ctx, args, local: int, K: int) -> dict:
+    """The benchmark deck advanced untimed until most nodes move, then K
+    cycles timed (CUDA events, state resident) and 4 profiled."""
+    n = args.mesh
+    adv = args.dev_advance
+    spec = workload_spec(M, n, adv + K + 8)
+    run = M.Run(spec, ctx)
+    t0 = time.perf_counter()
+    run.step(adv)
+    adv_s = time.perf_counter() - t0
+    u = run.fetch("node_velocity").reshape(-1, 2)
+    moving = float(np.mean((u[:, 0] != 0) | (u[:, 1] != 0)))
+    l0 = run.kernel_launches
+    with Clocks(local) as clk:
+        ms = run.timed(K)
+    launches = run.kernel_launches - l0
+    prof = run.profile(4)
+    err = run.error()[0]
+    run.close()
+    kinds = {k: v for k, v in prof.items() if v[1] > 0}
+    cells = n * n
+    out = {"value": cells * K / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / K,
+           "steps": K, "timed_cycles": [adv + 1, adv + K],
+           "nodes_moving": moving, "advance_s": adv_s, "gpu_launches": launches,
+           "error_word": err, "clocks": clk.summary(),
+           "roofline": roofline_of(M, kinds, spec, "developed", local),
+           "path": path_traffic(kinds, spec, "developed", ms / K),
+           "kernel_ms": {k: [round(v[0], 4), v[1]] for k, v in kinds.items()}}
+    if not args.no_cpu:
+        out["cpu_baseline"] = port_developed(M, lambda m, c: workload_spec(M, m, c))
+        out["vs_cpu"] = out["value"] / out["cpu_baseline"]["value"]
+    return out
+
+
 def run_ours(args) -> None:
     rank, world, local = dist_env()
     if world > 1:
@@ -463,13 +637,13 @@ def run_ours(args) -> None:
     ctx = M.Context(local)
     W, K = args.warmup, args.steps
     n = args.mesh
-    spec = workload_spec(M, n, K + 16)
     cells = n * n
-    # warm-up: graph instantiation, first launches, clocks up
-    w = M.Run(workload_spec(M, n, W + 1), ctx)
-    w.timed(W)
-    w.close()
-    run = M.Run(spec, ctx)
+    # the K timed cycles end the configured window; the cycles before them
+    # (at least W) run untimed and warm the graph, caches and clocks; 8 more
+    # cycles after the window are profiled kernel by kernel
+    adv, length = timed_window(K, W)
+    run = M.Run(workload_spec(M, n, length + 8), ctx)
+    run.step(adv)
     state_bytes = run.device_bytes
     launches0 = run.kernel_launches
     barrier_max(0.0, world)
@@ -479,79 +653,74 @@ def run_ours(args) -> None:
     launches = run.kernel_launches - launches0
     ms = barrier_max(ms, world)
     value = cells * K * world / (ms * 1e-3)
-    # per-kernel profile over 8 further cycles of the same run
     prof = run.profile(8)
     run.close()
-    # dominant kernel and its roofline
     kinds = {k: v for k, v in prof.items() if v[1] > 0}
-    dom = max(kinds, key=lambda k: kinds[k][0])
-    dom_ms, dom_n = kinds[dom]
-    per_launch_ms = dom_ms / dom_n
-    node_kernel = dom in ("k_lag_nodes", "k_dual_grad", "k_dual_update")
-    units = (n + 1) * (n + 1) if node_kernel else cells
-    alg = algorithmic_bytes(dom, spec.nbmat, bool(spec.pb)) * units
-    achieved = alg / (per_launch_ms * 1e-3) / 1e9
-    peaks = load_peaks()
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
-    prof_file = ROOT / "profiles" / "kernel_counters_bisod_vnr.json"
-    traffic = None
-    fp64 = None
-    fp64_peak = M.fp64_peak_tflops(local)
-    if prof_file.exists():
-        pj = json.loads(prof_file.read_text())
-        kp = pj.get("kernels", {}).get(dom, {})
-        if "dram_bytes_per_unit" in kp:
-            traffic = kp["dram_bytes_per_unit"] * units
-        if "fp64_flops_per_unit" in kp:
-            fl = kp["fp64_flops_per_unit"] * units
-            ach = fl / (per_launch_ms * 1e-3) / 1e12
-            fp64 = {"achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
-                    "frac": ach / fp64_peak, "flops_per_launch": fl,
-                    "peak_source": "measured DFMA chain (hydro_fp64_peak)"}
-    if fp64 is None:
-        fp64 = {"achieved": None, "peak": fp64_peak, "unit": "TFLOP/s",
-                "peak_source": "measured DFMA chain (hydro_fp64_peak)"}
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
-                "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-                "algorithmic_bytes_per_launch": alg,
-                "launch_ms": per_launch_ms,
-                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"
-                if not peaks.get("fallback") else "of fallback",
-                "fp64": fp64}
-    # end to end through the C ABI with host buffers
+    spec = workload_spec(M, n, CYCLES)
+    roofline = roofline_of(M, kinds, spec, "kernels", local)
+    path = path_traffic(kinds, spec, "kernels", ms / K)
+    # end to end through the C ABI with host buffers: the whole configured
+    # job (creation with the device-built initial state, 200 cycles, fetch)
     t0 = time.perf_counter()
-    e = M.Run(workload_spec(M, n, K), ctx)
-    e.step(K)
+    e = M.Run(workload_spec(M, n, CYCLES), ctx)
+    e.step(CYCLES)
     outs = [e.fetch(f) for f in ("density", "pressure", "energy", "fracvol_env",
                                  "node_velocity")]
     e2e_s = time.perf_counter() - t0
     h2d = CTRL_BYTES  # the control block; the initial state is built on the device
     d2h = sum(o.nbytes for o in outs)
     e.close()
-    e2e = {"value": cells * K / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
-           "includes": "run creation (device-built initial state), K cycles, fetch of 5 fields"}
+    e2e = {"value": cells * CYCLES / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": h2d / CYCLES, "d2h_bytes_per_step": d2h / CYCLES,
+           "includes": f"run creation (device-built initial state), all {CYCLES} "
+                       "cycles, fetch of 5 fields"}
     if rank != 0:
         return
-    cpu = None if args.no_cpu else cpu_baseline(lambda: workload_spec(M, n, 200))
-    cfg = dict(WORKLOAD, form="plain", state_bytes=state_bytes)
-    if n != 2048:
-        cfg["mesh"] = [n, n]
-        cfg["workload"] = cfg["workload"].replace("2048x2048", f"{n}x{n}")
+    cpu = None if args.no_cpu else cpu_baseline(lambda: workload_spec(M, n, CYCLES))
+    developed = None if args.no_dev else bench_developed(M, ctx, args, local, K)
     batched = None if args.no_batch else bench_batch(M, ctx, args, local)
-    served = None if args.no_serve else bench_serve(M, args, local)
     eucclhyd = None if args.no_euc else bench_euc(M, ctx, args, local)
+    served = None if args.no_serve else bench_serve(M, args, local)
+    summary = {
+        "plain": {"value": value, "e2e": e2e["value"], "window": [adv + 1, adv + K],
+                  "dominant": roofline["kernel"], "hbm_frac": round(roofline["frac"], 3),
+                  "path_hbm_frac": path and round(path["path_hbm_frac"], 3),
+                  "vs_cpu": cpu and value / cpu["value"]},
+    }
+    if developed:
+        summary["developed"] = {"value": developed["value"],
+                                "nodes_moving": round(developed["nodes_moving"], 3),
+                                "dominant": developed["roofline"]["kernel"],
+                                "hbm_frac": round(developed["roofline"]["frac"], 3),
+                                "vs_cpu": developed.get("vs_cpu")}
+    if eucclhyd:
+        summary["eucclhyd"] = {"value": eucclhyd["value"]}
+    if served:
+        summary["served"] = [[o["rate_req_s"], o["completed"], round((o["value"] or 0) / 1e6, 1),
+                              round(o["p50_latency_s"] or 0, 3), round(o["p99_latency_s"] or 0, 3)]
+                             for o in served["rates"]]
+        summary["served_columns"] = ["rate_req_s", "completed", "M_cell_updates_s",
+                                     "p50_s", "p99_s"]
+    if batched:
+        summary["batched"] = {"value": batched["value"],
+                              "plain_mix": batched["plain_mix"]["value"],
+                              "speedup_vs_plain_mix": batched["speedup_vs_plain_mix"],
+                              "same_cycles": batched["timed_cycles"]}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (analytic initial state)", "config": cfg,
-        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-        "gpu_launches": launches,
+        "data": "synthetic (analytic initial state)",
+        "config": workload_config(K, W, n), "form": "plain",
+        "window": [adv + 1, adv + K], "state_bytes": state_bytes,
+        "e2e": e2e, "roofline": roofline, "path": path, "cpu_baseline": cpu,
+        "clocks": clocks, "gpu_launches": launches,
         "kernel_ms": {k: [round(v[0], 4), v[1]] for k, v in kinds.items()},
-        "batched": batched,
         "served": served,
         "eucclhyd": eucclhyd,
+        "developed": developed,
+        "batched": batched,
+        "summary": summary,
     }
     print(json.dumps(line))
 
@@ -570,9 +739,11 @@ def main() -> None:
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-euc", action="store_true")
     ap.add_argument("--euc-steps", type=int, default=60)
-    ap.add_argument("--serve-rates", default="50,200,1000,2000")
-    ap.add_argument("--serve-n", type=int, default=24)
-    ap.add_argument("--serve-timeout", type=float, default=120.0)
+    ap.add_argument("--serve-rates", default="4,50,100,200,500,1000,2000")
+    ap.add_argument("--serve-n", type=int, default=200)
+    ap.add_argument("--serve-timeout", type=float, default=240.0)
+    ap.add_argument("--dev-advance", type=int, default=4500)
+    ap.add_argument("--no-dev", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -199,6 +199,8 @@ typedef struct hydro_serve_done {
   double latency_s;  /* submission to retirement                          */
   long cycles;       /* cycles the run did                                */
   long cells;
+  double wait_s;     /* submission to admission (HBM budget, slots)       */
+  double resident_s; /* placement on the device to retirement             */
 } hydro_serve_done;
 typedef struct hydro_serve_stats {
   long submitted, admitted, completed, failed;

@@ -66,7 +66,8 @@ class HydroSpec(C.Structure):
 class ServeDone(C.Structure):
     """struct hydro_serve_done"""
     _fields_ = [("req_id", C.c_long), ("status", C.c_int), ("latency_s", C.c_double),
-                ("cycles", C.c_long), ("cells", C.c_long)]
+                ("cycles", C.c_long), ("cells", C.c_long), ("wait_s", C.c_double),
+                ("resident_s", C.c_double)]
 
 
 class ServeStats(C.Structure):

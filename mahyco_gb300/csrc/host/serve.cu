@@ -44,7 +44,7 @@ struct ServeRequest {
   long id = 0;
   hydro_spec spec{};
   int keep = 0;
-  Clock::time_point submitted;
+  Clock::time_point submitted, admitted, placed;
   // placed run (while resident / kept)
   hydro_run* run = nullptr;
   long long cycles_enqueued = 0;
@@ -137,6 +137,7 @@ void worker_main(ServeState* S) {
         in_use += need;
         reserved += need;
         q.bytes = need;
+        q.admitted = Clock::now();
         preparing.push_back(q);
         S->waiting.pop_front();
         const hydro_spec sp = preparing.back().spec;
@@ -196,6 +197,8 @@ void worker_main(ServeState* S) {
           d.req_id = r.id;
           d.status = (int)code;
           d.latency_s = secs(r.submitted, now);
+          d.wait_s = secs(r.submitted, r.admitted);
+          d.resident_s = secs(r.placed, now);
           d.cycles = cyc;
           d.cells = (long)r.spec.nx * r.spec.ny;
           S->done.push_back(d);
@@ -243,12 +246,14 @@ void worker_main(ServeState* S) {
         d.req_id = q.id;
         d.status = -1;
         d.latency_s = secs(q.submitted, Clock::now());
+        d.wait_s = secs(q.submitted, q.admitted);
         S->done.push_back(d);
         S->st.failed += 1;
         S->cv.notify_all();
         continue;
       }
       q.run = run;
+      q.placed = Clock::now();
       q.cycles_enqueued = 0;
       if (!S->any) {
         S->any = true;

@@ -6,6 +6,8 @@ reproduce the reference's final state bit for bit, through the C ABI.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 import pytest
 
@@ -73,19 +75,80 @@ def test_gpu_matches_port_larger(n, cycles, pb, lim, dual, M, ctx, port_lib):
         assert_bitwise(f, get_field(g, f, spec.nbmat), get_field(c, f, spec.nbmat))
 
 
-def test_gpu_full_size_conservation(M, ctx):
-    """2048^2 bi-material Sod (the large single-instance workload), 20 cycles:
-    total mass is conserved to 1e-12 relative; fields stay finite."""
-    spec = _bisod(M, 2048, 20, True, "superBee", 0)
+def vnr_totals(run, spec):
+    """Total mass, x / y momentum and total energy of a VNR state, from the
+    fetched fields (exactly rounded sums): cell masses rho * V on the Euler
+    mesh, nodal momentum m_p u_p, internal energy rho e V plus the nodal
+    kinetic energy m_p |u_p|^2 / 2."""
+    V = spec.dx * spec.dy
+    rho, e = run.fetch("density"), run.fetch("energy")
+    mp = run.fetch("node_mass")
+    u = run.fetch("node_velocity").reshape(-1, 2)
+    return {"mass": math.fsum(rho * V),
+            "momentum_x": math.fsum(mp * u[:, 0]),
+            "momentum_y": math.fsum(mp * u[:, 1]),
+            "energy": math.fsum(rho * e * V) + math.fsum(0.5 * mp * (u[:, 0] ** 2 + u[:, 1] ** 2)),
+            # momentum scale: the whole mass moving at the largest sound speed
+            "momentum_scale": math.fsum(mp) * float(np.max(run.fetch("sound_speed")))}
+
+
+def test_gpu_config2_full_size_matches_port(M, ctx, port_lib):
+    """The large single-instance workload exactly as benchmarked (bi-material
+    Sod Y on 2048^2 with the 50/50 mixed row, VNR, order 2, superBee +
+    PenteBorne pure, A1 dual flux, 200 cycles): every cell and node field
+    bit-identical to the C restatement, and the conservation totals.
+
+    Mass is conserved to 1e-13 relative.  Momentum is not a conserved
+    quantity of this problem (the walls push on the fluid: the initial
+    pressure jump between the bottom and top walls accelerates it upwards);
+    x-momentum, zero by the mirror symmetry in x, stays within 1e-13 of the
+    momentum scale (total mass times the largest sound speed).  Total energy
+    is not conserved exactly by the reference's staggered scheme (its remap
+    of the nodal kinetic energy is not conservative: the C restatement, bit
+    for bit the reference, drifts by 5e-8 over 200 cycles on 256^2 and by
+    2e-5 over 1400), so the energy totals are checked equal to the port's."""
+    import bench
+    spec = bench.workload_spec(M, 2048, 200)
     run = M.Run(spec, ctx)
-    m0 = run.fetch("cell_mass").sum()
+    t0 = vnr_totals(run, spec)
     run.simulate()
-    m1 = run.fetch("cell_mass").sum()
-    assert abs(m1 - m0) <= 1e-12 * m0
+    assert run.time()[2] == 200
+    ref = port_lib.PortRun(spec)
+    ref.simulate()
+    assert run.time() == ref.time()
+    for f in CELL_FIELDS + NODE_FIELDS + ["node_mass"]:
+        assert_bitwise(f, get_field(run, f, spec.nbmat), get_field(ref, f, spec.nbmat))
+    t1, tr = vnr_totals(run, spec), vnr_totals(ref, spec)
+    assert t1 == tr
+    assert abs(t1["mass"] - t0["mass"]) <= 1e-13 * t0["mass"]
+    assert abs(t1["momentum_x"]) <= 1e-13 * t1["momentum_scale"]
     rho = run.fetch("density")
     assert np.all(np.isfinite(rho)) and rho.min() > 0
     assert run.error()[0] & ~M.ERR_NEGATIVE == 0
-    assert run.time()[2] == 20
+
+
+def test_gpu_developed_flow_matches_port(M, ctx, port_lib):
+    """The benchmark deck on 256^2 run well past the initial dt ramp, until
+    the waves cross most of the mesh (most nodes moving, so the exact
+    at-rest shortcuts are taken almost nowhere): every field bit-identical to
+    the C restatement, mass conserved to 1e-13 relative."""
+    import bench
+    spec = bench.workload_spec(M, 256, 1400)
+    run = M.Run(spec, ctx)
+    t0 = vnr_totals(run, spec)
+    run.simulate()
+    ref = port_lib.PortRun(spec)
+    ref.simulate()
+    assert run.time() == ref.time()
+    u = run.fetch("node_velocity").reshape(-1, 2)
+    moving = float(np.mean((u[:, 0] != 0) | (u[:, 1] != 0)))
+    assert moving > 0.6, moving
+    for f in CELL_FIELDS + NODE_FIELDS + ["node_mass"]:
+        assert_bitwise(f, get_field(run, f, spec.nbmat), get_field(ref, f, spec.nbmat))
+    t1 = vnr_totals(run, spec)
+    assert t1 == vnr_totals(ref, spec)
+    assert abs(t1["mass"] - t0["mass"]) <= 1e-13 * t0["mass"]
+    assert abs(t1["momentum_x"]) <= 1e-13 * t1["momentum_scale"]
 
 
 def test_gpu_error_word_instead_of_abort(M, ctx):
@@ -166,3 +229,39 @@ def test_gpu_triple_point_full_size_matches_port(M, ctx, port_lib):
     assert abs(m1 - m0) <= 1e-11 * m0
     assert run.error()[0] & ~M.ERR_NEGATIVE == 0
     assert run.time()[2] == 8
+
+
+def euc_totals(run, spec):
+    """Total mass, momentum and energy of a Eucclhyd state from the fetched
+    cell-centred fields (exactly rounded sums over rho V, rho u V and
+    rho (e + |u|^2 / 2) V on the Euler mesh)."""
+    V = spec.dx * spec.dy
+    rho, e = run.fetch("density"), run.fetch("energy")
+    u = run.fetch("cell_velocity").reshape(-1, 2)
+    m = rho * V
+    return {"mass": math.fsum(m), "momentum_x": math.fsum(m * u[:, 0]),
+            "momentum_y": math.fsum(m * u[:, 1]),
+            "energy": math.fsum(m * (e + 0.5 * (u[:, 0] ** 2 + u[:, 1] ** 2)))}
+
+
+def test_gpu_triple_point_conservation(M, ctx, port_lib):
+    """224x96 triple point, 300 cycles (order-3 projection, superBee): the
+    mass, momentum and energy totals equal the C restatement's (bit for bit
+    the reference).  The reference conserves none of them to 1e-13 here:
+    the walls push on the fluid (momentum), the kinetic energy is remapped
+    without the conservative correction, and the C restatement itself moves
+    the mass rho V by -2.6e-5 and the total energy by -6.3e-4 over these
+    cycles; so the check is equality with the port, with bounds just above
+    those drifts."""
+    spec = triple_point(M, 224, 96, 300)
+    spec.pb = spec.pb_mixte = 0
+    run = M.Run(spec, ctx)
+    t0 = euc_totals(run, spec)
+    run.simulate()
+    ref = port_lib.PortRun(spec)
+    ref.simulate()
+    assert run.time() == ref.time()
+    t1 = euc_totals(run, spec)
+    assert t1 == euc_totals(ref, spec)
+    assert abs(t1["mass"] - t0["mass"]) <= 1e-4 * t0["mass"]
+    assert abs(t1["energy"] - t0["energy"]) <= 1e-3 * t0["energy"]
