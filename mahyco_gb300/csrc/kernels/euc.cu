@@ -51,7 +51,6 @@ DV double dot2(double a0, double a1, double b0, double b1) {
   r += a1 * b1;
   return r;
 }
-DV double cross2(double a0, double a1, double b0, double b1) { return a0 * b1 - a1 * b0; }
 // dot2 is exactly +0 when one vector is two zeros and the other finite
 // (plus_zero of a signed zero, plus a signed zero)
 DV bool dot2_zero(double a0, double a1, double b0, double b1) {

@@ -8,9 +8,11 @@
 //                                                        ConditionsLimites.cc)
 //   k_lag_cells    sub-volumes, densities, div u, pseudo-viscosity, energy,
 //                  EOS, mean pressure, then the cell part of PrepareRemap
-//   sweep x2:  k_sweep_grad (limited slopes / plateau-slope integrals),
-//              k_sweep_face (face values), k_sweep_update (conservative
-//              update), k_dual_grad + k_dual_update (nodal momentum remap)
+//   sweep x2:  k_sweep_grad (face gradients, limited slopes / plateau-slope
+//              integrals), k_sweep_update_f (face values of orders 1-2 and
+//              the conservative update; order 3: k_o3_grad, k_o3_ystar,
+//              k_sweep_face3, k_sweep_update), k_dual_grad + k_dual_update
+//              (nodal momentum remap)
 //   k_final        remapVariables + EOS + mean pressure + next dt / pmax
 //   k_end          loop condition and time swap
 //
@@ -581,49 +583,6 @@ DV double fnv_horizontal(const RunView& v, long long na, long long nb) {
 }
 
 // ----------------------------------------------------------- remap sweep
-// Face gradients of one sweep (Remap::computeGradPhiFace{1,2},
-// remap/PhaseRemap1.cc:22-55, PhaseRemap2.cc:21-55): one thread per inner
-// face perpendicular to the sweep, (Phi(front) - Phi(back)) / deltaxLagrange,
-// stored in the face-value planes (k_sweep_face overwrites them later).
-struct FaceGrad {
-  int sweep;
-  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
-    // no slopes at order 1, nor at order 3 without PenteBorne (batched
-    // launches; the plain cycle does not launch these then)
-    if (v.order <= 1 || (v.order == 3 && v.pb == 0)) return;
-    const Ctrl& C = *v.ctrl;
-    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
-    const long long P = v.pitch, FP = v.fpitch;
-    long long back, front, fidx;
-    int ax;
-    if (dirx) {
-      if (i >= v.ny || j < 1 || j >= v.nx) return;
-      front = (long long)i * v.nx + j;
-      back = front - 1;
-      fidx = (long long)i * (v.nx + 1) + j;
-      ax = 0;
-    } else {
-      if (j >= v.nx || i < 1 || i >= v.ny) return;
-      back = (long long)i * v.nx + j;
-      front = back - v.nx;
-      fidx = (long long)i * v.nx + j;
-      ax = 1;
-    }
-    const double dx = plus_zero(v.XcL[ax * P + front] - v.XcL[ax * P + back]);
-    // with PenteBorne only the integrated components' slopes are read (see
-    // SweepGrad): the most any cell integrates
-    int nk = v.ncomp;
-    if (v.pb == 1) {
-      const int nb = v.nbmat;
-      const bool euc = (v.scheme == HYDRO_SCHEME_EUCCLHYD);
-      nk = (v.pb_complet == 1) ? (euc ? v.ncomp : 3 * nb) : (v.pb_mixte == 1 ? 2 * nb : nb);
-      if (!euc && v.dual_method == 2 && nk < 2 * nb) nk = 2 * nb;
-    }
-    for (int k = 0; k < nk; ++k)
-      v.phiF[k * FP + fidx] = qdiv(v.Phi[k * P + front] - v.Phi[k * P + back], dx);
-  }
-};
-
 // Limited slopes and plateau-slope integrals of one sweep
 // (Remap::computeGradPhiFace{1,2} + computeGradPhi{1,2},
 // remap/PhaseRemap1.cc:22-323, remap/PhaseRemap2.cc:21-323).
@@ -677,16 +636,13 @@ struct SweepGradT {
       has_gp = (i > 0);          // bottom face
       has_gm = (i < v.ny - 1);   // top face
     }
-    // face gradients written by k_face_grad
-    const long long FP = v.fpitch;
-    long long fp_idx, fm_idx;
-    if (dirx) {
-      fm_idx = (long long)i * (v.nx + 1) + j;  // left face
-      fp_idx = fm_idx + 1;                     // right face
-    } else {
-      fp_idx = (long long)i * v.nx + j;        // bottom face
-      fm_idx = fp_idx + v.nx;                  // top face
-    }
+    // The two face gradients are formed here (Remap::computeGradPhiFace
+    // {1,2}, remap/PhaseRemap1.cc:22-55): (Phi(front) - Phi(back)) /
+    // (XcL(front) - XcL(back)) with the reference's back / front cells, the
+    // "plus" face between c (back) and cf (front), the "minus" face between
+    // cb (back) and c (front).  Each inner face's gradient is formed by both
+    // of its cells with the same operations, so no face plane is written and
+    // read back; a cell that takes the no-flux exit below forms neither.
     // Eucclhyd carries momentum (and kinetic energy) after the material
     // components instead of the VNR pseudo-viscosity, and has no dual remap
     const bool euc = (v.scheme == HYDRO_SCHEME_EUCCLHYD);
@@ -768,12 +724,18 @@ struct SweepGradT {
     const int nint = (v.pb_complet == 1) ? (euc ? ncomp : 3 * nb) : (vp ? 2 * nb : nb);
     const int nuse = (cfd && nint < 2 * nb) ? 2 * nb : nint;
     const int ngrad = (pb == 1) ? nuse : ncomp;
+    const int ax = dirx ? 0 : 1;
+    const double xc = v.XcL[ax * P + c];
+    // one denominator per face, shared by its components (the IEEE quotient
+    // bit for bit, see shared_div)
+    const SharedDiv Sp = shared_div(has_gp ? plus_zero(v.XcL[ax * P + cf] - xc) : 1.0);
+    const SharedDiv Sm = shared_div(has_gm ? plus_zero(xc - v.XcL[ax * P + cb]) : 1.0);
     double grad[kMaxComp];
     for (int k = 0; k < ngrad; ++k) {
       const double y0 = v.Phi[k * P + c];
       const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
-      const double gp = has_gp ? v.phiF[k * FP + fp_idx] : 0.;
-      const double gm = has_gm ? v.phiF[k * FP + fm_idx] : 0.;
+      const double gp = has_gp ? qdiv_shared(Sp, v.Phi[k * P + cf] - y0) : 0.;
+      const double gm = has_gm ? qdiv_shared(Sm, y0 - v.Phi[k * P + cb]) : 0.;
       grad[k] = limit_grad1(lim, gp, gm, yp, ym, h0, hp, hm);
       if (pb == 0) v.gP[k * P + c] = grad[k];
     }
@@ -966,6 +928,8 @@ template <int ORDERS>
 struct SweepFaceT {
   int sweep;
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    // batched launches: the update of an order-1/2 run forms its face values
+    if (ORDERS == 3 && v.order <= 2) return;
     const Ctrl& C = *v.ctrl;
     const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
     const long long P = v.pitch, FP = v.fpitch;
@@ -1045,7 +1009,6 @@ struct SweepFaceT {
         cs[4] = (long long)ibb * v.nx + j; cs[5] = (long long)ibbb * v.nx + j;
       }
       const double* H = dirx ? v.Hx : v.Hy;
-      const double* Uin = (sweep == 1) ? v.UL : v.U1;
       const double vdt = fnv * C.dt_n;
       double h[6];
       for (int t = 0; t < 6; ++t) h[t] = H[cs[t]];
@@ -1101,9 +1064,45 @@ struct SweepFaceT {
   }
 };
 
+// Face values of orders 1-2 (Remap::computeUpwindFaceQuantitiesForProjection
+// {1,2}, remap/PhaseRemap1.cc:331-452) formed where they are used: the
+// update of each cell forms the values of its two faces with SweepFace's
+// operations (so each inner face's value is formed by both of its cells,
+// bit for bit the same), instead of reading them from a face plane.
+struct LowFace {
+  long long av, ar;  // PenteBorne: value = dPAv(av) - dPAr(ar)
+  long long cu;      // otherwise: the upwind cell, value = Phi(cu) + s * gP(cu)
+  double s;
+};
+DV LowFace low_face(const RunView& v, bool dirx, long long cb, long long cf, double fnv,
+                    double xf) {
+  LowFace F;
+  F.av = dirx ? cb : cf;
+  F.ar = dirx ? cf : cb;
+  F.cu = cb;
+  F.s = 0.;
+  if (v.pb == 0) {
+    const int ax = dirx ? 0 : 1;
+    const long long P = v.pitch;
+    const double dxl = plus_zero(v.XcL[ax * P + cf] - v.XcL[ax * P + cb]);
+    F.cu = pos(fnv * dxl) ? cb : cf;
+    F.s = plus_zero(xf - v.XcL[ax * P + F.cu]);
+  }
+  return F;
+}
+DV double low_face_value(const RunView& v, const LowFace& F, int k) {
+  const long long P = v.pitch;
+  if (v.pb == 0) return v.Phi[k * P + F.cu] + F.s * v.gP[k * P + F.cu];
+  return v.dPAv[k * P + F.av] - v.dPAr[k * P + F.ar];
+}
+
 // Conservative update of one sweep (Remap::computeUremap{1,2},
 // remap/PhaseRemap1.cc:459-568, PhaseRemap2.cc:454-497).
-struct SweepUpdate {
+// FACES: 0 = the face values come from the face plane (order 3, written by
+// SweepFace), 1 = they are formed here (orders 1-2), 2 = the run's order
+// decides (batched launches).
+template <int FACES>
+struct SweepUpdateT {
   int sweep;
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
     const Ctrl& C = *v.ctrl;
@@ -1122,6 +1121,7 @@ struct SweepUpdate {
     long long fidx[2];
     double coef[2];
     double nrm[2];  // outer normal component of face 0 / face 1 along the sweep
+    double fva, fvb;  // normal velocities of face 0 / face 1
     const long long n0 = (long long)i * (v.nx + 1) + j;
     if (dirx) {
       has[0] = (j >= 1);
@@ -1131,6 +1131,8 @@ struct SweepUpdate {
       const double fl = ld(v.flv, i);
       const double va = fnv_vertical(v, n0, n0 + v.nx + 1);
       const double vb = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);
+      fva = va;
+      fvb = vb;
       const double na = ld(v.nout, 0 * P + c), nb_ = ld(v.nout, 1 * P + c);
       nrm[0] = na;
       nrm[1] = nb_;
@@ -1149,6 +1151,8 @@ struct SweepUpdate {
       const double fl = ld(v.flh, j);
       const double va = fnv_horizontal(v, n0, n0 + 1);
       const double vb = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);
+      fva = va;
+      fvb = vb;
       const double na = ld(v.nout, 2 * P + c), nb_ = ld(v.nout, 3 * P + c);
       nrm[0] = na;
       nrm[1] = nb_;
@@ -1158,6 +1162,19 @@ struct SweepUpdate {
       } else {
         coef[0] = mul_pm1(fl, na);
         coef[1] = mul_pm1(fl, nb_);
+      }
+    }
+    // orders 1-2: the two faces' reconstruction (back / front cells as
+    // SweepFace names them, the face's abscissa or ordinate)
+    const bool form = (FACES == 1) || (FACES == 2 && v.order <= 2);
+    LowFace lf[2];
+    if (form) {
+      if (dirx) {
+        if (has[0]) lf[0] = low_face(v, true, c - 1, c, fva, ld(v.xs, j));
+        if (has[1]) lf[1] = low_face(v, true, c, c + 1, fvb, ld(v.xs, j + 1));
+      } else {
+        if (has[0]) lf[0] = low_face(v, false, c, c - v.nx, fva, ld(v.ys, i));
+        if (has[1]) lf[1] = low_face(v, false, c + v.nx, c, fvb, ld(v.ys, i + 1));
       }
     }
     // dual-method components: masses (A1) or volumes (A2)
@@ -1176,8 +1193,13 @@ struct SweepUpdate {
   #pragma unroll
       for (int t = 0; t < 4; ++t) {
         const int k = k0 + t;
-        qa[t] = (k < ncomp && has[0]) ? v.phiF[k * FP + fidx[0]] : 0.;
-        qb[t] = (k < ncomp && has[1]) ? v.phiF[k * FP + fidx[1]] : 0.;
+        if (form) {
+          qa[t] = (k < ncomp && has[0]) ? low_face_value(v, lf[0], k) : 0.;
+          qb[t] = (k < ncomp && has[1]) ? low_face_value(v, lf[1], k) : 0.;
+        } else {
+          qa[t] = (k < ncomp && has[0]) ? v.phiF[k * FP + fidx[0]] : 0.;
+          qb[t] = (k < ncomp && has[1]) ? v.phiF[k * FP + fidx[1]] : 0.;
+        }
         ui[t] = (k < ncomp) ? Uin[k * P + c] : 0.;
       }
       // a group whose face values are all zeros: each component keeps its
@@ -1772,16 +1794,15 @@ __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
 
 __global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
 __global__ void __launch_bounds__(kBX* kBY, 6) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
-__global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { plain_items(v, FaceGrad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_grad(RunView v, int sweep) { plain_items(v, O3Grad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_ystar(RunView v, int sweep) { plain_items(v, O3Ystar{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) { plain_items(v, SweepGradT<0>{sweep}); }
 // eight resident blocks: the kernel waits on memory more than it computes
 // at rest; measured faster than the register-limited four to six
 __global__ void __launch_bounds__(kBX* kBY, 8) k_sweep_grad_pb(RunView v, int sweep) { plain_items(v, SweepGradT<1>{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFaceT<2>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdate{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdateT<0>{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_update_f(RunView v, int sweep) { plain_items(v, SweepUpdateT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
 // ten resident blocks: where nodes are quiet the kernel waits on memory
 __global__ void __launch_bounds__(kBX* kBY, 10) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
@@ -1816,12 +1837,10 @@ __device__ __forceinline__ void batch_items(const BatchArgs& b, const F& f) {
 
 __global__ void __launch_bounds__(kBatchThreads) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_face_lo(BatchArgs b) { batch_items(b, SweepFaceT<2>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdate{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_final(BatchArgs b) { batch_items(b, Final{}); }
@@ -1884,9 +1903,9 @@ int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* 
   auto H = [&](int kind) {
     if (hook) (*hook)(kind);
   };
-  // limited slopes feed the order-2 face values and PenteBorne only
+  // limited slopes (with their face gradients) feed the order-2 face values
+  // and PenteBorne only
   if (v.order == 2 || (v.order == 3 && v.pb == 1)) {
-    H(11); k_face_grad<<<fg, blk, 0, s>>>(v, sweep); ++nk;
     H(4);
     if (v.pb == 1) k_sweep_grad_pb<<<cg, blk, 0, s>>>(v, sweep);
     else k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep);
@@ -1896,10 +1915,11 @@ int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* 
     H(16); k_o3_grad<<<cg, blk, 0, s>>>(v, sweep); ++nk;
     H(17); k_o3_ystar<<<cg, blk, 0, s>>>(v, sweep); ++nk;
     H(5); k_sweep_face3<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+    H(6); k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
   } else {
-    H(5); k_sweep_face<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+    // orders 1-2: the update forms its face values
+    H(6); k_sweep_update_f<<<cg, blk, 0, s>>>(v, sweep); ++nk;
   }
-  H(6); k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
   return nk;
 }
 
@@ -1949,7 +1969,6 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
   H(3); kb_lag_cells<<<L.grid[kPhLagCells], T, 0, s>>>(args(kPhLagCells, 0)); ++nk;
   for (int sweep = 1; sweep <= 2; ++sweep) {
     if (L.any_order2) {
-      H(11); kb_face_grad<<<L.grid[kPhFaceGrad], T, 0, s>>>(args(kPhFaceGrad, sweep)); ++nk;
       H(4);
       if (L.variant & kBatchNoPB)
         kb_sweep_grad_nopb<<<L.grid[kPhSweepGrad], T, 0, s>>>(args(kPhSweepGrad, sweep));
@@ -1957,12 +1976,10 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
         kb_sweep_grad<<<L.grid[kPhSweepGrad], T, 0, s>>>(args(kPhSweepGrad, sweep));
       ++nk;
     }
-    H(5);
-    if (L.variant & kBatchNoOrder3)
-      kb_sweep_face_lo<<<L.grid[kPhSweepFace], T, 0, s>>>(args(kPhSweepFace, sweep));
-    else
-      kb_sweep_face<<<L.grid[kPhSweepFace], T, 0, s>>>(args(kPhSweepFace, sweep));
-    ++nk;
+    // order-3 runs' face values (the update forms those of the others)
+    if (!(L.variant & kBatchNoOrder3)) {
+      H(5); kb_sweep_face<<<L.grid[kPhSweepFace], T, 0, s>>>(args(kPhSweepFace, sweep)); ++nk;
+    }
     H(6); kb_sweep_update<<<L.grid[kPhSweepUpdate], T, 0, s>>>(args(kPhSweepUpdate, sweep)); ++nk;
     H(7); kb_dual_grad<<<L.grid[kPhDualGrad], T, 0, s>>>(args(kPhDualGrad, sweep)); ++nk;
     H(8); kb_dual_update<<<L.grid[kPhDualUpdate], T, 0, s>>>(args(kPhDualUpdate, sweep)); ++nk;
@@ -1978,9 +1995,9 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
 int batch_occupancy(int* blocks_per_sm, int variant) {
   const void* fns[kNumPhases] = {
       (const void*)kb_lag_nodes,   (const void*)kb_lag_cells,
-      (const void*)kb_face_grad,
+      (const void*)kb_dual_grad,  // face-gradient phase: no longer launched
       (variant & kBatchNoPB) ? (const void*)kb_sweep_grad_nopb : (const void*)kb_sweep_grad,
-      (variant & kBatchNoOrder3) ? (const void*)kb_sweep_face_lo : (const void*)kb_sweep_face,
+      (const void*)kb_sweep_face,
       (const void*)kb_sweep_update,
       (const void*)kb_dual_grad,   (const void*)kb_dual_update,
       (const void*)kb_final};
