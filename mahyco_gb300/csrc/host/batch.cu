@@ -123,9 +123,12 @@ void fill_launch(BatchPlan* p) {
       L.ntiles[on][w] = p->d_ntiles + on * kNumTileShapes + w;
     }
   L.any_order2 = 0;
+  L.any_face = 0;
   L.variant = kBatchNoOrder3 | kBatchNoPB;
   for (auto* r : p->runs) {
     if (r->v.order > 1) L.any_order2 = 1;
+    // the face phase serves order-3 runs and order-1 runs without PenteBorne
+    if (r->v.order == 3 || (r->v.order == 1 && r->v.pb == 0)) L.any_face = 1;
     if (r->v.order == 3) L.variant &= ~kBatchNoOrder3;
     if (r->v.pb == 1) L.variant &= ~kBatchNoPB;
   }

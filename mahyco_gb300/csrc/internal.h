@@ -238,6 +238,8 @@ struct BatchLaunch {
   int shape[kNumPhases];  // tile shape index per phase
   int grid[kNumPhases];   // persistent grid size per phase
   int any_order2;         // launch the slope phases
+  int any_face;           // launch the face phase (order 3, or order 1
+                          // without PenteBorne)
   int variant;            // kBatch* bits: lighter kernels when no run needs
                           // the order-3 faces / the PenteBorne slopes
 };

@@ -8,11 +8,13 @@
 //                                                        ConditionsLimites.cc)
 //   k_lag_cells    sub-volumes, densities, div u, pseudo-viscosity, energy,
 //                  EOS, mean pressure, then the cell part of PrepareRemap
-//   sweep x2:  k_sweep_grad (face gradients, limited slopes / plateau-slope
-//              integrals), k_sweep_update_f (face values of orders 1-2 and
-//              the conservative update; order 3: k_o3_grad, k_o3_ystar,
-//              k_sweep_face3, k_sweep_update), k_dual_grad + k_dual_update
-//              (nodal momentum remap)
+//   sweep x2:  k_sweep_grad (face gradients, limited slopes and the
+//              order-2 face values of upwind cells; with PenteBorne
+//              k_sweep_grad_pb: plateau-slope integrals), k_sweep_update
+//              (conservative update; k_sweep_update_f forms the PenteBorne
+//              face values itself; order 3: k_o3_grad, k_o3_ystar,
+//              k_sweep_face3 first; order 1: k_sweep_face first),
+//              k_dual_grad + k_dual_update (nodal momentum remap)
 //   k_final        remapVariables + EOS + mean pressure + next dt / pmax
 //   k_end          loop condition and time swap
 //
@@ -728,8 +730,45 @@ struct SweepGradT {
     const double xc = v.XcL[ax * P + c];
     // one denominator per face, shared by its components (the IEEE quotient
     // bit for bit, see shared_div)
-    const SharedDiv Sp = shared_div(has_gp ? plus_zero(v.XcL[ax * P + cf] - xc) : 1.0);
-    const SharedDiv Sm = shared_div(has_gm ? plus_zero(xc - v.XcL[ax * P + cb]) : 1.0);
+    const double dxp = has_gp ? plus_zero(v.XcL[ax * P + cf] - xc) : 1.0;
+    const double dxm = has_gm ? plus_zero(xc - v.XcL[ax * P + cb]) : 1.0;
+    const SharedDiv Sp = shared_div(dxp);
+    const SharedDiv Sm = shared_div(dxm);
+    // Without PenteBorne the order-2 face values (SweepFace) are formed here:
+    // a face's value is Phi(cu) + (x_f - XcL(cu)) * slope(cu) of its upwind
+    // cell cu = pos(fnv * dxl) ? back : front, with dxl = XcL(front) -
+    // XcL(back), the plus face's denominator above (c its back cell) or the
+    // minus face's (c its front cell).  Each inner face has one upwind cell,
+    // which writes its value; the slopes themselves are not stored.  (The
+    // update cannot form these values: in the first sweep it rewrites Phi,
+    // which a neighbour's face value reads.)
+    bool up_p = false, up_m = false;
+    double sp = 0., sm = 0.;
+    long long fp = 0, fm = 0;
+    const long long FP = v.fpitch;
+    if (pb == 0) {
+      const long long n0 = (long long)i * (v.nx + 1) + j;
+      double fnv_p, fnv_m, xf_p, xf_m;
+      if (dirx) {
+        fm = (long long)i * (v.nx + 1) + j;  // left face
+        fp = fm + 1;                         // right face
+        fnv_m = fnv_vertical(v, n0, n0 + v.nx + 1);
+        fnv_p = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);
+        xf_m = ld(v.xs, j);
+        xf_p = ld(v.xs, j + 1);
+      } else {
+        fp = (long long)i * v.nx + j;        // bottom face
+        fm = fp + v.nx;                      // top face
+        fnv_p = fnv_horizontal(v, n0, n0 + 1);
+        fnv_m = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);
+        xf_p = ld(v.ys, i);
+        xf_m = ld(v.ys, i + 1);
+      }
+      up_p = has_gp && pos(fnv_p * dxp);   // c is the plus face's back cell
+      up_m = has_gm && !pos(fnv_m * dxm);  // c is the minus face's front cell
+      sp = plus_zero(xf_p - xc);
+      sm = plus_zero(xf_m - xc);
+    }
     double grad[kMaxComp];
     for (int k = 0; k < ngrad; ++k) {
       const double y0 = v.Phi[k * P + c];
@@ -737,7 +776,10 @@ struct SweepGradT {
       const double gp = has_gp ? qdiv_shared(Sp, v.Phi[k * P + cf] - y0) : 0.;
       const double gm = has_gm ? qdiv_shared(Sm, y0 - v.Phi[k * P + cb]) : 0.;
       grad[k] = limit_grad1(lim, gp, gm, yp, ym, h0, hp, hm);
-      if (pb == 0) v.gP[k * P + c] = grad[k];
+      if (pb == 0) {
+        if (up_p) v.phiF[k * FP + fp] = y0 + sp * grad[k];
+        if (up_m) v.phiF[k * FP + fm] = y0 + sm * grad[k];
+      }
     }
     if (pb == 1) {
       const int plim = vp ? v.limiter_pure : v.limiter;
@@ -928,8 +970,10 @@ template <int ORDERS>
 struct SweepFaceT {
   int sweep;
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
-    // batched launches: the update of an order-1/2 run forms its face values
-    if (ORDERS == 3 && v.order <= 2) return;
+    // batched launches: an order-2 run without PenteBorne has its face
+    // values from the slope kernel, a PenteBorne run of orders 1-2 forms them
+    // in the update
+    if (ORDERS == 3 && (v.order == 2 || (v.order == 1 && v.pb == 1))) return;
     const Ctrl& C = *v.ctrl;
     const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
     const long long P = v.pitch, FP = v.fpitch;
@@ -1064,43 +1108,33 @@ struct SweepFaceT {
   }
 };
 
-// Face values of orders 1-2 (Remap::computeUpwindFaceQuantitiesForProjection
-// {1,2}, remap/PhaseRemap1.cc:331-452) formed where they are used: the
-// update of each cell forms the values of its two faces with SweepFace's
-// operations (so each inner face's value is formed by both of its cells,
-// bit for bit the same), instead of reading them from a face plane.
+// PenteBorne face values of orders 1-2 (Remap::computeUpwindFaceQuantities
+// ForProjection{1,2}, remap/PhaseRemap1.cc:331-452) formed where they are
+// used: the update of each cell forms the values of its two faces,
+// dPAv(av) - dPAr(ar) as SweepFace forms them (each inner face's value is
+// formed by both of its cells, bit for bit the same), instead of reading
+// them from a face plane.  The update writes neither plane, so this is safe
+// while it rewrites Phi.
 struct LowFace {
-  long long av, ar;  // PenteBorne: value = dPAv(av) - dPAr(ar)
-  long long cu;      // otherwise: the upwind cell, value = Phi(cu) + s * gP(cu)
-  double s;
+  long long av, ar;
 };
-DV LowFace low_face(const RunView& v, bool dirx, long long cb, long long cf, double fnv,
-                    double xf) {
+DV LowFace low_face(bool dirx, long long cb, long long cf) {
   LowFace F;
   F.av = dirx ? cb : cf;
   F.ar = dirx ? cf : cb;
-  F.cu = cb;
-  F.s = 0.;
-  if (v.pb == 0) {
-    const int ax = dirx ? 0 : 1;
-    const long long P = v.pitch;
-    const double dxl = plus_zero(v.XcL[ax * P + cf] - v.XcL[ax * P + cb]);
-    F.cu = pos(fnv * dxl) ? cb : cf;
-    F.s = plus_zero(xf - v.XcL[ax * P + F.cu]);
-  }
   return F;
 }
 DV double low_face_value(const RunView& v, const LowFace& F, int k) {
   const long long P = v.pitch;
-  if (v.pb == 0) return v.Phi[k * P + F.cu] + F.s * v.gP[k * P + F.cu];
   return v.dPAv[k * P + F.av] - v.dPAr[k * P + F.ar];
 }
 
 // Conservative update of one sweep (Remap::computeUremap{1,2},
 // remap/PhaseRemap1.cc:459-568, PhaseRemap2.cc:454-497).
-// FACES: 0 = the face values come from the face plane (order 3, written by
-// SweepFace), 1 = they are formed here (orders 1-2), 2 = the run's order
-// decides (batched launches).
+// FACES: 0 = the face values come from the face plane (written by the slope
+// kernel at order 2 without PenteBorne, by SweepFace otherwise), 1 = they
+// are formed here (PenteBorne at orders 1-2), 2 = the run's options decide
+// (batched launches).
 template <int FACES>
 struct SweepUpdateT {
   int sweep;
@@ -1121,7 +1155,6 @@ struct SweepUpdateT {
     long long fidx[2];
     double coef[2];
     double nrm[2];  // outer normal component of face 0 / face 1 along the sweep
-    double fva, fvb;  // normal velocities of face 0 / face 1
     const long long n0 = (long long)i * (v.nx + 1) + j;
     if (dirx) {
       has[0] = (j >= 1);
@@ -1131,8 +1164,6 @@ struct SweepUpdateT {
       const double fl = ld(v.flv, i);
       const double va = fnv_vertical(v, n0, n0 + v.nx + 1);
       const double vb = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);
-      fva = va;
-      fvb = vb;
       const double na = ld(v.nout, 0 * P + c), nb_ = ld(v.nout, 1 * P + c);
       nrm[0] = na;
       nrm[1] = nb_;
@@ -1151,8 +1182,6 @@ struct SweepUpdateT {
       const double fl = ld(v.flh, j);
       const double va = fnv_horizontal(v, n0, n0 + 1);
       const double vb = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);
-      fva = va;
-      fvb = vb;
       const double na = ld(v.nout, 2 * P + c), nb_ = ld(v.nout, 3 * P + c);
       nrm[0] = na;
       nrm[1] = nb_;
@@ -1164,17 +1193,17 @@ struct SweepUpdateT {
         coef[1] = mul_pm1(fl, nb_);
       }
     }
-    // orders 1-2: the two faces' reconstruction (back / front cells as
-    // SweepFace names them, the face's abscissa or ordinate)
-    const bool form = (FACES == 1) || (FACES == 2 && v.order <= 2);
+    // PenteBorne at orders 1-2: the two faces' back / front cells as
+    // SweepFace names them
+    const bool form = (FACES == 1) || (FACES == 2 && v.order <= 2 && v.pb == 1);
     LowFace lf[2];
     if (form) {
       if (dirx) {
-        if (has[0]) lf[0] = low_face(v, true, c - 1, c, fva, ld(v.xs, j));
-        if (has[1]) lf[1] = low_face(v, true, c, c + 1, fvb, ld(v.xs, j + 1));
+        lf[0] = low_face(true, c - 1, c);
+        lf[1] = low_face(true, c, c + 1);
       } else {
-        if (has[0]) lf[0] = low_face(v, false, c, c - v.nx, fva, ld(v.ys, i));
-        if (has[1]) lf[1] = low_face(v, false, c + v.nx, c, fvb, ld(v.ys, i + 1));
+        lf[0] = low_face(false, c, c - v.nx);
+        lf[1] = low_face(false, c + v.nx, c);
       }
     }
     // dual-method components: masses (A1) or volumes (A2)
@@ -1800,6 +1829,7 @@ __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) {
 // eight resident blocks: the kernel waits on memory more than it computes
 // at rest; measured faster than the register-limited four to six
 __global__ void __launch_bounds__(kBX* kBY, 8) k_sweep_grad_pb(RunView v, int sweep) { plain_items(v, SweepGradT<1>{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFaceT<2>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdateT<0>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update_f(RunView v, int sweep) { plain_items(v, SweepUpdateT<1>{sweep}); }
@@ -1916,9 +1946,16 @@ int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* 
     H(17); k_o3_ystar<<<cg, blk, 0, s>>>(v, sweep); ++nk;
     H(5); k_sweep_face3<<<fg, blk, 0, s>>>(v, sweep); ++nk;
     H(6); k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
-  } else {
-    // orders 1-2: the update forms its face values
+  } else if (v.pb == 1) {
+    // PenteBorne, orders 1-2: the update forms its face values
     H(6); k_sweep_update_f<<<cg, blk, 0, s>>>(v, sweep); ++nk;
+  } else {
+    // without PenteBorne the slope kernel wrote the order-2 face values; at
+    // order 1 (no slopes) the face kernel forms them
+    if (v.order == 1) {
+      H(5); k_sweep_face<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+    }
+    H(6); k_sweep_update<<<cg, blk, 0, s>>>(v, sweep); ++nk;
   }
   return nk;
 }
@@ -1976,8 +2013,10 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
         kb_sweep_grad<<<L.grid[kPhSweepGrad], T, 0, s>>>(args(kPhSweepGrad, sweep));
       ++nk;
     }
-    // order-3 runs' face values (the update forms those of the others)
-    if (!(L.variant & kBatchNoOrder3)) {
+    // face values of order-3 runs and of order-1 runs without PenteBorne
+    // (the slope phase writes those of order-2 runs without PenteBorne, the
+    // update forms the PenteBorne ones)
+    if (L.any_face) {
       H(5); kb_sweep_face<<<L.grid[kPhSweepFace], T, 0, s>>>(args(kPhSweepFace, sweep)); ++nk;
     }
     H(6); kb_sweep_update<<<L.grid[kPhSweepUpdate], T, 0, s>>>(args(kPhSweepUpdate, sweep)); ++nk;
