@@ -124,11 +124,13 @@ void fill_launch(BatchPlan* p) {
     }
   L.any_order2 = 0;
   L.any_face = 0;
+  L.any_face_grad = 0;
   L.variant = kBatchNoOrder3 | kBatchNoPB;
   for (auto* r : p->runs) {
     if (r->v.order > 1) L.any_order2 = 1;
     // the face phase serves order-3 runs and order-1 runs without PenteBorne
     if (r->v.order == 3 || (r->v.order == 1 && r->v.pb == 0)) L.any_face = 1;
+    if (r->v.order == 2 && r->v.pb == 0) L.any_face_grad = 1;
     if (r->v.order == 3) L.variant &= ~kBatchNoOrder3;
     if (r->v.pb == 1) L.variant &= ~kBatchNoPB;
   }

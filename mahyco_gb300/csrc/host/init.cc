@@ -39,6 +39,22 @@ int init_bc(const hydro_spec& s, HostInit& h) {
     h.v_left[1] = 0.0;
     h.bc_top = kBcSym;
     h.bc_bottom = kBcSym;
+  } else if (t == 0 || t == 11) {
+    // UnitTestCase / BiUnitTestCase (Init.cc:65-93): velocity (1, 0)
+    // imposed on every side, a flux condition on the left
+    h.bc_right = kBcImposed;
+    h.v_right[0] = 1.0;
+    h.v_right[1] = 0.0;
+    h.bc_left = kBcImposed;
+    h.v_left[0] = 1.0;
+    h.v_left[1] = 0.0;
+    h.flux_bc = kFluxLeft;
+    h.bc_bottom = kBcImposed;
+    h.v_bottom[0] = 1.0;
+    h.v_bottom[1] = 0.0;
+    h.bc_top = kBcImposed;
+    h.v_top[0] = 1.0;
+    h.v_top[1] = 0.0;
   } else if (t == 8 || t == 19) {
     // Advection Y (Init.cc:51-64)
     h.bc_bottom = kBcImposed;
@@ -63,7 +79,7 @@ int init_options(const hydro_spec& s, HostInit& h) {
   if (s.nx < 2 || s.ny < 2) return fail(-12, "nx and ny must be >= 2");
   const int t = s.test_case;
   const bool advection = (t == 7 || t == 8 || t == 18 || t == 19 || t == 20 || t == 21);
-  if (!(t == 4 || t == 5 || t == 15 || t == 16 || t == 1 || advection))
+  if (!(t == 4 || t == 5 || t == 15 || t == 16 || t == 1 || t == 0 || t == 11 || advection))
     return fail(-10, "VNR initialisation: unsupported test case");
   h.nx = s.nx;
   h.ny = s.ny;

@@ -15,6 +15,9 @@ struct HostInit {
   double v_left[2] = {0, 1}, v_right[2] = {0, 1}, v_bottom[2] = {1, 0},
          v_top[2] = {1, 0};
   int periodic_x = 0;
+  // sides whose remap takes a boundary flux (Cdl::left/right/bottom/top
+  // FluxBC, remap/BoundaryFluxes.cc): kFlux* bits
+  int flux_bc = 0;
   // initial dt_n when it does not come from the initial state (Eucclhyd,
   // VNR without the Lagrange phase); VNR with it reduces over the cells on
   // the device
@@ -28,7 +31,7 @@ struct HostInit {
 int init_options(const hydro_spec& spec, HostInit& out);
 
 // Eucclhyd set-up (eucclhyd_remap/Init.cc) for the Sod, bi-material Sod,
-// triple-point and Sedov cases.
+// triple-point, Sedov, Noh, shock-bubble and unit test cases.
 int init_options_euc(const hydro_spec& spec, HostInit& out);
 
 }  // namespace hydro

@@ -83,6 +83,11 @@ size_t layout(RunView& v, char* base) {
   v.dPAv = a.take<double>(nc * P);
   v.dPAr = a.take<double>(nc * P);
   v.DPF = a.take<double>(nb * P);
+  // face gradients of runs without PenteBorne (the slope kernel reads them
+  // while it writes face values into phiF): the plateau-slope integral
+  // planes, which those runs never use (2 nc cell planes hold nc face
+  // planes: FP <= 2 P for nx, ny >= 2)
+  v.phiG = v.dPAv;
   v.phiF = a.take<double>(nc * FP);
   v.FFd = a.take<double>(nb * P);
   if (v.order == 3) {
@@ -272,6 +277,7 @@ int prepare_run(const hydro_spec& spec_in, PreparedRun& pr) {
     v.v_top[d] = h.v_top[d];
   }
   v.periodic_x = h.periodic_x;
+  v.flux_bc = h.flux_bc;
   pr.bytes = layout(v, nullptr);
   return 0;
 }

@@ -19,6 +19,8 @@ int fail(int rc, const std::string& msg);
 constexpr int kBcSym = 200;
 constexpr int kBcImposed = 201;
 constexpr int kBcPeriodic = 203;
+// sides with a boundary flux in the remap (Cdl::leftFluxBC ... topFluxBC)
+constexpr int kFluxLeft = 1, kFluxRight = 2, kFluxBottom = 4, kFluxTop = 8;
 
 // Number of conserved components carried through the remap.  The reference
 // carries 13 (nbequamax, includes/Constantes.h:9-13); for nbmat materials
@@ -64,6 +66,7 @@ struct RunView {
   int bc_left, bc_right, bc_bottom, bc_top;
   double v_left[2], v_right[2], v_bottom[2], v_top[2];
   int periodic_x;
+  int flux_bc;        // kFlux* bits: sides whose remap takes a boundary flux
 
   // ---- constant Euler geometry
   const double* xs;      // nx+1 node abscissae (dx * j)
@@ -95,6 +98,8 @@ struct RunView {
   double *dPAv, *dPAr;  // ncomp planes (plateau-slope swept integrals)
   double* DPF;        // nbmat planes (plateau-slope dual mass flux)
   double* phiF;       // ncomp face planes
+  double* phiG;       // ncomp face planes of face gradients (runs without
+                      // PenteBorne: aliases dPAv / dPAr, unused by them)
   double* FFd;        // nbmat planes: each cell's share of the nodal mass
                       // fluxes of the sweep (A1 / A2 dual methods)
   const unsigned char* nsym;  // VNR: per node, 1 where the corner normals of
@@ -239,6 +244,8 @@ struct BatchLaunch {
   int grid[kNumPhases];   // persistent grid size per phase
   int any_order2;         // launch the slope phases
   int any_face;           // launch the face phase (order 3, or order 1
+                          // without PenteBorne)
+  int any_face_grad;      // launch the face-gradient phase (order 2
                           // without PenteBorne)
   int variant;            // kBatch* bits: lighter kernels when no run needs
                           // the order-3 faces / the PenteBorne slopes

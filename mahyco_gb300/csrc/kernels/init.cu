@@ -182,6 +182,22 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_cells_vnr(RunView v, int t, 
       pm[0] = p;
       cm[0] = sqrt(g * rhom[0] / pm[0]);
       snd = cm[0];
+    } else if (t == 0 || t == 11) {
+      // unit tests (Init.cc:331-361): density 1 left of x = 0.4, 0.1 right
+      // of it (a cell centred on 0.4 keeps 0), pressure 1, sound speed
+      // sqrt(gamma), material 1 in every cell
+      fm[0] = 1.; mfm[0] = 1.;
+      p = 1.0; pm[0] = 1.0; pm[1] = 0.0;
+      snd = sqrt(g); cm[0] = sqrt(g); cm[1] = sqrt(g);
+      const double r = Xc[0];
+      if (r < 0.4) {
+        rho = 1.; rhom[0] = 1.;
+      } else if (r > 0.4) {
+        rho = 0.1; rhom[0] = 0.1;
+      }
+      if (r > 0.6) {
+        rho = 0.1; rhom[0] = 0.1;
+      }
     } else if (t == 18 && variant == 2) {
       // advection step (extension): rho 1 | 0.1 at x = 0.5, two materials
       const int m = (Xc[0] < 0.5) ? 0 : 1;
@@ -309,8 +325,8 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_nodes_vnr(RunView v, int t, 
   const long long pn = i * (v.nx + 1) + j;
   const double x0 = xs(v, j), x1 = ys(v, i);
   double u = 0.0, w = 0.0;
-  if (t == 18 && variant == 2) {
-    u = 1.0;
+  if ((t == 18 && variant == 2) || t == 0 || t == 11) {
+    u = 1.0;  // the advection step extension; the unit tests (Init.cc:362-370)
   } else if (t == 7 || t == 8 || t == 18 || t == 19 || t == 20 || t == 21) {
     const bool isx = (t == 7 || t == 18 || t == 20);
     const bool vit = (t == 20 || t == 21);
@@ -521,6 +537,57 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_cells_euc(RunView v, int t, 
     rho = d;
     fm[m] = 1.; mfm[m] = 1.;
     rhom[m] = d;
+  } else if (t == 14) {
+    // BiShockBubble (Init.cc:272-302, 411-415, 528-560): air everywhere,
+    // the bubble (centre (0.320, 0.04), radius 0.025) overrides it; both
+    // energies with the first material's exponent, as the reference writes
+    e = 1.e5 / ((g[0] - 1.0) * 1.0);
+    em[0] = e;
+    rho = 1.0;
+    rhom[0] = 1.0;
+    fm[0] = 1.; mfm[0] = 1.;
+    const double r = sqrt((x0 - 0.320) * (x0 - 0.320) + (x1 - 0.04) * (x1 - 0.04));
+    if (r <= 0.025) {
+      e = 1.e5 / ((g[0] - 1.0) * 0.182);
+      em[0] = 0.;
+      em[1] = e;
+      rhom[0] = 0.0;
+      rhom[1] = 0.182;
+      rho = 0.182;
+      fm[0] = 0.; fm[1] = 1.;
+      mfm[0] = 0.; mfm[1] = 1.;
+    }
+    if (x0 >= 0.60) {
+      v.uc[c] = -124.824;
+      v.uco[c] = -124.824;
+    }
+  } else if (t == 6 || t == 17 || t == 0 || t == 11) {
+    // Noh, unit tests (Init.cc:202-214): e0 = p0 / ((1.4 - 1) rho0) with
+    // p0 = rho0 = 1, for the cell and every material
+    const double e0 = 1. / ((1.4 - 1.0) * 1.);
+    e = e0;
+    em[0] = em[1] = em[2] = e0;
+    if (t == 6 || t == 17) {
+      // initCellVelocity (Init.cc:394-401): -u0 * n / |n| with u0 = 0 (a
+      // signed zero); no density initialisation (zero density)
+      const double u0 = 0.;
+      const double nv = sqrt(x0 * x0 + x1 * x1);
+      v.uc[c] = -u0 * x0 / nv;
+      v.uc[P + c] = -u0 * x1 / nv;
+      v.uco[c] = v.uc[c];
+      v.uco[P + c] = v.uc[P + c];
+    } else {
+      // velocity (1, 0) (Init.cc:416-419); density 1, material 1 left of
+      // x = 0.5 and (bi-material) material 2 right of it (Init.cc:438-480)
+      v.uc[c] = 1.0;
+      v.uc[P + c] = 0.0;
+      v.uco[c] = 1.0;
+      v.uco[P + c] = 0.0;
+      rho = 1.0;
+      const int m = (t == 11 && !(x0 <= 0.5)) ? 1 : 0;
+      fm[m] = 1.; mfm[m] = 1.;
+      rhom[m] = 1.0;
+    }
   } else {  // Sedov (test case 1; 12 has no density initialisation)
     const double e1 = 1.e-6 / ((g[0] - 1.0) * 1.);
     bool centre = false;

@@ -8,9 +8,10 @@
 //                                                        ConditionsLimites.cc)
 //   k_lag_cells    sub-volumes, densities, div u, pseudo-viscosity, energy,
 //                  EOS, mean pressure, then the cell part of PrepareRemap
-//   sweep x2:  k_sweep_grad (face gradients, limited slopes and the
-//              order-2 face values of upwind cells; with PenteBorne
-//              k_sweep_grad_pb: plateau-slope integrals), k_sweep_update
+//   sweep x2:  without PenteBorne k_face_grad (face gradients) and
+//              k_sweep_grad (limited slopes, the order-2 face values of
+//              upwind cells); with PenteBorne k_sweep_grad_pb (its face
+//              gradients, slopes and plateau-slope integrals); k_sweep_update
 //              (conservative update; k_sweep_update_f forms the PenteBorne
 //              face values itself; order 3: k_o3_grad, k_o3_ystar,
 //              k_sweep_face3 first; order 1: k_sweep_face first),
@@ -585,6 +586,40 @@ DV double fnv_horizontal(const RunView& v, long long na, long long nb) {
 }
 
 // ----------------------------------------------------------- remap sweep
+// Face gradients of one sweep for runs without PenteBorne
+// (Remap::computeGradPhiFace{1,2}, remap/PhaseRemap1.cc:22-55,
+// PhaseRemap2.cc:21-55): one thread per inner face perpendicular to the
+// sweep, (Phi(front) - Phi(back)) / deltaxLagrange, into the face-gradient
+// planes.  Every component has a slope there, and each face's gradients
+// are formed once (the PenteBorne slope kernel forms its few itself).
+struct FaceGrad {
+  int sweep;
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    if (v.order != 2 || v.pb != 0) return;
+    const Ctrl& C = *v.ctrl;
+    const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+    const long long P = v.pitch, FP = v.fpitch;
+    long long back, front, fidx;
+    int ax;
+    if (dirx) {
+      if (i >= v.ny || j < 1 || j >= v.nx) return;
+      front = (long long)i * v.nx + j;
+      back = front - 1;
+      fidx = (long long)i * (v.nx + 1) + j;
+      ax = 0;
+    } else {
+      if (j >= v.nx || i < 1 || i >= v.ny) return;
+      back = (long long)i * v.nx + j;
+      front = back - v.nx;
+      fidx = (long long)i * v.nx + j;
+      ax = 1;
+    }
+    const double dx = plus_zero(v.XcL[ax * P + front] - v.XcL[ax * P + back]);
+    for (int k = 0; k < v.ncomp; ++k)
+      v.phiG[k * FP + fidx] = qdiv(v.Phi[k * P + front] - v.Phi[k * P + back], dx);
+  }
+};
+
 // Limited slopes and plateau-slope integrals of one sweep
 // (Remap::computeGradPhiFace{1,2} + computeGradPhi{1,2},
 // remap/PhaseRemap1.cc:22-323, remap/PhaseRemap2.cc:21-323).
@@ -638,13 +673,16 @@ struct SweepGradT {
       has_gp = (i > 0);          // bottom face
       has_gm = (i < v.ny - 1);   // top face
     }
-    // The two face gradients are formed here (Remap::computeGradPhiFace
-    // {1,2}, remap/PhaseRemap1.cc:22-55): (Phi(front) - Phi(back)) /
-    // (XcL(front) - XcL(back)) with the reference's back / front cells, the
-    // "plus" face between c (back) and cf (front), the "minus" face between
-    // cb (back) and c (front).  Each inner face's gradient is formed by both
-    // of its cells with the same operations, so no face plane is written and
-    // read back; a cell that takes the no-flux exit below forms neither.
+    // With PenteBorne the two face gradients are formed here
+    // (Remap::computeGradPhiFace{1,2}, remap/PhaseRemap1.cc:22-55):
+    // (Phi(front) - Phi(back)) / (XcL(front) - XcL(back)) with the
+    // reference's back / front cells, the "plus" face between c (back) and
+    // cf (front), the "minus" face between cb (back) and c (front).  Each
+    // inner face's gradient is formed by both of its cells with the same
+    // operations, so no face plane is written and read back, and a cell that
+    // takes the no-flux exit below forms neither (the few integrated
+    // components only).  Without PenteBorne FaceGrad formed them once per
+    // face for every component.
     // Eucclhyd carries momentum (and kinetic energy) after the material
     // components instead of the VNR pseudo-viscosity, and has no dual remap
     const bool euc = (v.scheme == HYDRO_SCHEME_EUCCLHYD);
@@ -732,8 +770,8 @@ struct SweepGradT {
     // bit for bit, see shared_div)
     const double dxp = has_gp ? plus_zero(v.XcL[ax * P + cf] - xc) : 1.0;
     const double dxm = has_gm ? plus_zero(xc - v.XcL[ax * P + cb]) : 1.0;
-    const SharedDiv Sp = shared_div(dxp);
-    const SharedDiv Sm = shared_div(dxm);
+    const SharedDiv Sp = shared_div(pb == 1 ? dxp : 1.0);
+    const SharedDiv Sm = shared_div(pb == 1 ? dxm : 1.0);
     // Without PenteBorne the order-2 face values (SweepFace) are formed here:
     // a face's value is Phi(cu) + (x_f - XcL(cu)) * slope(cu) of its upwind
     // cell cu = pos(fnv * dxl) ? back : front, with dxl = XcL(front) -
@@ -746,19 +784,22 @@ struct SweepGradT {
     double sp = 0., sm = 0.;
     long long fp = 0, fm = 0;
     const long long FP = v.fpitch;
+    if (dirx) {
+      fm = (long long)i * (v.nx + 1) + j;  // left face
+      fp = fm + 1;                         // right face
+    } else {
+      fp = (long long)i * v.nx + j;        // bottom face
+      fm = fp + v.nx;                      // top face
+    }
     if (pb == 0) {
       const long long n0 = (long long)i * (v.nx + 1) + j;
       double fnv_p, fnv_m, xf_p, xf_m;
       if (dirx) {
-        fm = (long long)i * (v.nx + 1) + j;  // left face
-        fp = fm + 1;                         // right face
         fnv_m = fnv_vertical(v, n0, n0 + v.nx + 1);
         fnv_p = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);
         xf_m = ld(v.xs, j);
         xf_p = ld(v.xs, j + 1);
       } else {
-        fp = (long long)i * v.nx + j;        // bottom face
-        fm = fp + v.nx;                      // top face
         fnv_p = fnv_horizontal(v, n0, n0 + 1);
         fnv_m = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);
         xf_p = ld(v.ys, i);
@@ -773,8 +814,14 @@ struct SweepGradT {
     for (int k = 0; k < ngrad; ++k) {
       const double y0 = v.Phi[k * P + c];
       const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
-      const double gp = has_gp ? qdiv_shared(Sp, v.Phi[k * P + cf] - y0) : 0.;
-      const double gm = has_gm ? qdiv_shared(Sm, y0 - v.Phi[k * P + cb]) : 0.;
+      double gp = 0., gm = 0.;
+      if (pb == 1) {
+        if (has_gp) gp = qdiv_shared(Sp, v.Phi[k * P + cf] - y0);
+        if (has_gm) gm = qdiv_shared(Sm, y0 - v.Phi[k * P + cb]);
+      } else {
+        if (has_gp) gp = v.phiG[k * FP + fp];
+        if (has_gm) gm = v.phiG[k * FP + fm];
+      }
       grad[k] = limit_grad1(lim, gp, gm, yp, ym, h0, hp, hm);
       if (pb == 0) {
         if (up_p) v.phiF[k * FP + fp] = y0 + sp * grad[k];
@@ -1206,6 +1253,23 @@ struct SweepUpdateT {
         lf[1] = low_face(false, c + v.nx, c);
       }
     }
+    // Boundary flux (Remap::computeBoundaryFluxes, remap/BoundaryFluxes.cc
+    // :14-120, added after the neighbour faces' fluxes): on a side with a
+    // flux condition, the flux through the cell's boundary face carries the
+    // value of its opposite face.  bcf 1: face 0 (left / bottom) with face
+    // 1's value; 2: face 1 (right / top) with face 0's value.  The branches
+    // and their order are the reference's, including its test for the top
+    // side, which every cell up to the first one of the top row passes.
+    int bcf = 0;
+    if (v.flux_bc) {
+      if (dirx) {
+        if ((v.flux_bc & kFluxLeft) && j == 0) bcf = 1;
+        else if ((v.flux_bc & kFluxRight) && j == v.nx - 1) bcf = 2;
+      } else {
+        if ((v.flux_bc & kFluxBottom) && i == 0) bcf = 1;
+        else if ((v.flux_bc & kFluxTop) && c <= (long long)v.nx * (v.ny - 1)) bcf = 2;
+      }
+    }
     // dual-method components: masses (A1) or volumes (A2)
     const int doff = (v.dual_method == 1) ? 0 : nb;
     double U[kMaxComp];
@@ -1280,6 +1344,8 @@ struct SweepUpdateT {
             F1 = coef[1] * q1;
             red = has[0] ? red + F1 : plus_zero(F1);
           }
+          if (bcf == 1) red = red + coef[0] * q1;
+          else if (bcf == 2) red = red + coef[1] * q0;
           U[k] = uin - red;
         }
         same = same && ubits(U[k]) == ubits(uin);
@@ -1823,6 +1889,7 @@ __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
 
 __global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
 __global__ void __launch_bounds__(kBX* kBY, 6) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
+__global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { plain_items(v, FaceGrad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_grad(RunView v, int sweep) { plain_items(v, O3Grad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_ystar(RunView v, int sweep) { plain_items(v, O3Ystar{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) { plain_items(v, SweepGradT<0>{sweep}); }
@@ -1867,6 +1934,7 @@ __device__ __forceinline__ void batch_items(const BatchArgs& b, const F& f) {
 
 __global__ void __launch_bounds__(kBatchThreads) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
@@ -1936,6 +2004,9 @@ int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* 
   // limited slopes (with their face gradients) feed the order-2 face values
   // and PenteBorne only
   if (v.order == 2 || (v.order == 3 && v.pb == 1)) {
+    if (v.pb == 0) {
+      H(11); k_face_grad<<<fg, blk, 0, s>>>(v, sweep); ++nk;
+    }
     H(4);
     if (v.pb == 1) k_sweep_grad_pb<<<cg, blk, 0, s>>>(v, sweep);
     else k_sweep_grad<<<cg, blk, 0, s>>>(v, sweep);
@@ -2006,6 +2077,9 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
   H(3); kb_lag_cells<<<L.grid[kPhLagCells], T, 0, s>>>(args(kPhLagCells, 0)); ++nk;
   for (int sweep = 1; sweep <= 2; ++sweep) {
     if (L.any_order2) {
+      if (L.any_face_grad) {
+        H(11); kb_face_grad<<<L.grid[kPhFaceGrad], T, 0, s>>>(args(kPhFaceGrad, sweep)); ++nk;
+      }
       H(4);
       if (L.variant & kBatchNoPB)
         kb_sweep_grad_nopb<<<L.grid[kPhSweepGrad], T, 0, s>>>(args(kPhSweepGrad, sweep));
@@ -2034,7 +2108,7 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
 int batch_occupancy(int* blocks_per_sm, int variant) {
   const void* fns[kNumPhases] = {
       (const void*)kb_lag_nodes,   (const void*)kb_lag_cells,
-      (const void*)kb_dual_grad,  // face-gradient phase: no longer launched
+      (const void*)kb_face_grad,
       (variant & kBatchNoPB) ? (const void*)kb_sweep_grad_nopb : (const void*)kb_sweep_grad,
       (const void*)kb_sweep_face,
       (const void*)kb_sweep_update,

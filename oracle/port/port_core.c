@@ -281,6 +281,14 @@ static int vnr_init_bc(port_run* R) {
     R->leftBC = BC_IMPOSED; R->leftV[0] = 1.0; R->leftV[1] = 0.0;
     R->topBC = BC_SYM;
     R->bottomBC = BC_SYM;
+  } else if (t == 0 || t == 11) {
+    /* UnitTestCase / BiUnitTestCase (Init.cc:65-93): velocity (1, 0)
+     * imposed on every side, a flux condition on the left */
+    R->rightBC = BC_IMPOSED; R->rightV[0] = 1.0; R->rightV[1] = 0.0;
+    R->leftBC = BC_IMPOSED; R->leftV[0] = 1.0; R->leftV[1] = 0.0;
+    R->leftFluxBC = 1;
+    R->bottomBC = BC_IMPOSED; R->bottomV[0] = 1.0; R->bottomV[1] = 0.0;
+    R->topBC = BC_IMPOSED; R->topV[0] = 1.0; R->topV[1] = 0.0;
   } else if (t == 8 || t == 19) {
     R->bottomBC = BC_IMPOSED; R->bottomV[0] = 0.0; R->bottomV[1] = 1.0;
     R->bottomCellBC = BC_PERIODIC;
@@ -368,6 +376,39 @@ static int vnr_init_state(port_run* R) {
       R->c_n0[c] = R->cm_n0[NM * c];
     }
     for (long p = 0; p < R->nn; ++p) R->u_n0[2 * p] = R->u_n0[2 * p + 1] = 0.0;
+  } else if (t == 0 || t == 11) {
+    /* unit tests (Init.cc:331-361): density 1 left of x = 0.4, 0.1 right
+     * of it (the reference leaves a cell centred on 0.4 at 0), pressure 1,
+     * sound speed sqrt(gamma), velocity (1, 0) */
+    for (long c = 0; c < R->nc; ++c) {
+      double* f = R->fm + NM * c;
+      double* mf = R->mfm + NM * c;
+      f[0] = 1.; f[1] = 0.;
+      mf[0] = 1.; mf[1] = 0.;
+      R->p_n0[c] = 1.0;
+      R->pm_n0[NM * c] = 1.0;
+      R->pm_n0[NM * c + 1] = 0.0;
+      R->c_n0[c] = sqrt(g);
+      R->cm_n0[NM * c] = sqrt(g);
+      R->cm_n0[NM * c + 1] = sqrt(g);
+      R->rhom_n0[NM * c + 1] = 0.;
+      const double r = R->Xc0[2 * c];
+      if (r < 0.4) {
+        R->rho_n0[c] = 1.;
+        R->rhom_n0[NM * c] = 1.;
+      } else if (r > 0.4) {
+        R->rho_n0[c] = 0.1;
+        R->rhom_n0[NM * c] = 0.1;
+      }
+      if (r > 0.6) {
+        R->rho_n0[c] = 0.1;
+        R->rhom_n0[NM * c] = 0.1;
+      }
+    }
+    for (long p = 0; p < R->nn; ++p) {
+      R->u_n0[2 * p] = 1.0;
+      R->u_n0[2 * p + 1] = 0.0;
+    }
   } else if (t == 18 && R->s.init_variant == 2) {
     /* advection step (extension): material 1, rho 1, left of x = 0.5;
      * material 2, rho 0.1, right of it; uniform velocity (1, 0) */

@@ -150,13 +150,25 @@ static int init_bc(port_run* R) {
   memcpy(w->bcV[3], ex, sizeof ex);
   if (t == 4 || t == 5 || t == 15 || t == 16 || t == 2 || t == 13) {
     R->leftBC = R->rightBC = R->topBC = R->bottomBC = BC_SYM;
-  } else if (t == 1 || t == 12) {
+  } else if (t == 1 || t == 12 || t == 6 || t == 17) {
     R->leftBC = BC_SYM;
     R->bottomBC = BC_SYM;
     R->rightBC = BC_IMPOSED;
     R->topBC = BC_IMPOSED;
     w->bcV[1][0] = w->bcV[1][1] = 0.0;
     w->bcV[2][0] = w->bcV[2][1] = 0.0;
+  } else if (t == 14) {
+    /* BiShockBubble (Init.cc:30-46) */
+    R->leftBC = BC_SYM;
+    R->rightBC = BC_IMPOSED;
+    w->bcV[1][0] = -124.824;
+    w->bcV[1][1] = 0.0;
+    R->rightFluxBC = 1;
+    R->topBC = BC_SYM;
+    R->bottomBC = BC_SYM;
+  } else if (t == 0 || t == 11) {
+    /* unit tests: no branch, the Cdl defaults (condition 0) */
+    R->leftBC = R->rightBC = R->topBC = R->bottomBC = 0;
   } else {
     port_set_error("Eucclhyd: test case not supported by the restatement");
     return -1;
@@ -231,10 +243,40 @@ static int init_state(port_run* R) {
         if (nrm(R->X0 + 2 * nd[k]) < R->s.threshold) centre = 1;
       R->e_n0[c] = centre ? e1 + 0.244816 / (R->s.dx * R->s.dy) : e1;
       em[0] = R->e_n0[c];
+    } else if (t == 14) {
+      /* air everywhere, then the bubble (Init.cc:272-302) */
+      double e = 1.e5 / ((g[0] - 1.0) * 1.0);
+      em[0] = e;
+      em[1] = 0.;
+      R->e_n0[c] = e;
+      const double r = sqrt((xc[0] - 0.320) * (xc[0] - 0.320) + (xc[1] - 0.04) * (xc[1] - 0.04));
+      if (r <= 0.025) {
+        e = 1.e5 / ((g[0] - 1.0) * 0.182);
+        em[0] = 0.;
+        em[1] = e;
+        R->e_n0[c] = e;
+      }
+    } else if (t == 6 || t == 17 || t == 0 || t == 11) {
+      /* Init.cc:202-214 */
+      const double p0 = 1., rho0 = 1., gamma = 1.4;
+      const double e0 = p0 / ((gamma - 1.0) * rho0);
+      R->e_n0[c] = e0;
+      for (int m = 0; m < NM; ++m) em[m] = e0;
     }
-    /* initCellVelocity: zero for these cases */
+    /* initCellVelocity (Init.cc:391-421) */
     R->cell_u_n0[2 * c] = 0.0;
     R->cell_u_n0[2 * c + 1] = 0.0;
+    if (t == 6 || t == 17) {
+      const double u0 = 0.;
+      const double n1 = xc[0], n2 = xc[1];
+      const double nv = sqrt(n1 * n1 + n2 * n2);
+      R->cell_u_n0[2 * c] = -u0 * n1 / nv;
+      R->cell_u_n0[2 * c + 1] = -u0 * n2 / nv;
+    } else if (t == 14) {
+      if (xc[0] >= 0.60) R->cell_u_n0[2 * c] = -124.824;
+    } else if (t == 0 || t == 11) {
+      R->cell_u_n0[2 * c] = 1.0;
+    }
   }
   /* initDensity */
   for (long c = 0; c < nc; ++c) {
@@ -271,6 +313,25 @@ static int init_state(port_run* R) {
     } else if (t == 1) {
       R->rho_n0[c] = 1.0;
       rm[0] = 1.0;
+    } else if (t == 14) {
+      /* Init.cc:528-560 */
+      rm[0] = 1.0;
+      R->rho_n0[c] = 1.0;
+      f[0] = 1.; f[1] = 0.; mf[0] = 1.; mf[1] = 0.;
+      const double r = sqrt((xc[0] - 0.320) * (xc[0] - 0.320) + (xc[1] - 0.04) * (xc[1] - 0.04));
+      if (r <= 0.025) {
+        rm[0] = 0.0; rm[1] = 0.182; R->rho_n0[c] = 0.182;
+        f[0] = 0.; f[1] = 1.; mf[0] = 0.; mf[1] = 1.;
+      }
+    } else if (t == 0 || t == 11) {
+      /* Init.cc:438-480 */
+      if (t == 0 || xc[0] <= 0.5) {
+        f[0] = 1.; f[1] = 0.; mf[0] = 1.; mf[1] = 0.;
+        R->rho_n0[c] = 1.0; rm[0] = 1.0; rm[1] = 0.;
+      } else {
+        f[0] = 0.; f[1] = 1.; mf[0] = 0.; mf[1] = 1.;
+        R->rho_n0[c] = 1.; rm[0] = 0.; rm[1] = 1.0;
+      }
     }
     if (R->nbmat == 1) {
       f[0] = 1.; f[1] = 0.; f[2] = 0.;
@@ -324,7 +385,14 @@ int port_euc_setup(port_run* R) {
   memcpy(R->e_n, R->e_n0, nc * sizeof(double));
   memcpy(R->em_n, R->em_n0, NM * nc * sizeof(double));
   const int t = R->s.test_case;
-  R->dt_init = (t == 2 || t == 13) ? 1.0e-5 : 1.0e-4;
+  if (t == 2 || t == 13)
+    R->dt_init = 1.0e-5;
+  else if (t == 14)
+    R->dt_init = 1.0e-7;
+  else if (t == 0 || t == 11)
+    R->dt_init = 0.0; /* no branch: the value-initialised deltat_n */
+  else
+    R->dt_init = 1.0e-4;
   R->dt_n = R->dt_init;
   return 0;
 }

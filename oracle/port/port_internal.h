@@ -44,6 +44,7 @@ struct port_run {
   int leftBC, rightBC, topBC, bottomBC;
   double leftV[2], rightV[2], topV[2], bottomV[2];
   int leftCellBC, rightCellBC, topCellBC, bottomCellBC;
+  int leftFluxBC, rightFluxBC, bottomFluxBC, topFluxBC; /* Cdl::*FluxBC */
 
   /* Euler geometry */
   double *X0, *Xc0, *Vpc0, *eulerV, *Xf, *fL, *fN, *nOut;

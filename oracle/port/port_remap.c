@@ -531,6 +531,39 @@ void port_remap_sweep(port_run* R, int sweep) {
       }
       for (int k = 0; k < NEQ; ++k) red[k] = red[k] + ffc[k];
     }
+    /* Remap::computeBoundaryFluxes (remap/BoundaryFluxes.cc:14-120): the
+     * flux through a boundary face with a flux condition, carrying the
+     * value of the cell's opposite face; branches in the reference's order
+     * (slots: 0 bottom, 1 left, 2 right, 3 top) */
+    if (R->leftFluxBC + R->rightFluxBC + R->bottomFluxBC + R->topFluxBC > 0) {
+      int fb = -1, fo = -1;
+      if (R->bottomFluxBC == 1 && c < R->nx && exy[1] == 1) {
+        fb = 0; fo = 3;
+      } else if (R->topFluxBC == 1 && c <= R->nx * (R->ny - 1) && c < R->nc && exy[1] == 1) {
+        fb = 3; fo = 0;
+      } else if (R->leftFluxBC == 1 && exy[0] == 1 && j == 0) {
+        fb = 1; fo = 2;
+      } else if (R->rightFluxBC == 1 && exy[0] == 1 && j == R->nx - 1) {
+        fb = 2; fo = 1;
+      }
+      if (fb >= 0) {
+        const long f = fs[fb], fo_ = fs[fo];
+        const double* n = R->fN + 2 * f;
+        const double* no = R->nOut + (4 * c + fb) * 2;
+        double bf[NEQ];
+        if (fabs(dot2(n, exy)) < 1.0E-10) {
+          for (int k = 0; k < NEQ; ++k) bf[k] = 0.0 * phiF[NEQ * fo_ + k];
+        } else {
+          double s;
+          if (pb == 0)
+            s = dot2(no, exy) * R->fnv[f] * R->fL[f] * dt;
+          else
+            s = dot2(no, exy) * R->fL[f];
+          for (int k = 0; k < NEQ; ++k) bf[k] = s * phiF[NEQ * fo_ + k];
+        }
+        for (int k = 0; k < NEQ; ++k) red[k] = red[k] + bf[k];
+      }
+    }
     double* U = Uout + NEQ * c;
     for (int k = 0; k < NEQ; ++k) U[k] = Uin[NEQ * c + k] - red[k];
     if (sweep == 1) {

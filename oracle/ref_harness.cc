@@ -13,7 +13,7 @@
 // reference is touched.
 //
 // usage: mahyco_dump DECK OUTDIR [--cycles N] [--vtk DIR] [--ext-mixed-row]
-//                    [--gamma g0,g1,g2] [--cfl C]
+//                    [--gamma g0,g1,g2] [--cfl C] [--init-only]
 //   --cycles N       stop after N cycles (GestTemps::max_time_iterations=N+1,
 //                    the loop test at VnrRemap.cc:194-195)
 //   --vtk DIR        let the reference write its own VTK output under DIR
@@ -22,6 +22,9 @@
 //   --ext-mixed-row  bi-material Sod: make the first cell row/column past
 //                    the interface a 50/50 mixed cell (extension used by the
 //                    2048^2 bi-material workload; same rule as the GPU build)
+//   --init-only      dump the state the time loop would start from (after
+//                    setUpTimeLoopN) instead of running it: pins the initial
+//                    state of cases whose first cycle stops the reference
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -44,6 +47,7 @@ struct Args {
   bool mixed_row = false;
   std::vector<double> gamma;
   double cfl = -1.0;
+  bool init_only = false;
 };
 
 void dump_raw(const std::string& dir, const std::string& name,
@@ -133,6 +137,8 @@ Args parse(int argc, char** argv) {
       a.cycles = std::atol(argv[++i]);
     } else if (k == "--vtk" && i + 1 < argc) {
       a.vtk = argv[++i];
+    } else if (k == "--init-only") {
+      a.init_only = true;
     } else if (k == "--ext-mixed-row") {
       a.mixed_row = true;
     } else if (k == "--cfl" && i + 1 < argc) {
@@ -209,6 +215,26 @@ int main(int argc, char** argv) {
     if (o->sansLagrange == 0) c->initPseudo();
     c->setUpTimeLoopN();
     c->computeNodeMass();
+    if (a.init_only) {
+      // the state the time loop starts from (after setUpTimeLoopN's copies)
+      dump_scalar(od, "density", c->m_density_n, nc);
+      dump_scalar(od, "pressure", c->m_pressure_n, nc);
+      dump_scalar(od, "energy", c->m_internal_energy_n, nc);
+      dump_scalar(od, "sound_speed", c->m_speed_velocity_n, nc);
+      dump_scalar(od, "pseudo", c->m_pseudo_viscosity_n, nc);
+      dump_scalar(od, "divu", c->m_divu_n, nc);
+      dump_scalar(od, "cell_mass", c->m_cell_mass, nc);
+      dump_vec(od, "density_env", c->m_density_env_n, nc, 3);
+      dump_vec(od, "energy_env", c->m_internal_energy_env_n, nc, 3);
+      dump_vec(od, "pressure_env", c->m_pressure_env_n, nc, 3);
+      dump_vec(od, "fracvol_env", c->m_fracvol_env, nc, 3);
+      dump_vec(od, "mass_fraction_env", c->m_mass_fraction_env, nc, 3);
+      dump_vec(od, "node_velocity", c->m_node_velocity_n, nn, 2);
+      dump_scalar(od, "node_mass", c->m_node_mass, nn);
+      write_meta(od, "VNR", nx, ny, o->nbmat, 0, gt->t_n, gt->deltat_n);
+      Kokkos::finalize();
+      return 0;
+    }
     c->executeTimeLoopN();
     // The last cycle does not swap (VnrRemap.cc:198): final state is _nplus1.
     dump_scalar(od, "density", c->m_density_nplus1, nc);
@@ -239,6 +265,19 @@ int main(int argc, char** argv) {
     c->initDensity();
     c->initMeshGeometryForFaces();
     c->setUpTimeLoopN();
+    if (a.init_only) {
+      dump_scalar(od, "density", c->m_density_n, nc);
+      dump_scalar(od, "energy", c->m_internal_energy_n, nc);
+      dump_vec(od, "cell_velocity", c->m_cell_velocity_n, nc, 2);
+      dump_vec(od, "density_env", c->m_density_env_n, nc, 3);
+      dump_vec(od, "energy_env", c->m_internal_energy_env_n, nc, 3);
+      dump_vec(od, "fracvol_env", c->m_fracvol_env, nc, 3);
+      dump_vec(od, "mass_fraction_env", c->m_mass_fraction_env, nc, 3);
+      dump_vec(od, "node_velocity", c->m_node_velocity_n, nn, 2);
+      write_meta(od, "Eucclhyd", nx, ny, o->nbmat, 0, gt->t_n, gt->deltat_n);
+      Kokkos::finalize();
+      return 0;
+    }
     c->executeTimeLoopN();
     dump_scalar(od, "density", c->m_density_nplus1, nc);
     dump_scalar(od, "pressure", c->m_pressure, nc);

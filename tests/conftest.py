@@ -48,6 +48,34 @@ EUC_FIELDS = ["density", "pressure", "energy", "sound_speed", "cell_velocity",
               "node_velocity"]
 
 
+# fields of an initial-state fixture (harness --init-only): a Eucclhyd run's
+# pressure and sound speed are first formed by its first cycle
+EUC_INIT_FIELDS = ["density", "energy", "cell_velocity", "density_env", "energy_env",
+                   "fracvol_env", "mass_fraction_env", "node_velocity"]
+# error word bit of the way the reference stops in the first cycle
+STOP_BITS = {"nan": 1, "energy": 2, "dt": 4}
+
+
+def init_only(meta) -> bool:
+    """An initial-state fixture: the reference stops in the first cycle."""
+    return meta.get("init_only") == "1"
+
+
+def init_fields_of(spec):
+    return EUC_INIT_FIELDS if spec.scheme == 2000 else CELL_FIELDS + NODE_FIELDS + ["node_mass"]
+
+
+def check_first_cycle_stop(run, meta):
+    """The run, stepped from its initial state, stops in the first cycle
+    with the error the reference stops on (and at the cell it names)."""
+    done = run.step(3)
+    code, cell = run.error()
+    assert done and (code & STOP_BITS[meta["reference_stop"]]), (code, meta["reference_stop"])
+    if int(meta["reference_stop_cell"]) >= 0:
+        assert cell == int(meta["reference_stop_cell"]), (cell, meta["reference_stop_cell"])
+    assert run.time()[2] <= 1
+
+
 def fields_of(spec):
     """Fields a fixture of this scheme holds (all compared bit for bit)."""
     if spec.scheme == 2000:  # Eucclhyd

@@ -40,6 +40,10 @@ DUMP = ROOT / "oracle" / "_ref" / "mahyco_dump"
 FIELDS = ["density", "pressure", "energy", "sound_speed", "pseudo", "divu",
           "cell_mass", "density_env", "energy_env", "pressure_env",
           "fracvol_env", "mass_fraction_env", "node_velocity", "node_mass"]
+# what the harness dumps of a Eucclhyd run's initial state (--init-only: the
+# pressure and sound speed are first formed by the first cycle)
+FIELDS_EUC_INIT = ["density", "energy", "cell_velocity", "density_env", "energy_env",
+                   "fracvol_env", "mass_fraction_env", "node_velocity"]
 # what the harness dumps for a Eucclhyd run (the cell-centred velocity, the
 # pressure and sound speed of the last cycle's start)
 FIELDS_EUC = ["density", "pressure", "energy", "sound_speed", "cell_velocity",
@@ -125,6 +129,71 @@ def main() -> None:
     s.max_cycles = 1
     cases.append(("POINT_TRIPLE_o3_pb_mixte_1cycle", s, tmp / "tp_o3_pb.txt",
                   ("--cycles", "1")))
+    # conservative projection (projectionConservative = oui, Eucclhyd): the
+    # kinetic energy is remapped and corrects the internal energy
+    # (eucclhyd_remap/PhaseRemapFinal.cc:115); no deck of the reference's
+    # suite switches it on
+    for src_case, name in (("SOD_X_bi_mat_Superbee_PenteBorne_pure", "SOD_X_bi_mat_Superbee_PB_pure_conservative"),
+                           ("SOD_Y_bi_mat_MinMod_simple", "SOD_Y_bi_mat_MinMod_conservative"),
+                           ("POINT_TRIPLE_SuperBee_PenteBorne_mixte", "POINT_TRIPLE_SuperBee_PB_mixte_conservative")):
+        s = M.parse_deck(tests / src_case / "donnees.txt")
+        s.projection_conservative = 1
+        write_deck(s, tmp / f"{name}.txt")
+        cases.append((name, s, tmp / f"{name}.txt", ()))
+    # shock on a helium bubble (BiShockBubble, Eucclhyd): the gas enters
+    # through the right side at the imposed velocity and the remap takes that
+    # side's boundary flux (remap/BoundaryFluxes.cc), the one reference case
+    # that switches computeBoundaryFluxes on; a 130x16 mesh of the
+    # reference's 0.00125 deck at 0.005, exponents 1.4 / 1.667
+    base = M.parse_deck(tests / "POINT_TRIPLE_MinMod_simple" / "donnees.txt")
+    for lim, pb, order, cyc, tag in (("minmod", 0, 2, 120, "MinMod_o2"),
+                                     ("superBee", 1, 2, 120, "SuperBee_PenteBorne_pure"),
+                                     ("superBee", 0, 3, 60, "SuperBee_o3")):
+        s = base.copy()
+        s.test_case, s.nbmat = 14, 2
+        s.nx, s.ny, s.dx, s.dy = 130, 16, 0.005, 0.005
+        s.final_time, s.output_time = 1.0, 1.0
+        s.gamma[0], s.gamma[1] = 1.4, 1.667
+        s.limiter, s.pb, s.pb_mixte, s.pb_complet = M.LIMITERS[lim], pb, 0, 0
+        s.projection_order = order
+        s.max_cycles = cyc
+        name = f"SHOCK_BUBBLE_{tag}"
+        write_deck(s, tmp / f"{name}.txt")
+        cases.append((name, s, tmp / f"{name}.txt",
+                      ("--cycles", str(cyc), "--gamma", "1.4,1.667,1.4")))
+    # Cases whose first cycle stops the reference: Noh and bi-material Noh
+    # (no density initialisation: NaN in the remap final, "cell--Nan 0"),
+    # the Eucclhyd unit tests (deltat_n stays 0: "pas de temps minimum") and
+    # the VNR unit tests (e = 25 > 5: the energy abort).  Their initial state
+    # is pinned (--init-only) and the stop is recorded beside it.
+    init_cases = []
+    base_e = M.parse_deck(tests / "SOD_X_Mono_mat_MinMod_simple" / "donnees.txt")
+    base_v = M.parse_deck(tests / "SOD_X_Mono_mat_Minmod_vnr_o2" / "donnees.txt")
+    # (stop, cell): what the reference prints when it stops in the first
+    # cycle ("cell--Nan 0", "Fin de la simulation par pas de temps minimum",
+    # "16 energie 25 ...")
+    for name, base, tc, nb, nx, ny, stop in (
+            ("NOH_euc_init", base_e, 6, 1, 40, 40, ("nan", 0)),
+            ("BINOH_euc_init", base_e, 17, 2, 40, 40, ("nan", 0)),
+            ("UNIT_euc_init", base_e, 0, 1, 40, 10, ("dt", -1)),
+            ("BIUNIT_euc_init", base_e, 11, 2, 40, 10, ("dt", -1)),
+            ("UNIT_vnr_init", base_v, 0, 1, 40, 10, ("energy", 16)),
+            ("BIUNIT_vnr_init", base_v, 11, 2, 40, 10, ("energy", 16))):
+        s = base.copy()
+        s.test_case, s.nbmat, s.nx, s.ny = tc, nb, nx, ny
+        s.dx, s.dy = 1.0 / nx, (1.0 / ny if ny == nx else 0.1)
+        s.max_cycles = 0
+        write_deck(s, tmp / f"{name}.txt")
+        init_cases.append((name, s, tmp / f"{name}.txt", stop))
+    for name, spec, deck, stop in init_cases:
+        if a.only and a.only not in name:
+            continue
+        euc = spec.scheme == M.SCHEME_EUCCLHYD
+        meta, fields = run_reference(deck, 0, ("--init-only",),
+                                     FIELDS_EUC_INIT if euc else FIELDS)
+        meta["init_only"] = "1"
+        meta["reference_stop"], meta["reference_stop_cell"] = stop[0], str(stop[1])
+        save(name, spec, meta, fields)
     for name, spec, deck, extra in cases:
         if a.only and a.only not in name:
             continue

@@ -12,7 +12,8 @@ import numpy as np
 import pytest
 
 from conftest import (CELL_FIELDS, GOLDEN, NODE_FIELDS, assert_bitwise,
-                      fields_of, get_field, golden_cases, load_golden)
+                      check_first_cycle_stop, fields_of, get_field, golden_cases,
+                      init_fields_of, init_only, load_golden)
 
 pytestmark = pytest.mark.gpu
 
@@ -34,6 +35,14 @@ def ctx(M):
 def test_gpu_matches_reference(case, M, ctx):
     spec, meta, want = load_golden(GOLDEN / f"{case}.npz")
     run = M.Run(spec, ctx)
+    if init_only(meta):
+        # the reference stops in the first cycle: its initial state, then
+        # the same stop through the error word
+        assert run.time() == (0.0, float(meta["dt"]), 0)
+        for f in init_fields_of(spec):
+            assert_bitwise(f"{case}:{f}", get_field(run, f, spec.nbmat), want[f])
+        check_first_cycle_stop(run, meta)
+        return
     run.simulate(chunk=256)
     t, dt, n = run.time()
     assert n == int(meta["cycles"])
@@ -265,3 +274,47 @@ def test_gpu_triple_point_conservation(M, ctx, port_lib):
     assert t1 == euc_totals(ref, spec)
     assert abs(t1["mass"] - t0["mass"]) <= 1e-4 * t0["mass"]
     assert abs(t1["energy"] - t0["energy"]) <= 1e-3 * t0["energy"]
+
+
+@pytest.mark.parametrize("case", ["UNIT_vnr_init", "BIUNIT_vnr_init"])
+def test_gpu_left_flux_boundary_matches_port(case, M, ctx, port_lib):
+    """The VNR unit tests, whose remap takes a flux through the left side
+    (remap/BoundaryFluxes.cc, leftFluxBC of vnr_remap/Init.cc:65-93), run
+    for 300 cycles with the |e| > 5 abort switched off (energy_limit 0: the
+    reference stops on it in the first cycle, which the golden test pins):
+    bit-identical to the C restatement, the inflow visible in the mass."""
+    spec, _, _ = load_golden(GOLDEN / f"{case}.npz")
+    spec.energy_limit = 0.0
+    spec.max_cycles = 300
+    spec.final_time = 10.0
+    g = M.Run(spec, ctx)
+    m0 = math.fsum(g.fetch("density")) * spec.dx * spec.dy
+    g.simulate()
+    c = port_lib.PortRun(spec)
+    c.simulate()
+    assert g.time() == c.time() and g.time()[2] == 300
+    assert g.error() == c.error()
+    for f in CELL_FIELDS + NODE_FIELDS + ["node_mass"]:
+        assert_bitwise(f"{case}:{f}", get_field(g, f, spec.nbmat), get_field(c, f, spec.nbmat))
+    m1 = math.fsum(g.fetch("density")) * spec.dx * spec.dy
+    assert m1 != m0
+
+
+@pytest.mark.parametrize("order,pb", [(2, 0), (2, 1), (3, 0)])
+def test_gpu_shock_bubble_larger_matches_port(order, pb, M, ctx, port_lib):
+    """The shock on a helium bubble on the reference deck's own 520x64 mesh
+    (0.00125 spacing), 150 cycles: the right side's inflow through the
+    remap's boundary flux, bit-identical to the C restatement."""
+    spec, _, _ = load_golden(GOLDEN / "SHOCK_BUBBLE_MinMod_o2.npz")
+    spec.nx, spec.ny, spec.dx, spec.dy = 520, 64, 0.00125, 0.00125
+    spec.projection_order, spec.pb = order, pb
+    spec.limiter = M.LIMITERS["superBee"]
+    spec.max_cycles = 150
+    g = M.Run(spec, ctx)
+    g.simulate()
+    c = port_lib.PortRun(spec)
+    c.simulate()
+    assert g.time() == c.time()
+    assert g.error() == c.error()
+    for f in fields_of(spec):
+        assert_bitwise(f, get_field(g, f, spec.nbmat), get_field(c, f, spec.nbmat))
