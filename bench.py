@@ -93,16 +93,29 @@ def workload_config(K: int, W: int, n: int = 2048) -> dict:
 
 
 # Algorithmic (compulsory) bytes per unit of each kernel: every input plane
-# read once, every output plane written once; units are cells or nodes.
+# read once, every output plane written once; units are cells or nodes (a
+# face counts as a cell); nc live remap components, nb materials.
 def algorithmic_bytes(kind: str, nb: int, pb: bool) -> int:
     nc = 3 * nb + 1
     d = 8
     table = {
-        "k_lag_nodes": 18,                       # u, cell mass, p, q, cqs / u, XL, m
+        # u, cell mass, p, q, corner normals / u, Lagrange position, node mass
+        "k_lag_nodes": 18,
+        # state planes in / Lagrange state, remap inputs (U, Phi), geometry out
         "k_lag_cells": (7 + 7 * nb) + (8 + nb + 2 * nc),
-        "k_sweep_grad": (nc + 3 + (4 if pb else 0)) + (2 * nc if pb else nc),
+        # without PenteBorne: Phi, centroid in / nc face gradients out
+        "k_face_grad": (nc + 1) + nc,
+        # PenteBorne: Phi, centroid, width, 2 node velocities, 2 outer
+        # normals in / the two plateau-slope integrals out; otherwise Phi,
+        # nc face gradients, centroid, width, 2 node velocities in / nc
+        # face values out
+        "k_sweep_grad": (nc + 6) + 2 * nc if pb else (2 * nc + 4) + nc,
+        # order 1 / order 3 face values
         "k_sweep_face": (2 * nc if pb else 2 * nc + 2) + nc,
-        "k_sweep_update": (2 * nc + 5) + (nc + 2 * nb) + (nc + 1) // 2,
+        # U, the two integrals (PenteBorne) or the face values, 2 node
+        # velocities, 2 outer normals in / U, the nodal mass-flux shares,
+        # Phi and the flags in the first sweep (half of the launches) out
+        "k_sweep_update": ((3 * nc + 4) if pb else (2 * nc + 5)) + (nc + nb) + (nc + 1) // 2,
         "k_dual_grad": 5,
         "k_dual_update": (2 * nb + 2 + 8) + 5,
         "k_final": (nc + 2) + (6 + 7 * nb + 1),

@@ -1932,16 +1932,16 @@ __device__ __forceinline__ void batch_items(const BatchArgs& b, const F& f) {
   }
 }
 
-__global__ void __launch_bounds__(kBatchThreads) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_final(BatchArgs b) { batch_items(b, Final{}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
+__global__ void __launch_bounds__(kBatchThreads, 5) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 5) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 6) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 4) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 6) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 5) kb_final(BatchArgs b) { batch_items(b, Final{}); }
 
 // One thread per run: cycle start (begin + reduction reset) and cycle end.
 __global__ void kb_begin(const RunView* views, const int* ninst) {
