@@ -531,7 +531,7 @@ def roofline_of(M, kinds: dict, spec, regime: str, local: int) -> dict:
         pj = json.loads(prof_file.read_text())
         table = pj.get(regime, {})
         table = table.get("kernels", table)
-        kp = table.get(dom) or table.get(dom + "_pb", {})
+        kp = table.get(dom) or table.get(dom + "_pb") or table.get(dom + "_f", {})
         if "dram_bytes_per_unit" in kp:
             traffic = kp["dram_bytes_per_unit"] * units
         if "fp64_flops_per_unit" in kp:
@@ -569,7 +569,7 @@ def path_traffic(kinds: dict, spec, regime: str, ms_per_cycle: float) -> dict | 
     cycles = max(v[1] for k, v in kinds.items() if k in ("k_lag_cells", "k_final"))
     per_cell = 0.0
     for k, (ms, cnt) in kinds.items():
-        kp = table.get(k) or table.get(k + "_pb")
+        kp = table.get(k) or table.get(k + "_pb") or table.get(k + "_f")
         if not kp:
             continue
         units = nodes if k in ("k_lag_nodes", "k_dual_grad", "k_dual_update") else cells

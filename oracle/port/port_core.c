@@ -1208,6 +1208,7 @@ static void vnr_cycle(port_run* R) {
     vnr_eos_and_mean(R);
   }
   int cont = (R->n + 1 < R->max_iter && R->t_np1 < R->s.final_time);
+  R->swapped = cont;
   if (cont) {
     int tmp = R->x_then_y_np1;
     R->x_then_y_np1 = R->x_then_y_n;
@@ -1366,9 +1367,12 @@ int port_step(port_run* R, int ncycles, int* done) {
 }
 
 int port_time(port_run* R, double* t, double* dt, long* cycle) {
-  /* after the last cycle the reference does not swap: report t_{n+1} */
-  if (t) *t = R->done ? R->t_np1 : R->t_n;
-  if (dt) *dt = R->done ? R->dt_np1 : R->dt_n;
+  /* after the last cycle the reference does not swap: report t_{n+1}; a
+   * VNR run stopped by an error after a cycle that swapped reports the
+   * time it reached (the reference exits inside that cycle) */
+  const int cur = !R->done || R->swapped;
+  if (t) *t = cur ? R->t_n : R->t_np1;
+  if (dt) *dt = cur ? R->dt_n : R->dt_np1;
   if (cycle) *cycle = R->n;
   return 0;
 }

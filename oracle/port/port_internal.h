@@ -94,6 +94,7 @@ struct port_run {
   long n;
   double t_n, t_np1, dt_n, dt_np1, dt_init;
   int done;
+  int swapped; /* the last VNR cycle swapped n and n+1 (it was not the last) */
   unsigned err;
   long err_cell;
 };
