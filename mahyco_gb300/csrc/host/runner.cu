@@ -82,6 +82,8 @@ size_t layout(RunView& v, char* base) {
   v.gP = a.take<double>(nc * P);
   v.dPAv = a.take<double>(nc * P);
   v.dPAr = a.take<double>(nc * P);
+  v.pbz = a.take<unsigned char>(P);
+  v.u1s = a.take<unsigned char>(P);
   v.DPF = a.take<double>(nb * P);
   // face gradients of runs without PenteBorne (the slope kernel reads them
   // while it writes face values into phiF): the plateau-slope integral

@@ -94,8 +94,12 @@ struct RunView {
   double* UL;         // ncomp planes (also receives the second sweep)
   double* Phi;        // ncomp planes
   double* U1;         // ncomp planes
+  unsigned char* u1s; // per cell (orders 1-2): the first sweep left every
+                      // component unchanged and did not store U1
   double* gP;         // ncomp planes (limited gradients)
   double *dPAv, *dPAr;  // ncomp planes (plateau-slope swept integrals)
+  unsigned char* pbz;   // per cell: bit 0 / bit 1 set where every dPAr /
+                        // dPAv component is +0.0 and was not stored
   double* DPF;        // nbmat planes (plateau-slope dual mass flux)
   double* phiF;       // ncomp face planes
   double* phiG;       // ncomp face planes of face gradients (runs without

@@ -702,10 +702,7 @@ struct SweepGradT {
         const unsigned long long z = ubits(v.u[o + n0]) | ubits(v.u[o + n0 + 1]) |
                                      ubits(v.u[o + n0 + v.nx + 1]) | ubits(v.u[o + n0 + v.nx + 2]);
         if ((z & kMag) == 0 && is_finite(C.dt_n)) {
-          for (int k = 0; k < ncomp; ++k) {
-            v.dPAr[k * P + c] = 0.0;
-            v.dPAv[k * P + c] = 0.0;
-          }
+          v.pbz[c] = 3;  // both integral planes all +0.0, not stored
           if (cfd) {
             const double fl = dirx ? half(ld(v.flv, i) + ld(v.flv, i)) : half(ld(v.flh, j) + ld(v.flh, j));
             const double zf = 0.0 * fl;
@@ -737,10 +734,7 @@ struct SweepGradT {
       // half-faces: every flux stored below is then exactly 0 (0 * flen for
       // the dual one) whatever the slopes, so they are not formed
       if (iszero(ppa) && iszero(ppb) && (!cfd || iszero(ppd))) {
-        for (int k = 0; k < ncomp; ++k) {
-          v.dPAr[k * P + c] = 0.0;
-          v.dPAv[k * P + c] = 0.0;
-        }
+        v.pbz[c] = 3;
         if (cfd) {
           const double z = 0.0 * flen;
           for (int m = 0; m < nb; ++m) v.DPF[m * P + c] = z;
@@ -894,10 +888,13 @@ struct SweepGradT {
           else
             F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
         }
-        for (int k = 0; k < ncomp; ++k) out[k * P] = iszero(ppv) ? 0.0 : F[k];
+        for (int k = 0; k < ncomp; ++k) out[k * P] = F[k];
       };
-      finish(Fr, ppa, v.dPAr + c);
-      finish(Fv, ppb, v.dPAv + c);
+      // a zero swept length makes every integral of that side exactly +0.0:
+      // recorded in pbz instead of stored (bit 0: dPAr, bit 1: dPAv)
+      v.pbz[c] = (iszero(ppa) ? 1 : 0) | (iszero(ppb) ? 2 : 0);
+      if (!iszero(ppa)) finish(Fr, ppa, v.dPAr + c);
+      if (!iszero(ppb)) finish(Fv, ppb, v.dPAv + c);
     }
   }
 };
@@ -1064,21 +1061,9 @@ struct SweepFaceT {
           for (int t = 0; t < 4; ++t)
             if (k0 + t < ncomp) out[(k0 + t) * FP] = a[t] + s * g[t];
         }
-      } else {
-        const long long av = dirx ? cb : cf, ar = dirx ? cf : cb;
-        for (int k0 = 0; k0 < ncomp; k0 += 4) {
-          double a[4], b[4];
-  #pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            const int k = k0 + t;
-            a[t] = (k < ncomp) ? v.dPAv[k * P + av] : 0.;
-            b[t] = (k < ncomp) ? v.dPAr[k * P + ar] : 0.;
-          }
-  #pragma unroll
-          for (int t = 0; t < 4; ++t)
-            if (k0 + t < ncomp) out[(k0 + t) * FP] = a[t] - b[t];
-        }
       }
+      // (with PenteBorne the update forms the face values of orders 1-2 from
+      // the integral planes and their zero flags: nothing to store here)
     } else {
       // order 3: six cells along the sweep, "minus" side first, clamped
       long long cs[6];
@@ -1164,16 +1149,27 @@ struct SweepFaceT {
 // while it rewrites Phi.
 struct LowFace {
   long long av, ar;
+  bool zv, zr;  // dPAv(av) / dPAr(ar) all +0.0 (pbz)
 };
-DV LowFace low_face(bool dirx, long long cb, long long cf) {
+DV LowFace low_face(const RunView& v, bool dirx, long long cb, long long cf) {
   LowFace F;
   F.av = dirx ? cb : cf;
   F.ar = dirx ? cf : cb;
+  F.zv = (v.pbz[F.av] & 2) != 0;
+  F.zr = (v.pbz[F.ar] & 1) != 0;
   return F;
 }
 DV double low_face_value(const RunView& v, const LowFace& F, int k) {
   const long long P = v.pitch;
-  return v.dPAv[k * P + F.av] - v.dPAr[k * P + F.ar];
+  // an integral plane flagged in pbz holds +0.0 for every component (the
+  // slope kernel did not store it); subz: a - b exactly, on the integer pipe
+  // when b (or both) is a zero -- the usual case, as only the face's upwind
+  // cell integrates an outflow, and everywhere at rest (each face value is
+  // formed twice here, so its subtraction should not cost two FP64
+  // instructions)
+  const double a = F.zv ? 0.0 : v.dPAv[k * P + F.av];
+  const double b = F.zr ? 0.0 : v.dPAr[k * P + F.ar];
+  return subz(a, b);
 }
 
 // Conservative update of one sweep (Remap::computeUremap{1,2},
@@ -1192,8 +1188,15 @@ struct SweepUpdateT {
     const long long P = v.pitch, FP = v.fpitch;
     const long long c = (long long)i * v.nx + j;
     const int ncomp = v.ncomp, nb = v.nbmat;
-    const double* Uin = (sweep == 1) ? v.UL : v.U1;
-    double* Uout = (sweep == 1) ? v.U1 : v.UL;
+    // Orders 1-2: a cell whose components all come through the first sweep
+    // bit for bit unchanged is flagged in u1s instead of having them copied
+    // into U1; the second sweep then takes its input from UL (which holds
+    // them) and, if it leaves them unchanged too, stores nothing (UL already
+    // holds the result).  The order-3 reconstruction reads neighbours' U1,
+    // so order-3 runs store U1 always.
+    const bool lowo = v.order <= 2;
+    const bool from_ul = (sweep == 2) && lowo && v.u1s[c] != 0;
+    const double* Uin = (sweep == 1 || from_ul) ? v.UL : v.U1;
     const double dt = C.dt_n;
     // the two faces perpendicular to the sweep, in getNeighbourCells order
     // (below before above, left before right); faces parallel to the sweep
@@ -1246,11 +1249,11 @@ struct SweepUpdateT {
     LowFace lf[2];
     if (form) {
       if (dirx) {
-        lf[0] = low_face(true, c - 1, c);
-        lf[1] = low_face(true, c, c + 1);
+        if (has[0]) lf[0] = low_face(v, true, c - 1, c);
+        if (has[1]) lf[1] = low_face(v, true, c, c + 1);
       } else {
-        lf[0] = low_face(false, c, c - v.nx);
-        lf[1] = low_face(false, c + v.nx, c);
+        if (has[0]) lf[0] = low_face(v, false, c, c - v.nx);
+        if (has[1]) lf[1] = low_face(v, false, c + v.nx, c);
       }
     }
     // Boundary flux (Remap::computeBoundaryFluxes, remap/BoundaryFluxes.cc
@@ -1308,7 +1311,6 @@ struct SweepUpdateT {
           const int k = k0 + t;
           if (k >= ncomp) break;
           U[k] = ui[t];
-          Uout[k * P + c] = ui[t];
           if (dual_share && k >= doff && k < doff + nb) {
             // the signed-zero fluxes times the normals, summed: -0 only when
             // both terms are -0
@@ -1349,7 +1351,6 @@ struct SweepUpdateT {
           U[k] = uin - red;
         }
         same = same && ubits(U[k]) == ubits(uin);
-        Uout[k * P + c] = U[k];
         if (dual_share && k >= doff && k < doff + nb) {
           // the cell's share of the nodal mass flux (UtilesDualRemap.cc A1
           // :10-233, A2 :401-644): the two face fluxes times their outer
@@ -1361,6 +1362,14 @@ struct SweepUpdateT {
           v.FFd[(k - doff) * P + c] = w;
         }
       }
+    }
+    // the stores, after every load
+    if (sweep == 1) {
+      if (lowo) v.u1s[c] = same ? 1 : 0;
+      if (!(lowo && same))
+        for (int k = 0; k < ncomp; ++k) v.U1[k * P + c] = U[k];
+    } else if (!(from_ul && same)) {
+      for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
     }
     if (sweep == 1) {
       double* Phi = v.Phi;
@@ -1932,16 +1941,16 @@ __device__ __forceinline__ void batch_items(const BatchArgs& b, const F& f) {
   }
 }
 
-__global__ void __launch_bounds__(kBatchThreads, 8) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
-__global__ void __launch_bounds__(kBatchThreads, 5) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
-__global__ void __launch_bounds__(kBatchThreads, 8) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 5) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 6) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 4) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 6) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 8) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 8) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 5) kb_final(BatchArgs b) { batch_items(b, Final{}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_final(BatchArgs b) { batch_items(b, Final{}); }
 
 // One thread per run: cycle start (begin + reduction reset) and cycle end.
 __global__ void kb_begin(const RunView* views, const int* ninst) {

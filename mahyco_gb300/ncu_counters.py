@@ -52,7 +52,8 @@ def read_capture(path: str) -> dict[str, list[dict]]:
         metric = row["Metric Name"]
         # times to microseconds, bytes to bytes
         if metric == "gpu__time_duration.sum":
-            val = val / 1e3 if unit == "nsecond" else val * (1e3 if unit == "msecond" else 1.0)
+            val *= {"ns": 1e-3, "nsecond": 1e-3, "us": 1.0, "usecond": 1.0,
+                    "ms": 1e3, "msecond": 1e3, "s": 1e6, "second": 1e6}.get(unit, 1.0)
         elif metric.startswith("dram__bytes"):
             scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3,
                      "MB": 1e6, "GB": 1e9}.get(unit, 1)
