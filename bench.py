@@ -92,10 +92,15 @@ def workload_config(K: int, W: int, n: int = 2048) -> dict:
     }
 
 
-# Algorithmic (compulsory) bytes per unit of each kernel: every input plane
-# read once, every output plane written once; units are cells or nodes (a
-# face counts as a cell); nc live remap components, nb materials.
-def algorithmic_bytes(kind: str, nb: int, pb: bool) -> int:
+# Algorithmic (compulsory) bytes per unit of each kernel: every plane it
+# must read read once, every plane it must write written once; units are
+# cells or nodes (a face counts as a cell); nc live remap components, nb
+# materials.  `rest`: the benchmark's regime, where almost every cell is at
+# rest: the slope kernel only records that a cell's plateau-slope integrals
+# are zeros (one flag byte) and the update reads the flags instead of those
+# planes and stores only the components a sweep changed, so what such a cell
+# must move is counted; otherwise (a developed flow) every plane.
+def algorithmic_bytes(kind: str, nb: int, pb: bool, rest: bool = False) -> int:
     nc = 3 * nb + 1
     d = 8
     table = {
@@ -120,7 +125,13 @@ def algorithmic_bytes(kind: str, nb: int, pb: bool) -> int:
         "k_dual_update": (2 * nb + 2 + 8) + 5,
         "k_final": (nc + 2) + (6 + 7 * nb + 1),
     }
-    return table.get(kind, 0) * d
+    if rest and pb:
+        # a cell at rest: the node velocity along the sweep in / its flag
+        # byte out; U, 2 node velocities, 2 outer normals and the flag bytes
+        # in / the mass-flux shares (and a flag byte) out
+        table["k_sweep_grad"] = 1.25
+        table["k_sweep_update"] = (nc + 4.25) + (nb + 0.125)
+    return int(table.get(kind, 0) * d)
 
 
 def load_peaks() -> dict:
@@ -520,7 +531,7 @@ def roofline_of(M, kinds: dict, spec, regime: str, local: int) -> dict:
     per_launch_ms = dom_ms / dom_n
     node_kernel = dom in ("k_lag_nodes", "k_dual_grad", "k_dual_update")
     units = (n + 1) * (spec.ny + 1) if node_kernel else cells
-    alg = algorithmic_bytes(dom, spec.nbmat, bool(spec.pb)) * units
+    alg = algorithmic_bytes(dom, spec.nbmat, bool(spec.pb), rest=(regime == "kernels")) * units
     achieved = alg / (per_launch_ms * 1e-3) / 1e9
     peaks = load_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))

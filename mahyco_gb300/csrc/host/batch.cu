@@ -253,6 +253,8 @@ int get_plan(hydro_ctx* ctx, hydro_run* const* runs, int n, BatchPlan** out) {
     if (runs[r]->ctx != ctx) return fail(-2, "batch: run belongs to another context");
     if (runs[r]->v.scheme != HYDRO_SCHEME_VNR)
       return fail(-4, "batch: the batched form advances VNR runs");
+    if (runs[r]->v.projection != 1)
+      return fail(-5, "batch: the batched form advances runs with the remap");
   }
   if (!ctx->plan) {
     auto* p = new BatchPlan();

@@ -70,6 +70,7 @@ size_t layout(RunView& v, char* base) {
   v.u = a.take<double>(2 * NP);
   v.node_mass = a.take<double>(NP);
   v.speed = a.take<double>(NP);
+  v.XN = (v.projection == 0) ? a.take<double>(2 * NP) : nullptr;
   v.XL = a.take<double>(2 * NP);
   v.vL = a.take<double>(P);
   v.rL = a.take<double>(P);
@@ -142,8 +143,10 @@ size_t layout(RunView& v, char* base) {
 int validate(const hydro_spec& s) {
   if (s.scheme != HYDRO_SCHEME_VNR && s.scheme != HYDRO_SCHEME_EUCCLHYD)
     return fail(-20, "unknown Lagrange scheme");
-  if (s.projection != 1)
-    return fail(-21, "the GPU path requires the remap (AvecProjection = oui)");
+  if (s.projection != 1 &&
+      !(s.projection == 0 && s.scheme == HYDRO_SCHEME_VNR && s.sans_lagrange == 0))
+    return fail(-21, "without the remap (AvecProjection = non) the GPU path runs the "
+                     "VNR scheme with its Lagrange phase only");
   if (s.nbmat < 1 || s.nbmat > 3) return fail(-22, "nbmat must be 1..3");
   if (s.projection_order < 1 || s.projection_order > 3)
     return fail(-23, "projection order must be 1, 2 or 3");
@@ -635,6 +638,7 @@ size_t hydro_run_field_size(hydro_run* r, const char* f) {
   for (auto n : cell3)
     if (!strcmp(f, n)) return 3 * nc;
   if (!strcmp(f, "node_velocity")) return 2 * nn;
+  if (!strcmp(f, "node_coord")) return 2 * nn;
   if (dump_plane(r, f) >= 0) return dump_on_nodes(r, f) ? nn : nc;
   if (r->v.scheme == HYDRO_SCHEME_EUCCLHYD) {
     if (!strcmp(f, "cell_velocity")) return 2 * nc;
@@ -692,6 +696,25 @@ int hydro_run_fetch(hydro_run* r, const char* f, double* dst, size_t n) {
     for (long long c = 0; c < nc; ++c)
       for (int m = 0; m < 3; ++m)
         dst[3 * c + m] = m < v.nbmat ? tmp[m * v.pitch + c] : 0.0;
+    return 0;
+  }
+  if (!strcmp(f, "node_coord")) {
+    // the mesh the next output shows: the moving positions of a run without
+    // the remap, the Euler mesh (dx * j, dy * i) otherwise
+    if (!v.XN) {
+      for (long long p = 0; p < nn; ++p) {
+        const long long i = p / (v.nx + 1), j = p - i * (v.nx + 1);
+        dst[2 * p] = v.dx * (double)j;
+        dst[2 * p + 1] = v.dy * (double)i;
+      }
+      return 0;
+    }
+    CUDA_TRY(get(v.XN, 2 * v.npitch, tmp));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    for (long long p = 0; p < nn; ++p) {
+      dst[2 * p] = tmp[p];
+      dst[2 * p + 1] = tmp[v.npitch + p];
+    }
     return 0;
   }
   if (!strcmp(f, "node_velocity")) {

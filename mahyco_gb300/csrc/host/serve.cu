@@ -347,6 +347,8 @@ int hydro_serve_submit(hydro_ctx* ctx, const hydro_spec* spec, int keep,
   if (!ctx || !spec) return fail(-1, "hydro_serve_submit: null argument");
   if (spec->scheme != HYDRO_SCHEME_VNR)
     return fail(-4, "hydro_serve_submit: the serving loop advances VNR runs");
+  if (spec->projection != 1)
+    return fail(-5, "hydro_serve_submit: the serving loop advances runs with the remap");
   ServeState* S = get_serve(ctx);
   std::lock_guard<std::mutex> lk(S->mu);
   if (S->error) return fail(-2, "serving stopped: " + S->error_msg);

@@ -89,6 +89,9 @@ struct RunView {
   const double* rho0_left;  // ny: initial density of column 0 (periodic)
 
   // ---- Lagrange -> remap
+  double* XN;         // 2 node planes, runs without the remap only: the
+                      // node positions at the cycle's start (the mesh
+                      // moves; with the remap it is the Euler mesh)
   double* XL;         // 2 node planes
   double *vL, *rL, *XcL /*2 planes*/, *Hx, *Hy;
   double* UL;         // ncomp planes (also receives the second sweep)
@@ -195,7 +198,7 @@ __device__ __forceinline__ bool output_pause_here(Ctrl& C) {
 
 // Per-kernel timing hook for launch_cycle.
 using LaunchHook = std::function<void(int)>;
-constexpr int kNumKernelKinds = 18;
+constexpr int kNumKernelKinds = 19;
 extern const char* const kKernelNames[kNumKernelKinds];
 
 // ---- batched execution: many independent runs advance in one launch per

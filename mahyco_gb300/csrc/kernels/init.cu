@@ -33,27 +33,8 @@ constexpr int kBX = 32, kBY = 4;
 DV double xs(const RunView& v, long long j) { return v.dx * (double)j; }
 DV double ys(const RunView& v, long long i) { return v.dy * (double)i; }
 
-// sqrt(dot(a, a)) with the dot product accumulated from 0.0
-// (includes/Freefunctions.h:15-20)
-DV double norm2(double a, double b) {
-  double r = 0.0;
-  r = r + a * a;
-  r = r + b * b;
-  return sqrt(r);
-}
 DV double cross2(const double* a, const double* b) { return a[0] * b[1] - a[1] * b[0]; }
 
-// includes/Freefunctions.h:28-58 (computeLpcNpc)
-DV void lpc_npc(const double* xp, const double* xpp, const double* xpm, double out[2]) {
-  const double a0 = 0.5 * (xpp[1] - xp[1]), a1 = 0.5 * (xp[0] - xpp[0]);
-  const double la = norm2(a0, a1);
-  const double na0 = a0 / la, na1 = a1 / la;
-  const double b0 = 0.5 * (xp[1] - xpm[1]), b1 = 0.5 * (xpm[0] - xp[0]);
-  const double lb = norm2(b0, b1);
-  const double nb0 = b0 / lb, nb1 = b1 / lb;
-  out[0] = na0 * la + nb0 * lb;
-  out[1] = na1 * la + nb1 * lb;
-}
 
 // block-wide min of ordered encodings into *dst, one atomic per block
 DV void block_min_into(unsigned long long x, unsigned long long* dst) {
@@ -258,6 +239,9 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_cells_vnr(RunView v, int t, 
     }
     const double sq = sqrt(s0);
     const double cfl = (v.projection == 1) ? 0.05 : 0.1;
+    // without the remap the Lagrange kernel takes the cell's volume of the
+    // cycle's start from vL (the sum of its current sub-volumes)
+    if (v.projection == 0) v.vL[c] = s0;
     const_cast<double*>(v.s0)[c] = s0;
     const_cast<double*>(v.sqs0)[c] = sq;
     const_cast<double*>(v.cflsq)[c] = cfl * sq;
@@ -324,6 +308,10 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_nodes_vnr(RunView v, int t, 
   if (i > v.ny || j > v.nx) return;
   const long long pn = i * (v.nx + 1) + j;
   const double x0 = xs(v, j), x1 = ys(v, i);
+  if (v.XN) {  // a run without the remap starts from the generated mesh
+    v.XN[pn] = x0;
+    v.XN[v.npitch + pn] = x1;
+  }
   double u = 0.0, w = 0.0;
   if ((t == 18 && variant == 2) || t == 0 || t == 11) {
     u = 1.0;  // the advection step extension; the unit tests (Init.cc:362-370)

@@ -319,7 +319,11 @@ HD double addz(double a, double b) {
   if ((ua ^ ub) == ~kMag && ma < kInfBits) return 0.0;  // a + (-a)
   return a + b;
 }
-HD double subz(double a, double b) { return addz(a, -b); }
+// a - b = a + (-b) exactly; the sign of b is flipped on the integer pipe
+// (a negated double operand may otherwise cost an FP64 instruction)
+HD double subz(double a, double b) {
+  return addz(a, from_bits(ubits(b) ^ 0x8000000000000000ull));
+}
 HD double mulz(double a, double b) {
   const unsigned long long ua = ubits(a), ub = ubits(b);
   const unsigned long long ma = ua & kMag, mb = ub & kMag;
@@ -346,6 +350,28 @@ HD double mul1z(double a, double b) {
 struct CellGeom {
   double vol, xc0, xc1, hx, hy;
 };
+// sqrt(dot(a, a)) with the dot product accumulated from 0.0
+// (includes/Freefunctions.h:15-20)
+HD double norm2(double a, double b) {
+  double r = 0.0;
+  r = r + a * a;
+  r = r + b * b;
+  return sqrt(r);
+}
+// Corner normal l+ n+ + l- n- of a node xp between its successor xpp and
+// predecessor xpm in the cell's node order (includes/Freefunctions.h:28-58,
+// computeLpcNpc)
+HD void lpc_npc(const double* xp, const double* xpp, const double* xpm, double out[2]) {
+  const double a0 = 0.5 * (xpp[1] - xp[1]), a1 = 0.5 * (xp[0] - xpp[0]);
+  const double la = norm2(a0, a1);
+  const double na0 = a0 / la, na1 = a1 / la;
+  const double b0 = 0.5 * (xp[1] - xpm[1]), b1 = 0.5 * (xpm[0] - xp[0]);
+  const double lb = norm2(b0, b1);
+  const double nb0 = b0 / lb, nb1 = b1 / lb;
+  out[0] = na0 * la + nb0 * lb;
+  out[1] = na1 * la + nb1 * lb;
+}
+
 HD CellGeom vnr_cell_geometry(const double X[4][2], bool widths) {
   CellGeom G;
   double xc0 = plus_zero(X[0][0]), xc1 = plus_zero(X[0][1]);

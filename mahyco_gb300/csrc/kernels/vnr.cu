@@ -144,8 +144,10 @@ __device__ void block_reduce_minmax(unsigned long long dtv,
   __syncthreads();
 }
 
-// dt candidate of one cell (Vnr::computeDeltaT, VnrRemap.cc:26-46) with
-// projection: cfl*sqrt(sum V_pc) / (uc + c), uc = sum_p 0.25*|u_p|.
+// dt candidate of one cell (Vnr::computeDeltaT, VnrRemap.cc:26-46):
+// cfl*sqrt(sum V_pc) / (A*uc + c), uc = sum_p 0.25*|u_p|, with A = 1 and cfl
+// 0.05 with the remap, A = 0 and cfl 0.1 without it (the reference then
+// multiplies the nodal speed by zero).
 DV double cell_dt(const RunView& v, long long c, int i, int j) {
   const long long n0 = (long long)i * (v.nx + 1) + j;
   const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
@@ -153,6 +155,7 @@ DV double cell_dt(const RunView& v, long long c, int i, int j) {
   double uc = quarter(ld(v.speed, nd[0]));
 #pragma unroll
   for (int k = 1; k < 4; ++k) uc = addz(uc, quarter(ld(v.speed, nd[k])));
+  if (v.projection == 0) return ld(v.cflsq, c) / (0. * uc + v.c[c]);
   return ld(v.cflsq, c) / addz(uc, v.c[c]);
 }
 
@@ -195,13 +198,39 @@ struct LagNodes {
         }
         return s_val * r;
       };
+      // Corner normal of this node in cell t.  With the remap the mesh is
+      // the Euler one at every cycle's start and the set-up stored them;
+      // without it (Vnr::computeCornerNormal, PhaseLagrange.cc:114-136, at
+      // each cycle's start) they come from the current positions of the
+      // node and of its successor / predecessor in the cell's node order.
+      const long long NP = v.npitch, W = v.nx + 1;
+      auto corner = [&](int t, double& C0, double& C1) {
+        if (!v.XN) {
+          C0 = ld(v.cqs, (2 * loc[t]) * v.pitch + cells[t]);
+          C1 = ld(v.cqs, (2 * loc[t] + 1) * v.pitch + cells[t]);
+          return;
+        }
+        // successor, predecessor: (right, up), (up, left), (left, down),
+        // (down, right) for the cell's bottom-left, bottom-right, top-right
+        // and top-left node
+        const long long nxt[4] = {p + 1, p + W, p - 1, p - W};
+        const long long prv[4] = {p + W, p - 1, p - W, p + 1};
+        const long long a = nxt[loc[t]], b = prv[loc[t]];
+        const double xp[2] = {v.XN[p], v.XN[NP + p]};
+        const double xa[2] = {v.XN[a], v.XN[NP + a]};
+        const double xb[2] = {v.XN[b], v.XN[NP + b]};
+        double o[2];
+        lpc_npc(xp, xa, xb, o);
+        C0 = o[0];
+        C1 = o[1];
+      };
       auto force = [&](bool sym, double sx, double sy, double& r0, double& r1) {
         r0 = 0.0;
         r1 = 0.0;
         for (int t = 0; t < k; ++t) {
           const long long c = cells[t];
-          const double C0 = ld(v.cqs, (2 * loc[t]) * v.pitch + c);
-          const double C1 = ld(v.cqs, (2 * loc[t] + 1) * v.pitch + c);
+          double C0, C1;
+          corner(t, C0, C1);
           const double w = addz(v.p[c], v.q[c]);
           double t0, t1;
           if (!sym) {
@@ -226,7 +255,7 @@ struct LagNodes {
         // cancel exactly (nsym, set up with the derivation): the sum is +0
         // without the products
         bool zero = false;
-        if (ld_u8(v.nsym, p)) {
+        if (!v.XN && ld_u8(v.nsym, p)) {  // a flag of the Euler mesh
           const unsigned long long w0 = ubits(addz(v.p[cells[0]], v.q[cells[0]]));
           constexpr unsigned long long kMod = 1523ull << 52;  // 2^500
           zero = (w0 & kMag) < kMod;
@@ -301,10 +330,14 @@ struct LagNodes {
       v.u[p] = ux;
       v.u[v.npitch + p] = uy;
     }
-    // stored last: a store earlier would order the force loads behind it
+    // stored last: a store earlier would order the force loads behind it;
+    // updatePosition (PhaseLagrange.cc:203-208) from the cycle's start
+    // positions (the Euler mesh with the remap)
+    const double X0 = v.XN ? v.XN[p] : ld(v.xs, j);
+    const double X1 = v.XN ? v.XN[v.npitch + p] : ld(v.ys, i);
     v.node_mass[p] = m;
-    v.XL[p] = addz(ld(v.xs, j), mulz(C.dt_np1, ux));
-    v.XL[v.npitch + p] = addz(ld(v.ys, i), mulz(C.dt_np1, uy));
+    v.XL[p] = addz(X0, mulz(C.dt_np1, ux));
+    v.XL[v.npitch + p] = addz(X1, mulz(C.dt_np1, uy));
   }
 };
 
@@ -368,6 +401,10 @@ struct LagCells {
     // order the later loads behind them)
     const double rho_old = v.rho[c], divu_old = v.divu[c], c_old = v.c[c];
     const double sarg_old = v.sarg[c];
+    // sum of the sub-volumes at the cycle's start (the pseudo-viscosity's
+    // volume): the Euler cell's with the remap, the Lagrangian volume of the
+    // previous cycle (vL) without it
+    const double vol_start = (v.projection == 0) ? v.vL[c] : 0.0;
   #pragma unroll
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
@@ -418,9 +455,10 @@ struct LagCells {
         // flow has not arrived (0 / tau)
         divu_new = qdiv(rdt * (same_rho ? 0.0 : irho_new - irho_old), tau);
         if (neg(divu_old)) {
-          const double s0 = ld(v.s0, c);
+          const double s0 = (v.projection == 0) ? vol_start : ld(v.s0, c);
+          const double sq0 = (v.projection == 0) ? sqrt(vol_start) : ld(v.sqs0, c);
           q_new = 1.0 / tau *
-                  (-half(ld(v.sqs0, c)) * c_old * divu_new +
+                  (-half(sq0) * c_old * divu_new +
                    v.hgs1 * s0 * divu_new * divu_new);
         } else {
           q_new = 0.0;
@@ -1888,6 +1926,49 @@ __global__ void k_node_speed(RunView v) {
 }
 
 
+// ------------------------------------------------- Lagrange phase only
+// A run without the remap (AvecProjection = non): the Lagrange cell update,
+// then the next cycle's dt candidate (Vnr::computeDeltaT, VnrRemap.cc
+// :14-50: cfl 0.1, the sub-volumes just formed, the new node velocities and
+// sound speed, A = 0) and pressure maximum, which the remap's final kernel
+// reduces otherwise.
+struct LagCellsLagrangeOnly {
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    Ctrl& C = *v.ctrl;
+    unsigned long long dtb = ~0ull, pb = 0ull;
+    if (i < v.ny && j < v.nx) {
+      LagCells{}(v, i, j);
+      const long long c = (long long)i * v.nx + j, NP = v.npitch;
+      const long long n0 = (long long)i * (v.nx + 1) + j;
+      const long long nd[4] = {n0, n0 + 1, n0 + v.nx + 2, n0 + v.nx + 1};
+      double uc = 0.0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const double a = v.u[nd[k]], b = v.u[NP + nd[k]];
+        uc += sqrt(a * a + b * b) * 0.25;
+      }
+      const double d = 0.1 * sqrt(v.vL[c]) / (0. * uc + v.c[c]);
+      if (v.sans_lagrange == 0 && !is_nan(d)) dtb = ord_bits(d);
+      const double p = v.p[c];
+      if (!is_nan(p)) pb = ord_bits(p);
+    }
+    block_reduce_minmax(dtb, pb, &C);
+  }
+};
+
+// The new positions become the next cycle's (the reference swaps its node
+// coordinate views, VnrRemap.cc:217-221) unless the run has just ended:
+// after its last cycle the reference does not swap, and its final output
+// shows the last cycle's start positions.
+struct NextPositions {
+  __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
+    if (i > v.ny || j > v.nx || v.ctrl->done) return;
+    const long long p = (long long)i * (v.nx + 1) + j;
+    v.XN[p] = v.XL[p];
+    v.XN[v.npitch + p] = v.XL[v.npitch + p];
+  }
+};
+
 // ---------------------------------------------------------------- wrappers
 // Plain launches: one run, a 2D grid of kBX x kBY thread tiles.
 template <class F>
@@ -1898,6 +1979,8 @@ __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
 
 __global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
 __global__ void __launch_bounds__(kBX* kBY, 6) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
+__global__ void __launch_bounds__(kBX* kBY) k_lag_cells_lo(RunView v) { plain_items(v, LagCellsLagrangeOnly{}); }
+__global__ void __launch_bounds__(kBX* kBY) k_next_positions(RunView v) { plain_items(v, NextPositions{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { plain_items(v, FaceGrad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_grad(RunView v, int sweep) { plain_items(v, O3Grad{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_o3_ystar(RunView v, int sweep) { plain_items(v, O3Ystar{sweep}); }
@@ -1995,7 +2078,7 @@ const char* const kKernelNames[kNumKernelKinds] = {
     "k_sweep_grad", "k_sweep_face",       "k_sweep_update", "k_dual_grad",
     "k_dual_update", "k_final",           "k_end",         "k_face_grad",
     "ke_cell_pre",  "ke_nodes",           "ke_cells",      "ke_final",
-    "k_o3_grad",    "k_o3_ystar"};
+    "k_o3_grad",    "k_o3_ystar",        "k_next_positions"};
 
 // Enqueues one full cycle on stream s; hook(kind) is called before each
 // launch (and with kind = -1 after the last) when given.  Returns the number
@@ -2053,6 +2136,15 @@ int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook) {
   H(0); k_begin<<<1, 1, 0, s>>>(v); ++nk;
   H(1); k_reset_reductions<<<1, 1, 0, s>>>(v); ++nk;
   H(2); k_lag_nodes<<<ng, blk, 0, s>>>(v); ++nk;
+  if (v.projection == 0) {
+    // the Lagrange phase only: its cell kernel reduces the next dt, and the
+    // new positions are carried to the next cycle after the loop test
+    H(3); k_lag_cells_lo<<<cg, blk, 0, s>>>(v); ++nk;
+    H(10); k_end<<<1, 1, 0, s>>>(v); ++nk;
+    H(18); k_next_positions<<<ng, blk, 0, s>>>(v); ++nk;
+    H(-1);
+    return nk;
+  }
   H(3); k_lag_cells<<<cg, blk, 0, s>>>(v); ++nk;
   for (int sweep = 1; sweep <= 2; ++sweep) {
     nk += launch_sweep(v, sweep, s, hook);

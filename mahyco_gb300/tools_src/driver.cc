@@ -118,8 +118,12 @@ int main(int argc, char** argv) {
   Vars last_cells;  // the arrays of the last output (VNR's final call)
   const Vars empty_points = {{"VolumePart", nullptr}, {"VxPart", nullptr}, {"VyPart", nullptr}};
 
+  // without the remap the mesh moves: each output shows the positions of
+  // the cycle's start (Vnr::dumpVariables writes m_node_coord_n)
+  const bool moving = vnr && spec.projection == 0;
   auto dump = [&](long call, double t, const Vars& cells, const Vars& nodes) {
-    main_series.write((int)call, t, cells, nodes);
+    main_series.write((int)call, t, cells, nodes,
+                      moving ? fetch(run, "node_coord") : hydro_out::Array());
     if (particles) particles->write((int)call, t, cells, empty_points);
     if (!o.quiet) std::printf(" time = %g sortie demandée \n", t);
   };

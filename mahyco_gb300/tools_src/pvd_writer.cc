@@ -212,7 +212,8 @@ PvdSeries::PvdSeries(Writer& w, std::string module, const std::string& base, con
   });
 }
 
-void PvdSeries::write(int iteration, double time, const Vars& cell_vars, const Vars& node_vars) {
+void PvdSeries::write(int iteration, double time, const Vars& cell_vars, const Vars& node_vars,
+                      const Array& xy) {
   if (disabled_) return;
   std::vector<Writer::File> files(2);
   const std::string name = module_ + "." + std::to_string(iteration) + ".vtp";
@@ -225,7 +226,25 @@ void PvdSeries::write(int iteration, double time, const Vars& cell_vars, const V
   append_int(head, n_cells_);
   head += "\">\n\t\t\t<Points>\n\t\t\t\t<DataArray type=\"Float32\" NumberOfComponents=\"3\" format=\"ascii\">\n";
   vtp.pieces.push_back(w_.text(std::move(head)));
-  if (n_points_) vtp.pieces.push_back(points_);
+  if (n_points_ && xy) {
+    // a moving mesh: " x y 0" per node from this output's positions
+    const long np = n_points_;
+    Array keep = xy;
+    vtp.pieces.push_back(w_.format([keep, np] {
+      std::string s;
+      s.reserve((size_t)np * 24);
+      for (long q = 0; q < np; ++q) {
+        s.push_back(' ');
+        append_g6(s, (*keep)[2 * q]);
+        s.push_back(' ');
+        append_g6(s, (*keep)[2 * q + 1]);
+        s += " 0";
+      }
+      return s;
+    }));
+  } else if (n_points_) {
+    vtp.pieces.push_back(points_);
+  }
   std::string mid =
       "\n\t\t\t\t</DataArray>\n\t\t\t</Points>\n\t\t\t<Polys>\n\t\t\t\t<DataArray type=\"Int32\" "
       "Name=\"connectivity\" format=\"ascii\">\n";

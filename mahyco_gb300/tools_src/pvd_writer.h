@@ -62,8 +62,11 @@ class PvdSeries {
   bool disabled() const { return disabled_; }
   const std::string& directory() const { return dir_; }
   // Queues <module>.<iteration>.vtp and the rewrite of <module>.pvd.  Cell
-  // arrays hold mesh->cells() values, node arrays mesh->nodes().
-  void write(int iteration, double time, const Vars& cell_vars, const Vars& node_vars);
+  // arrays hold mesh->cells() values, node arrays mesh->nodes().  `xy`, when
+  // given, holds the node positions of a mesh that moves (x, y per node, in
+  // node order) in place of the generated mesh's.
+  void write(int iteration, double time, const Vars& cell_vars, const Vars& node_vars,
+             const Array& xy = nullptr);
 
  private:
   Writer& w_;

@@ -1404,6 +1404,7 @@ static const double* field_ptr(port_run* R, const char* name, size_t* n) {
     F("energy_env", R->em_n, R->em_np1, NM * nc)
     F("pressure_env", R->pm_n, R->pm_np1, NM * nc)
     F("node_velocity", R->u_n, R->u_np1, 2 * nn)
+    F("node_coord", R->X_n, R->X_np1, 2 * nn)
   } else {
     F("density", R->rho_n, R->rho_np1, nc)
     F("energy", R->e_n, R->e_np1, nc)

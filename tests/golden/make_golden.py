@@ -94,7 +94,8 @@ def main() -> None:
         if not deck.exists():
             continue
         spec = M.parse_deck(deck)
-        if spec.projection == 1:
+        # with the remap, and VNR without it (the Lagrange phase alone)
+        if spec.projection == 1 or spec.scheme == M.SCHEME_VNR:
             cases.append((d.name, spec, deck, ()))
     tmp = Path(tempfile.mkdtemp())
     # 200x10 Sod X, VNR, order-2 remap, minmod, t = 0.2

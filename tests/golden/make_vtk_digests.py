@@ -50,7 +50,11 @@ def main() -> None:
             if not deck.exists() or not (d / "reference").is_dir():
                 continue
             spec = M.parse_deck(deck)
-            if spec.projection != 1 or spec.scheme not in (M.SCHEME_VNR, M.SCHEME_EUCCLHYD):
+            # every deck the GPU path takes: both schemes with the remap, VNR
+            # without it (the Eucclhyd Lagrange-only deck is refused)
+            if spec.scheme not in (M.SCHEME_VNR, M.SCHEME_EUCCLHYD):
+                continue
+            if spec.projection != 1 and spec.scheme != M.SCHEME_VNR:
                 continue
             text = M.deck_text(spec)
             again = Path(tmp) / f"{d.name}.txt"

@@ -79,7 +79,8 @@ def test_batch_of_reference_decks(M):
     end at their own final times and match the reference's final state."""
     ctx = M.Context(0)
     cases = [c for c in golden_cases()
-             if load_golden(GOLDEN / f"{c}.npz")[0].scheme == M.SCHEME_VNR]
+             if load_golden(GOLDEN / f"{c}.npz")[0].scheme == M.SCHEME_VNR
+             and load_golden(GOLDEN / f"{c}.npz")[0].projection == 1]
     loaded = [load_golden(GOLDEN / f"{c}.npz") for c in cases]
     runs = [M.Run(spec, ctx) for spec, _, _ in loaded]
     batch = M.Batch(runs)
@@ -130,3 +131,21 @@ def test_batch_untuned_matches_tuned(M):
     M.Batch(b).step(40)
     for s, x, y in zip(specs, a, b):
         compare_runs(M, x, y, s.nbmat, f"{s.nx}x{s.ny}")
+
+
+def test_batch_and_server_refuse_runs_without_remap(M):
+    """The batched and served forms advance runs with the remap: a
+    Lagrange-only run is refused with a clear error (and the context stays
+    usable); it runs on the plain path."""
+    spec, _, _ = load_golden(GOLDEN / "SOD_X_Mono_mat_Lagrange_Vnr.npz")
+    ctx = M.Context(0)
+    run = M.Run(spec, ctx)
+    with pytest.raises(RuntimeError, match="remap"):
+        M.Batch([run], ctx).step(1)
+    srv = M.Server(ctx)
+    with pytest.raises(RuntimeError, match="remap"):
+        srv.submit(spec)
+    srv.stop(drain=False)
+    assert not run.step(5)
+    assert run.time()[2] == 5
+

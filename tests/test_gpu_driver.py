@@ -76,14 +76,17 @@ def test_driver_output_dir_and_none(driver, tmp_path):
     assert not any(none.iterdir())
 
 
-def test_driver_rejects_bad_deck_and_lagrange_only(driver, tmp_path):
+def test_driver_rejects_bad_deck_and_eucclhyd_lagrange_only(driver, tmp_path):
+    """A deck that does not parse exits 1; an Eucclhyd run without the remap
+    (the one reference deck the GPU path does not take) is refused at
+    creation with exit 2."""
     import mahyco_gb300 as M
     bad = tmp_path / "bad.txt"
     bad.write_text("# Cas test\nNotACase\n")
     res = subprocess.run([str(driver), str(bad)], cwd=tmp_path, capture_output=True,
                          text=True, timeout=120)
     assert res.returncode == 1
-    spec = M.parse_deck(_deck(tmp_path, "SOD_X_Mono_mat_Minmod_vnr_o2"))
+    spec = M.parse_deck(_deck(tmp_path, "POINT_TRIPLE_MinMod_simple"))
     spec.projection = 0
     lag = tmp_path / "lag.txt"
     M.write_deck(spec, lag)

@@ -318,3 +318,32 @@ def test_gpu_shock_bubble_larger_matches_port(order, pb, M, ctx, port_lib):
     assert g.error() == c.error()
     for f in fields_of(spec):
         assert_bitwise(f, get_field(g, f, spec.nbmat), get_field(c, f, spec.nbmat))
+
+
+@pytest.mark.parametrize("case,centred", [("SOD_X_bi_mat_Lagrange_Vnr", 0),
+                                          ("SOD_Y_Mono_mat_Lagrange_Vnr_Qcentree", 1)])
+def test_gpu_lagrange_only_larger_matches_port(case, centred, M, ctx, port_lib):
+    """VNR without the remap (the Lagrange phase alone, the mesh moving) on
+    a mesh eight times the reference deck's, 400 cycles: every field and the
+    node positions bit-identical to the C restatement, compared both in the
+    middle of the run and at its end (pseudo_centree as the deck has it)."""
+    spec, _, _ = load_golden(GOLDEN / f"{case}.npz")
+    assert spec.projection == 0 and spec.pseudo_centree == centred
+    spec.nx, spec.ny = spec.nx * 2 if spec.nx > spec.ny else spec.nx * 4, \
+        spec.ny * 4 if spec.nx > spec.ny else spec.ny * 2
+    spec.dx, spec.dy = (1.0 / spec.nx, 0.1 / spec.ny) if spec.nx > spec.ny else \
+        (0.1 / spec.nx, 1.0 / spec.ny)
+    spec.max_cycles = 400
+    g = M.Run(spec, ctx)
+    c = port_lib.PortRun(spec)
+    g.step(250)
+    c.step(250)
+    assert g.time() == c.time()
+    for f in CELL_FIELDS + NODE_FIELDS + ["node_coord"]:
+        assert_bitwise(f"{case}@250:{f}", get_field(g, f, spec.nbmat), get_field(c, f, spec.nbmat))
+    g.simulate()
+    c.simulate()
+    assert g.time() == c.time()
+    for f in CELL_FIELDS + NODE_FIELDS + ["node_mass"]:
+        assert_bitwise(f"{case}:{f}", get_field(g, f, spec.nbmat), get_field(c, f, spec.nbmat))
+    assert g.error()[0] & ~M.ERR_NEGATIVE == 0
