@@ -616,11 +616,13 @@ struct LagCells {
 // Face normal velocity (PrepareRemap.cc:42-63): mean of the two nodes'
 // Lagrange velocities along the face normal; "+ 0.0" is the dot product's
 // zero start for the other axis.
+// (addz: the sum of two zero velocities, the case at rest, on the integer
+// pipe)
 DV double fnv_vertical(const RunView& v, long long na, long long nb) {
-  return plus_zero(half(v.u[na] + v.u[nb]));
+  return plus_zero(half(addz(v.u[na], v.u[nb])));
 }
 DV double fnv_horizontal(const RunView& v, long long na, long long nb) {
-  return plus_zero(half(v.u[v.npitch + na] + v.u[v.npitch + nb]));
+  return plus_zero(half(addz(v.u[v.npitch + na], v.u[v.npitch + nb])));
 }
 
 // ----------------------------------------------------------- remap sweep
