@@ -566,6 +566,28 @@ struct LagCells {
         if (eos_of(v, m) == HYDRO_EOS_VOID) e_new += mf[m] * em_new[m];
       v.c[c] = cc;
       v.sarg[c] = sarg_new;
+      if (v.projection == 0) {
+        // Without the remap no later kernel forms the state after this
+        // phase: its densities, energies, pseudo-viscosity, and the
+        // pressures of computeEOSGP ((gamma - 1) rho e; a Void material
+        // keeps its pressure) and computePressionMoyenne (the sum from 0.0
+        // of f p) are stored here (PhaseLagrange.cc:392-485)
+        double pmean = 0.;
+        for (int m = 0; m < nb; ++m) {
+          const double pmm = (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS)
+                                 ? gm1_of(v, m) * rhom_new[m] * em_new[m]
+                                 : pm_o[m];
+          pmean += f[m] * pmm;
+          v.pm[m * P + c] = pmm;
+          v.rhom[m * P + c] = rhom_new[m];
+          v.em[m * P + c] = em_new[m];
+          if (!pos(rho_new) && eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) v.cm[m * P + c] = cm_new[m];
+        }
+        v.p[c] = pmean;
+        v.rho[c] = rho_new;
+        v.e[c] = e_new;
+        v.q[c] = q_new;
+      }
     } else {
       // no Lagrange phase (advection cases): energy and q are carried over
       e_new = v.e[c];
@@ -858,8 +880,9 @@ struct SweepGradT {
       }
       grad[k] = limit_grad1(lim, gp, gm, yp, ym, h0, hp, hm);
       if (pb == 0) {
-        if (up_p) v.phiF[k * FP + fp] = y0 + sp * grad[k];
-        if (up_m) v.phiF[k * FP + fm] = y0 + sm * grad[k];
+        // y0 + s * slope exactly (a zero slope on the integer pipe)
+        if (up_p) v.phiF[k * FP + fp] = addz(y0, mulz(sp, grad[k]));
+        if (up_m) v.phiF[k * FP + fm] = addz(y0, mulz(sm, grad[k]));
       }
     }
     if (pb == 1) {
@@ -1258,8 +1281,10 @@ struct SweepUpdateT {
       nrm[0] = na;
       nrm[1] = nb_;
       if (v.pb == 0) {
-        coef[0] = na * va * fl * dt;
-        coef[1] = nb_ * vb * fl * dt;
+        // ((n * u_f) * L) * dt exactly; a face at rest gives a zero on the
+        // integer pipe
+        coef[0] = mulz(mulz(mulz(na, va), fl), dt);
+        coef[1] = mulz(mulz(mulz(nb_, vb), fl), dt);
       } else {
         coef[0] = mul_pm1(fl, na);
         coef[1] = mul_pm1(fl, nb_);
@@ -1276,8 +1301,10 @@ struct SweepUpdateT {
       nrm[0] = na;
       nrm[1] = nb_;
       if (v.pb == 0) {
-        coef[0] = na * va * fl * dt;
-        coef[1] = nb_ * vb * fl * dt;
+        // ((n * u_f) * L) * dt exactly; a face at rest gives a zero on the
+        // integer pipe
+        coef[0] = mulz(mulz(mulz(na, va), fl), dt);
+        coef[1] = mulz(mulz(mulz(nb_, vb), fl), dt);
       } else {
         coef[0] = mul_pm1(fl, na);
         coef[1] = mul_pm1(fl, nb_);
@@ -1313,6 +1340,12 @@ struct SweepUpdateT {
         else if ((v.flux_bc & kFluxTop) && c <= (long long)v.nx * (v.ny - 1)) bcf = 2;
       }
     }
+    // A face whose coefficient is a zero (without PenteBorne: its normal
+    // velocity is, the face does not move) carries coef * q = the zero of
+    // sign(coef) xor sign(q) for every finite q, as a zero value q does:
+    // such faces take the still paths below.  Not with a boundary flux,
+    // whose term pairs one face's coefficient with the other's value.
+    const bool zc0 = bcf == 0 && iszero(coef[0]), zc1 = bcf == 0 && iszero(coef[1]);
     // dual-method components: masses (A1) or volumes (A2)
     const int doff = (v.dual_method == 1) ? 0 : nb;
     double U[kMaxComp];
@@ -1344,7 +1377,9 @@ struct SweepUpdateT {
       bool group_still = cfin;
   #pragma unroll
       for (int t = 0; t < 4; ++t)
-        if (k0 + t < ncomp) group_still = group_still && iszero(qa[t]) && iszero(qb[t]) && !is_nan(ui[t]);
+        if (k0 + t < ncomp)
+          group_still = group_still && (iszero(qa[t]) || (zc0 && is_finite(qa[t]))) &&
+                        (iszero(qb[t]) || (zc1 && is_finite(qb[t]))) && !is_nan(ui[t]);
       if (group_still) {
   #pragma unroll
         for (int t = 0; t < 4; ++t) {
@@ -1369,7 +1404,8 @@ struct SweepUpdateT {
         if (k >= ncomp) break;
         const double q0 = qa[t], q1 = qb[t], uin = ui[t];
         double F0 = 0., F1 = 0.;
-        if (cfin && iszero(q0) && iszero(q1) && !is_nan(uin)) {
+        if (cfin && (iszero(q0) || (zc0 && is_finite(q0))) &&
+            (iszero(q1) || (zc1 && is_finite(q1))) && !is_nan(uin)) {
           // nothing crosses either face: each flux coef * q is the zero of
           // sign(coef) xor sign(q), their sum from 0.0 is +0, and uin - +0 is
           // uin
