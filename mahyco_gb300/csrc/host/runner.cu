@@ -71,6 +71,7 @@ size_t layout(RunView& v, char* base) {
   v.node_mass = a.take<double>(NP);
   v.speed = a.take<double>(NP);
   v.XN = (v.projection == 0) ? a.take<double>(2 * NP) : nullptr;
+  v.vout = (v.projection == 0) ? a.take<double>(2 * NP) : nullptr;
   v.XL = a.take<double>(2 * NP);
   v.vL = a.take<double>(P);
   v.rL = a.take<double>(P);
@@ -607,7 +608,9 @@ static int fetch_dump(hydro_run* r, const char* f, int k, double* dst, size_t n)
   } else if (!strcmp(f, "VelocityX") || !strcmp(f, "VelocityY")) {
     plane = v.uco + k * v.pitch;
   } else if (!strcmp(f, "VitesseX") || !strcmp(f, "VitesseY")) {
-    plane = v.u + k * v.npitch;
+    // m_x/y_velocity: without the remap only the interior nodes' are
+    // refreshed (updateVelocity), a separate plane (vout) keeps that
+    plane = (v.vout ? v.vout : v.u) + k * v.npitch;
   } else if (k < v.nbmat) {
     plane = v.fm + k * v.pitch;
   }

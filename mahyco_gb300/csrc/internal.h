@@ -92,6 +92,10 @@ struct RunView {
   double* XN;         // 2 node planes, runs without the remap only: the
                       // node positions at the cycle's start (the mesh
                       // moves; with the remap it is the Euler mesh)
+  double* vout;       // 2 node planes, runs without the remap only: the
+                      // dumped node velocity (m_x/y_velocity), which the
+                      // reference then refreshes for interior nodes only
+                      // (the boundary nodes keep their initial velocity)
   double* XL;         // 2 node planes
   double *vL, *rL, *XcL /*2 planes*/, *Hx, *Hy;
   double* UL;         // ncomp planes (also receives the second sweep)

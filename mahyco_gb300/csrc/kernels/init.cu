@@ -336,6 +336,10 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_nodes_vnr(RunView v, int t, 
   }
   v.u[pn] = u;
   v.u[v.npitch + pn] = w;
+  if (v.vout) {
+    v.vout[pn] = u;
+    v.vout[v.npitch + pn] = w;
+  }
   // exact cancellation of the interior force sum (updateVelocity,
   // PhaseLagrange.cc:167-197): with one pressure w in the four cells the sum
   // is ((w C_0 + w C_1) + w C_2) + w C_3 per component, the first addition

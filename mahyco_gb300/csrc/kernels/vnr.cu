@@ -270,6 +270,10 @@ struct LagNodes {
         }
         ux = addz(u0x, step(r0));
         uy = addz(u0y, step(r1));
+        if (v.vout) {  // m_x/y_velocity, inner nodes only (PhaseLagrange.cc:193)
+          v.vout[p] = ux;
+          v.vout[v.npitch + p] = uy;
+        }
       }
       // sides in the reference's order: bottom, top, left, right
       if (i == 0) {
@@ -1371,9 +1375,10 @@ struct SweepUpdateT {
         }
         ui[t] = (k < ncomp) ? Uin[k * P + c] : 0.;
       }
-      // a group whose face values are all zeros: each component keeps its
-      // value (see below), decided once so that the arithmetic is branched
-      // over rather than issued under a predicate
+      // a group whose faces all carry zero fluxes (zero values, or faces
+      // with a zero coefficient): each component keeps its value (see
+      // below), decided once so that the arithmetic is branched over rather
+      // than issued under a predicate
       bool group_still = cfin;
   #pragma unroll
       for (int t = 0; t < 4; ++t)
