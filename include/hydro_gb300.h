@@ -164,6 +164,17 @@ int hydro_run_profile(hydro_run* run, int ncycles, double* ms,
 const char* hydro_kernel_name(int kind);
 int hydro_kernel_kinds(void);
 int hydro_fp64_peak(int device, double* tflops);
+/* The integer-pipe binary64 operations the kernels use for the common case
+ * (normal operands and result): op 0 a*b, 1 a+b, 2 a/b, 3 sqrt(a), 4 a-b,
+ * for n elements of device arrays a, b.  soft = the fast path's result,
+ * hw = the FP64 instruction's, fast[i] = 1 where the fast path applies
+ * (elsewhere the kernels use the FP64 instruction).  Asynchronous on
+ * stream. */
+int hydro_softfp_check(int op, const double* a, const double* b, double* soft, double* hw,
+                       unsigned char* fast, long long n, void* stream);
+/* Operations per second of dependent chains of mul, add, div, sqrt:
+ * rates[2k] the FP64 instruction, rates[2k+1] the integer-pipe form. */
+int hydro_softfp_rates(int device, double* rates);
 
 /* Batched form (no counterpart in the reference, which advances one mesh
  * per scheme object; each run's cycle is Vnr::executeTimeLoopN's cycle).

@@ -126,6 +126,8 @@ def lib() -> C.CDLL:
         L.hydro_kernel_name.restype = C.c_char_p
         L.hydro_kernel_kinds.restype = i
         L.hydro_fp64_peak.argtypes = [i, C.POINTER(C.c_double)]
+        L.hydro_softfp_check.argtypes = [i, vp, vp, vp, vp, vp, C.c_longlong, vp]
+        L.hydro_softfp_rates.argtypes = [i, C.POINTER(C.c_double)]
         runs_t = C.POINTER(vp)
         L.hydro_batch_step.argtypes = [vp, runs_t, i, i, C.POINTER(i)]
         L.hydro_batch_enqueue.argtypes = [vp, runs_t, i, i]
@@ -159,6 +161,15 @@ def fp64_peak_tflops(device: int = 0) -> float:
     t = C.c_double()
     _check(lib().hydro_fp64_peak(device, C.byref(t)), "hydro_fp64_peak")
     return t.value
+
+
+def softfp_rates(device: int = 0) -> dict:
+    """Operations per second of dependent FP64 chains: the FP64 instruction
+    against the integer-pipe form, for mul, add, div and sqrt."""
+    r = (C.c_double * 8)()
+    _check(lib().hydro_softfp_rates(device, r), "hydro_softfp_rates")
+    return {op: {"fp64_pipe": r[2 * k], "integer_pipe": r[2 * k + 1]}
+            for k, op in enumerate(("mul", "add", "div", "sqrt"))}
 
 
 def default_spec() -> HydroSpec:

@@ -136,7 +136,7 @@ DV void cell_eos(const RunView& v, int m, long long c, double& pm, double& cm) {
       // the volatile barrier keeps the division and the root inside this
       // branch (a select would form them for absent materials too)
       asm volatile("");
-      cm = sqrt(g * pm / rm);
+      cm = sqrt_ip(div_ip(g * pm, rm));
     } else {
       cm = 1.e-20;
     }
@@ -178,7 +178,7 @@ struct EucCellPre {
         snd = smax(snd, cm[m]);
       }
       const double rho = v.rho[c];
-      if (pos(rho)) snd = sqrt(v.gamma[0] * p / rho);
+      if (pos(rho)) snd = sqrt_ip(div_ip(v.gamma[0] * p, rho));
       v.p[c] = p;
       v.c[c] = snd;
       const double V = ldg(v.evol, c);
@@ -222,8 +222,8 @@ struct EucCellPre {
       }
       const double u0 = v.uc[c], u1 = v.uc[P + c];
       const double un = face_len(u0, u1);  // sqrt(dot(u, u))
-      const double cdt = (v.projection == 1) ? V / (ldg(v.perim, c) * (un + snd))
-                                             : V / (ldg(v.perim, c) * snd);
+      const double cdt = (v.projection == 1) ? div_ip(V, ldg(v.perim, c) * (un + snd))
+                                             : div_ip(V, ldg(v.perim, c) * snd);
       if (!is_nan(cdt)) dtb = ord_bits(cdt);
     }
     block_min(dtb, v.ctrl);
@@ -235,14 +235,14 @@ DV void bc_velocity(int bc, double V0, double V1, const double* Mp, const double
                     double& o0, double& o1) {
   if (bc == kBcSym) {
     const double mv0 = dot2(Mp[0], Mp[1], V0, V1), mv1 = dot2(Mp[2], Mp[3], V0, V1);
-    const double s = dot2(G[0], G[1], V0, V1) / dot2(mv0, mv1, V0, V1);
+    const double s = div_ip(dot2(G[0], G[1], V0, V1), dot2(mv0, mv1, V0, V1));
     o0 = V0 * s;
     o1 = V1 * s;
   } else if (bc == kBcImposed) {
     o0 = V0;
     o1 = V1;
   } else if (bc == 202) {  // free: inverse(Mp) . G
-    const double alpha = 1.0 / (Mp[0] * Mp[3] - Mp[1] * Mp[2]);
+    const double alpha = div_ip(1.0, Mp[0] * Mp[3] - Mp[1] * Mp[2]);
     const double i0 = Mp[3] * alpha, i1 = -Mp[1] * alpha, i2 = -Mp[2] * alpha,
                  i3 = Mp[0] * alpha;
     o0 = dot2(i0, i1, G[0], G[1]);
@@ -379,7 +379,7 @@ struct EucNodes {
       u0 = 0.0;
       u1 = 0.0;
       if (b1 == kBcSym && b2 == kBcSym) {
-        const double na = sqrt(dot2(A0, A1, A0, A1)), nbb = sqrt(dot2(B0, B1, B0, B1));
+        const double na = sqrt_ip(dot2(A0, A1, A0, A1)), nbb = sqrt_ip(dot2(B0, B1, B0, B1));
         if (fabs(fabs(dot2(A0, A1, B0, B1)) - na * nbb) < 1.0E-8)
           bc_velocity(kBcSym, A0, A1, Mp, G, u0, u1);
       } else if (b1 == kBcImposed && b2 == kBcImposed) {
@@ -540,8 +540,8 @@ struct EucCells {
     const bool qfin = (ubits(dt) & kMag) < kHi && (ubits(cmass) & kMag) >= kLo &&
                       is_finite(cmass);
     const double dr2 = (iszero(r2) && qfin) ? from_bits((ubits(dt) ^ ubits(cmass) ^ ubits(r2)) & ~kMag)
-                                            : dt / cmass * r2;
-    const double rhoL = 1 / addz(1 / rho, dr2);
+                                            : div_ip(dt, cmass) * r2;
+    const double rhoL = div_ip(1.0, addz(div_ip(1.0, rho), dr2));
     const double uc0 = v.uc[c], uc1 = v.uc[P + c];
     const double uL0 = addz(uc0, qdiv(mulz(r3a, dt), cmass));
     const double uL1 = addz(uc1, qdiv(mulz(r3b, dt), cmass));
@@ -576,7 +576,7 @@ struct EucCells {
         const bool pz = iszero(pr4[m]) && (ubits(f) & kMag) < kMid && (ubits(dt) & kMag) < kMid &&
                         (ubits(cmm) & kMag) >= kLo && is_finite(cmm);
         const double w = pz ? from_bits((ubits(f) ^ ubits(dt) ^ ubits(cmm) ^ ubits(pr4[m])) & ~kMag)
-                            : f * dt / cmm * pr4[m];
+                            : div_ip(f * dt, cmm) * pr4[m];
         peL[m] = addz(em, w);
       }
     }

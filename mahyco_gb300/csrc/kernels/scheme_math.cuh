@@ -10,6 +10,7 @@
 #define MAHYCO_GB300_SCHEME_MATH_CUH
 
 #include "hydro_gb300.h"
+#include "softfp.cuh"
 
 namespace hydro {
 
@@ -95,10 +96,16 @@ HD double from_ord(unsigned long long o) {
 // around it into an unconditional division, so divisions on paths that are
 // rarely taken cost nothing when they are not taken.
 #ifdef __CUDA_ARCH__
-static __device__ __noinline__ double ddiv_call(double n, double d) { return n / d; }
+static __device__ __noinline__ double ddiv_native(double n, double d) { return n / d; }
 #else
-static inline double ddiv_call(double n, double d) { return n / d; }
+static inline double ddiv_native(double n, double d) { return n / d; }
 #endif
+// n / d, the common case on the integer pipe (softfp.cuh), else the FP64
+// division behind its call.  Bit-identical to n / d for all inputs.
+HD double div_ip(double n, double d) {
+  unsigned long long r;
+  return sfp::div_fast(ubits(n), ubits(d), r) ? from_bits(r) : ddiv_native(n, d);
+}
 
 // n / d with the exact shortcuts decided on the integer pipe:
 //   n = +-0, d finite non-zero   -> zero with sign(n) xor sign(d)
@@ -125,9 +132,45 @@ HD double qdiv(double n, double d) {
       er >= 1 && er <= 0x7fe)
     return from_bits(((nb ^ db) & 0x8000000000000000ull) | ((unsigned long long)er << 52) |
                      (nb & 0xfffffffffffffull));
-  return ddiv_call(n, d);
+  unsigned long long r;
+  return sfp::div_fast(nb, db, r) ? from_bits(r) : ddiv_native(n, d);
 }
 
+
+// IEEE operations with their common case on the integer pipe (softfp.cuh):
+// the fast path when it applies, else the FP64 instruction behind a call
+// (so that the optimizer does not issue it under a predicate for every
+// thread).  Bit-identical to the plain operators for all inputs.
+#ifdef __CUDA_ARCH__
+static __device__ __noinline__ double dmul_call(double a, double b) { return a * b; }
+static __device__ __noinline__ double dadd_call(double a, double b) { return a + b; }
+static __device__ __noinline__ double dsub_call(double a, double b) { return a - b; }
+static __device__ __noinline__ double dsqrt_call(double a) { return sqrt(a); }
+#else
+static inline double dmul_call(double a, double b) { return a * b; }
+static inline double dadd_call(double a, double b) { return a + b; }
+static inline double dsub_call(double a, double b) { return a - b; }
+static inline double dsqrt_call(double a) { return __builtin_sqrt(a); }
+#endif
+HD double mul_ip(double a, double b) {
+  unsigned long long r;
+  return sfp::mul_fast(ubits(a), ubits(b), r) ? from_bits(r) : dmul_call(a, b);
+}
+HD double add_ip(double a, double b) {
+  unsigned long long r;
+  return sfp::add_fast(ubits(a), ubits(b), r) ? from_bits(r) : dadd_call(a, b);
+}
+// a - b: the sum with b's sign flipped on the fast path (which takes no
+// NaN); the fallback is the FP64 subtraction itself
+HD double sub_ip(double a, double b) {
+  unsigned long long r;
+  return sfp::add_fast(ubits(a), ubits(b) ^ 0x8000000000000000ull, r) ? from_bits(r)
+                                                                     : dsub_call(a, b);
+}
+HD double sqrt_ip(double a) {
+  unsigned long long r;
+  return sfp::sqrt_fast(ubits(a), r) ? from_bits(r) : dsqrt_call(a);
+}
 
 // Remap::fluxLimiter (remap/UtilesRemap.cc:9-23)
 HD double flux_limiter(int id, double r) {
@@ -188,18 +231,13 @@ HD double mul_pow2m(double x) {
   return mul_pow2m_call<K>(x);
 }
 // Several numerators over one denominator, each result the IEEE quotient
-// a / b bit for bit.  y = 1 / b is formed once by the IEEE division (so it is
-// the correctly rounded reciprocal); per numerator q0 = a * y is corrected
-// twice with exact residuals, q <- q + (a - b q) y (fused multiply-adds).
-// q0 is within two ulps of a / b, the first correction brings it within one
-// ulp, and then (Markstein's theorem: with y = RN(1/b) and q within one ulp
-// of a / b, RN(q + (a - bq) y) = RN(a / b), the residual a - bq being exact)
-// the second gives the correctly rounded quotient.  The theorem needs no
-// underflow or overflow in any step: operands whose exponents lie outside
-// [-500, 500], zeros, subnormals, infinities and NaNs take the IEEE division.
+// a / b bit for bit: the divisor's integer reciprocal is formed once
+// (softfp.cuh), each quotient then costs one high product and an exact
+// remainder correction on the integer pipe.  Operands or quotients outside
+// the normal range take the IEEE division.
 struct SharedDiv {
-  double b, y;
-  bool ok;
+  double b;
+  sfp::Divisor d;
 };
 HD bool div_safe_exp(double x) {
   const unsigned e = (unsigned)(ubits(x) >> 52) & 0x7ffu;
@@ -208,14 +246,7 @@ HD bool div_safe_exp(double x) {
 HD SharedDiv shared_div(double b) {
   SharedDiv S;
   S.b = b;
-  S.ok = div_safe_exp(b);
-  // the reciprocal of a power of two (within these exponents) is the power
-  // of two with the negated exponent, exactly 1.0 / b
-  const unsigned long long bb = ubits(b);
-  if (S.ok && (bb & 0xfffffffffffffull) == 0)
-    S.y = from_bits((bb & 0x8000000000000000ull) | ((2046ull - ((bb >> 52) & 0x7ffull)) << 52));
-  else
-    S.y = S.ok ? 1.0 / b : 0.0;
+  S.d = sfp::make_divisor(ubits(b));
   return S;
 }
 HD double fma_rn(double a, double b, double c) {
@@ -226,10 +257,8 @@ HD double fma_rn(double a, double b, double c) {
 #endif
 }
 HD double div_shared(const SharedDiv& S, double a) {
-  if (!(S.ok && div_safe_exp(a))) return ddiv_call(a, S.b);
-  const double q0 = a * S.y;
-  const double q1 = fma_rn(fma_rn(-q0, S.b, a), S.y, q0);
-  return fma_rn(fma_rn(-q1, S.b, a), S.y, q1);
+  unsigned long long r;
+  return sfp::div_fast_by(ubits(a), S.d, r) ? from_bits(r) : ddiv_native(a, S.b);
 }
 // A face length as the reference forms it, sqrt(0.0 + a*a + b*b).  For an
 // axis-aligned face (one component exactly zero) it is |a| (or |b|): the
@@ -240,9 +269,9 @@ HD double face_len(double a, double b) {
   if (iszero(a) && iszero(b)) return 0.0;  // sqrt(+0)
   if (iszero(b) && div_safe_exp(a)) return fabs(a);
   if (iszero(a) && div_safe_exp(b)) return fabs(b);
-  double r = a * a;  // 0.0 + a square (never -0) is the square
-  r = r + b * b;
-  return sqrt(r);
+  double r = mul_ip(a, a);  // 0.0 + a square (never -0) is the square
+  r = add_ip(r, mul_ip(b, b));
+  return sqrt_ip(r);
 }
 
 // qdiv's exact shortcuts (0 / d, x / 1, x / x), then div_shared
@@ -356,7 +385,7 @@ HD double norm2(double a, double b) {
   double r = 0.0;
   r = r + a * a;
   r = r + b * b;
-  return sqrt(r);
+  return sqrt_ip(r);
 }
 // Corner normal l+ n+ + l- n- of a node xp between its successor xpp and
 // predecessor xpm in the cell's node order (includes/Freefunctions.h:28-58,
@@ -364,10 +393,10 @@ HD double norm2(double a, double b) {
 HD void lpc_npc(const double* xp, const double* xpp, const double* xpm, double out[2]) {
   const double a0 = 0.5 * (xpp[1] - xp[1]), a1 = 0.5 * (xp[0] - xpp[0]);
   const double la = norm2(a0, a1);
-  const double na0 = a0 / la, na1 = a1 / la;
+  const double na0 = div_ip(a0, la), na1 = div_ip(a1, la);
   const double b0 = 0.5 * (xp[1] - xpm[1]), b1 = 0.5 * (xpm[0] - xp[0]);
   const double lb = norm2(b0, b1);
-  const double nb0 = b0 / lb, nb1 = b1 / lb;
+  const double nb0 = div_ip(b0, lb), nb1 = div_ip(b1, lb);
   out[0] = na0 * la + nb0 * lb;
   out[1] = na1 * la + nb1 * lb;
 }
@@ -405,7 +434,7 @@ HD CellGeom vnr_cell_geometry(const double X[4][2], bool widths) {
     r0 = (k == 0) ? plus_zero(t0) : r0 + t0;
     r1 = (k == 0) ? plus_zero(t1) : r1 + t1;
   }
-  const double sc = 1.0 / (6.0 * vol);
+  const double sc = div_ip(1.0, 6.0 * vol);
   G.xc0 = sc * r0;
   G.xc1 = sc * r1;
   G.hx = G.hy = 0.0;
@@ -443,7 +472,7 @@ HD CellGeom euc_cell_geometry(const double X[4][2], bool widths) {
     r7a = (k == 0) ? plus_zero(ta) : r7a + ta;
     r7b = (k == 0) ? plus_zero(tb) : r7b + tb;
   }
-  const double sc = 1.0 / (6.0 * G.vol);
+  const double sc = div_ip(1.0, 6.0 * G.vol);
   G.xc0 = r7a * sc;
   G.xc1 = r7b * sc;
   G.hx = G.hy = 0.0;
@@ -508,21 +537,21 @@ HD double flux_limiter_pp(int id, double gp, double gm, double yp, double ym,
   } else if (id == HYDRO_LIM_SUPERBEEG) {
     grady = pos(yp - ym) ? smax(fabs(gp), fabs(gm)) : -smax(fabs(gp), fabs(gm));
   } else if (id == HYDRO_LIM_VANLEERG) {
-    double lp = (half(h0) + hp) / (h0 + hp + hm);
-    double lm = (half(h0) + hm) / (h0 + hp + hm);
+    double lp = div_ip(half(h0) + hp, h0 + hp + hm);
+    double lm = div_ip(half(h0) + hm, h0 + hp + hm);
     if (nz(lp * gp + lm * gm))
-      grady = gp * gm / (lp * gp + lm * gm);
+      grady = div_ip(gp * gm, lp * gp + lm * gm);
     else
       grady = 0.;
   } else if (id == HYDRO_LIM_ULTRABEEG) {
-    grady = (yp - ym) / h0;
+    grady = div_ip(yp - ym, h0);
   } else if (id == HYDRO_LIM_ARITHMETICG) {
-    double lp = (half(h0) + hp) / (h0 + hp + hm);
-    double lm = (half(h0) + hm) / (h0 + hp + hm);
+    double lp = div_ip(half(h0) + hp, h0 + hp + hm);
+    double lm = div_ip(half(h0) + hm, h0 + hp + hm);
     grady = lm * gp + lp * gm;
   }
-  double gMp = gp * (h0 + hp) / h0;
-  double gMm = gm * (h0 + hm) / h0;
+  double gMp = div_ip(gp * (h0 + hp), h0);
+  double gMm = div_ip(gm * (h0 + hm), h0);
   double gM = smin(fabs(gMp), fabs(gMm));
   if (pos(yp - ym))
     grady = smin(fabs(gM), fabs(grady));
@@ -630,8 +659,8 @@ HD void compute_y0(int id, double yp, double ym, double h0, double hp,
     y0p = yp;
     y0m = ym;
   } else if (id == HYDRO_LIM_SUPERBEEG || id == HYDRO_LIM_SUPERBEE) {
-    y0p = ((h0 + hm) * yp + h0 * ym) / (dbl(h0) + hm);
-    y0m = ((h0 + hp) * ym + h0 * yp) / (dbl(h0) + hp);
+    y0p = div_ip((h0 + hm) * yp + h0 * ym, dbl(h0) + hm);
+    y0m = div_ip((h0 + hp) * ym + h0 * yp, dbl(h0) + hp);
   } else if (id == HYDRO_LIM_VANLEERG || id == HYDRO_LIM_VANLEER) {
     double a = smin(yp, ym);
     double b = smax(yp, ym);
@@ -639,16 +668,16 @@ HD void compute_y0(int id, double yp, double ym, double h0, double hp,
     double xm = (h0 * h0 + 3 * h0 * hp + 2 * hp * hp) * ym;
     xp += (h0 * h0 - h0 * hp - 2 * hp * hp + 2 * h0 * hm) * ym;
     xm += (h0 * h0 - h0 * hm - 2 * hm * hm + 2 * h0 * hp) * yp;
-    xp /= (2 * h0 * h0 + 5 * h0 * hm + 2 * hm * hm - h0 * hp - 2 * hp * hp);
-    xm /= (2 * h0 * h0 + 5 * h0 * hp + 2 * hp * hp - h0 * hm - 2 * hm * hm);
+    xp = div_ip(xp, 2 * h0 * h0 + 5 * h0 * hm + 2 * hm * hm - h0 * hp - 2 * hp * hp);
+    xm = div_ip(xm, 2 * h0 * h0 + 5 * h0 * hp + 2 * hp * hp - h0 * hm - 2 * hm * hm);
     y0p = smin(smax(xp, a), b);
     y0m = smin(smax(xm, a), b);
   } else if (id == HYDRO_LIM_ULTRABEEG) {
     y0p = half(yp + ym);
     y0m = half(yp + ym);
   } else if (id == HYDRO_LIM_ARITHMETICG) {
-    y0p = ((h0 + hm + hp) * yp + h0 * ym) / (dbl(h0) + hm + hp);
-    y0m = ((h0 + hm + hp) * ym + h0 * yp) / (dbl(h0) + hm + hp);
+    y0p = div_ip((h0 + hm + hp) * yp + h0 * ym, dbl(h0) + hm + hp);
+    y0m = div_ip((h0 + hm + hp) * ym + h0 * yp, dbl(h0) + hm + hp);
   } else if (id == 3000) {
     y0p = yp;
     y0m = ym;
@@ -672,7 +701,7 @@ HD double int2y(double X, double x0, double y0, double x1, double y1) {
     else if (fin && (pos(d) ? dge(n, d) : dle(n, d)))
       eta = 1.;
     else
-      eta = smin(smax(0., ddiv_call(n, d)), 1.);
+      eta = smin(smax(0., div_ip(n, d)), 1.);
     flux = (y0 + half(eta) * (y1 - y0)) * d * eta;
   }
   return flux;
@@ -723,20 +752,20 @@ HD double pp_integral(const PPShape& s, double a, double b, double h0,
 // order-3 face value (remap/UtilesRemap.cc:200-320)
 HD double eval_grad(double hm, double h0, double hp, double ym, double y0,
                     double yp) {
-  return h0 / (hm + h0 + hp) *
-         ((2. * hm + h0) / (h0 + hp) * (yp - y0) +
-          (h0 + 2. * hp) / (hm + h0) * (y0 - ym));
+  return div_ip(h0, hm + h0 + hp) *
+         (div_ip(2. * hm + h0, h0 + hp) * (yp - y0) +
+          div_ip(h0 + 2. * hp, hm + h0) * (y0 - ym));
 }
 HD double eval_ystar(double hmm, double hm, double hp, double hpp, double ymm,
                      double ym, double yp, double ypp, double gradm,
                      double gradp) {
-  double tmp1 = (2. * hp * hm) / (hm + hp) *
-                ((hmm + hm) / (2. * hm + hp) - (hpp + hp) / (2. * hp + hm)) *
+  double tmp1 = div_ip(2. * hp * hm, hm + hp) *
+                (div_ip(hmm + hm, 2. * hm + hp) - div_ip(hpp + hp, 2. * hp + hm)) *
                 (yp - ym);
-  double tmp2 = -hm * (hmm + hm) / (2. * hm + hp) * gradp +
-                hp * (hp + hpp) / (hm + 2. * hp) * gradm;
-  return ym + hm / (hm + hp) * (yp - ym) +
-         1. / (hmm + hm + hp + hpp) * (tmp1 + tmp2);
+  double tmp2 = div_ip(-hm * (hmm + hm), 2. * hm + hp) * gradp +
+                div_ip(hp * (hp + hpp), hm + 2. * hp) * gradm;
+  return ym + div_ip(hm, hm + hp) * (yp - ym) +
+         div_ip(1., hmm + hm + hp + hpp) * (tmp1 + tmp2);
 }
 HD double flux_ordre3(double ymmm, double ymm, double ym, double yp,
                       double ypp, double yppp, double hmmm, double hmm,
@@ -755,14 +784,14 @@ HD double flux_ordre3(double ymmm, double ymm, double ym, double yp,
   double flux;
   if (nonneg(vdt)) {
     double x = vdt, dx = hm;
-    flux = ystar - 0.5 * x / dx * (grad_m - (1. - 2. / 3. * x / dx) * ym6);
+    flux = ystar - div_ip(0.5 * x, dx) * (grad_m - (1. - div_ip(2. / 3. * x, dx)) * ym6);
   } else {
     double x = -vdt, dx = hp;
-    flux = ystar + 0.5 * x / dx * (grad_p - (1. - 2. / 3. * x / dx) * yp6);
+    flux = ystar + div_ip(0.5 * x, dx) * (grad_p - (1. - div_ip(2. / 3. * x, dx)) * yp6);
   }
-  double num = vdt / hm, nup = vdt / hp;
-  double ym_ym = ym + (1. - num) / num * (ym - ymm);
-  double yp_ym = yp - (1. + nup) / nup * (yp - ypp);
+  double num = div_ip(vdt, hm), nup = div_ip(vdt, hp);
+  double ym_ym = ym + div_ip(1. - num, num) * (ym - ymm);
+  double yp_ym = yp - div_ip(1. + nup, nup) * (yp - ypp);
   double i1inf = smin(ym, yp), i1sup = smax(ym, yp), i2inf, i2sup;
   if (nonneg(vdt)) {
     i2inf = smin(ym, ym_ym);
@@ -798,29 +827,29 @@ struct O3Face {
 };
 // eval_grad's coefficients for a cell of width h0 between widths hm, hp
 HD void o3_grad_coef(double hm, double h0, double hp, double& G0, double& A, double& B) {
-  G0 = h0 / (hm + h0 + hp);
-  A = (2. * hm + h0) / (h0 + hp);
-  B = (h0 + 2. * hp) / (hm + h0);
+  G0 = div_ip(h0, hm + h0 + hp);
+  A = div_ip(2. * hm + h0, h0 + hp);
+  B = div_ip(h0 + 2. * hp, hm + h0);
 }
 // eval_ystar's coefficients for a face between widths hm | hp, with the
 // next widths hmm, hpp outside
 HD void o3_ystar_coef(double hmm, double hm, double hp, double hpp, double* T) {
-  T[0] = (2. * hp * hm) / (hm + hp) *
-         ((hmm + hm) / (2. * hm + hp) - (hpp + hp) / (2. * hp + hm));
-  T[1] = -hm * (hmm + hm) / (2. * hm + hp);
-  T[2] = hp * (hp + hpp) / (hm + 2. * hp);
-  T[3] = hm / (hm + hp);
-  T[4] = 1. / (hmm + hm + hp + hpp);
+  T[0] = div_ip(2. * hp * hm, hm + hp) *
+         (div_ip(hmm + hm, 2. * hm + hp) - div_ip(hpp + hp, 2. * hp + hm));
+  T[1] = div_ip(-hm * (hmm + hm), 2. * hm + hp);
+  T[2] = div_ip(hp * (hp + hpp), hm + 2. * hp);
+  T[3] = div_ip(hm, hm + hp);
+  T[4] = div_ip(1., hmm + hm + hp + hpp);
 }
 // the face's coefficients that depend on vdt
 HD void o3_face_dt(O3Face& F, const double* h, double vdt) {
   F.fwd = nonneg(vdt);
   const double x = F.fwd ? vdt : -vdt, dx = F.fwd ? h[2] : h[3];
-  F.Q1 = 0.5 * x / dx;
-  F.Q2 = 2. / 3. * x / dx;
-  const double num = vdt / h[2], nup = vdt / h[3];
-  F.R1 = (1. - num) / num;
-  F.R2 = (1. + nup) / nup;
+  F.Q1 = div_ip(0.5 * x, dx);
+  F.Q2 = div_ip(2. / 3. * x, dx);
+  const double num = div_ip(vdt, h[2]), nup = div_ip(vdt, h[3]);
+  F.R1 = div_ip(1. - num, num);
+  F.R2 = div_ip(1. + nup, nup);
 }
 HD O3Face o3_face(const double* h, double vdt) {
   O3Face F;

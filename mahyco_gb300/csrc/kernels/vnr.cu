@@ -155,8 +155,8 @@ DV double cell_dt(const RunView& v, long long c, int i, int j) {
   double uc = quarter(ld(v.speed, nd[0]));
 #pragma unroll
   for (int k = 1; k < 4; ++k) uc = addz(uc, quarter(ld(v.speed, nd[k])));
-  if (v.projection == 0) return ld(v.cflsq, c) / (0. * uc + v.c[c]);
-  return ld(v.cflsq, c) / addz(uc, v.c[c]);
+  if (v.projection == 0) return div_ip(ld(v.cflsq, c), 0. * uc + v.c[c]);
+  return div_ip(ld(v.cflsq, c), addz(uc, v.c[c]));
 }
 
 // ------------------------------------------------------- Lagrange: nodes
@@ -193,7 +193,7 @@ struct LagNodes {
       auto step = [&](double r) {
         if (s_easy && iszero(r)) return r;
         if (!s_have) {
-          s_val = dt / m;
+          s_val = div_ip(dt, m);
           s_have = true;
         }
         return s_val * r;
@@ -448,11 +448,11 @@ struct LagCells {
         divu_new = 0.0;
         q_new = 0.0;
       } else {
-        irho_old = 1.0 / rho_old;
+        irho_old = div_ip(1.0, rho_old);
         // a density unchanged has the old reciprocal, and the difference of
         // the two is then +0 (x - x, x finite)
         const bool same_rho = ubits(rho_new) == ubits(rho_old) && is_finite(irho_old);
-        irho_new = same_rho ? irho_old : ddiv_call(1.0, rho_new);
+        irho_new = same_rho ? irho_old : div_ip(1.0, rho_new);
         have_irho = true;
         const double tau = half(irho_new + irho_old);
         // qdiv: the density, hence the divergence, is unchanged where the
@@ -460,8 +460,8 @@ struct LagCells {
         divu_new = qdiv(rdt * (same_rho ? 0.0 : irho_new - irho_old), tau);
         if (neg(divu_old)) {
           const double s0 = (v.projection == 0) ? vol_start : ld(v.s0, c);
-          const double sq0 = (v.projection == 0) ? sqrt(vol_start) : ld(v.sqs0, c);
-          q_new = 1.0 / tau *
+          const double sq0 = (v.projection == 0) ? sqrt_ip(vol_start) : ld(v.sqs0, c);
+          q_new = div_ip(1.0, tau) *
                   (-half(sq0) * c_old * divu_new +
                    v.hgs1 * s0 * divu_new * divu_new);
         } else {
@@ -493,12 +493,12 @@ struct LagCells {
             eq_inv = true;  // both 1 / rho_old, finite; not formed
           } else {
             if (!have_irho && (rn_cell || ro_cell)) {
-              irho_old = ddiv_call(1.0, rho_old);
+              irho_old = div_ip(1.0, rho_old);
               irho_new = irho_old;  // rest: rho_new == rho_old
               have_irho = true;
             }
-            irn = rn_cell ? irho_new : ddiv_call(1.0, rn);
-            iro = ro_cell ? irho_old : ddiv_call(1.0, ro);
+            irn = rn_cell ? irho_new : div_ip(1.0, rn);
+            iro = ro_cell ? irho_old : div_ip(1.0, ro);
             eq_inv = ubits(irn) == ubits(iro) && is_finite(irn);
           }
           const double em_old = em_o[m], pm_old = pm_o[m];
@@ -555,13 +555,13 @@ struct LagCells {
         // c_old is sqrt(g0 (g0 - 1) e) of the energy in sarg: the same energy
         // (bit for bit) gives the same root
         cc = (ubits(e_new) == ubits(sarg_old) && !is_nan(e_new)) ? c_old
-                                                                 : sqrt(v.g0gm1 * e_new);
+                                                                 : sqrt_ip(v.g0gm1 * e_new);
         sarg_new = e_new;
       } else {
         for (int m = 0; m < nb; ++m) {
           if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
             const double g = gamma_of(v, m);
-            cm_new[m] = sqrt(g * (g - 1.0) * em_new[m]);
+            cm_new[m] = sqrt_ip(g * (g - 1.0) * em_new[m]);
           }
           cc = smax(cc, cm_new[m]);
         }
@@ -930,12 +930,12 @@ struct SweepGradT {
           for (int m = 1; m < nb; m++) sfv += F[m];
           if (dgt(fabs(sfv), v.threshold)) {
             for (int m = 0; m < nb; m++) {
-              if (!vp) F[nb + m] = (F[nb + m] / sfv) * F[m];
-              F[2 * nb + m] = (F[2 * nb + m] / sfv) * F[nb + m];
+              if (!vp) F[nb + m] = div_ip(F[nb + m], sfv) * F[m];
+              F[2 * nb + m] = div_ip(F[2 * nb + m], sfv) * F[nb + m];
               sfm = (m == 0) ? plus_zero(F[nb + m]) : sfm + F[nb + m];
             }
             if (euc)
-              for (int k = 3 * nb; k < ncomp; ++k) F[k] = (F[k] / sfv) * sfm;
+              for (int k = 3 * nb; k < ncomp; ++k) F[k] = div_ip(F[k], sfv) * sfm;
             else
               F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
           } else {
@@ -1878,13 +1878,13 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   if (pos(rho)) {
     // c_in is sqrt(g0 (g0 - 1) e') of the energy e' in sarg: the same
     // energy (bit for bit) gives the same root
-    cc = (ubits(e) == ubits(sarg_in) && !is_nan(e)) ? c_in : sqrt(v.g0gm1 * e);
+    cc = (ubits(e) == ubits(sarg_in) && !is_nan(e)) ? c_in : sqrt_ip(v.g0gm1 * e);
     sarg_out = e;
   } else {
     MAT_LOOP(m, 0) {
       if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
         const double g = gamma_of(v, m);
-        cm[m] = sqrt(g * (g - 1.0) * emo[m]);
+        cm[m] = sqrt_ip(g * (g - 1.0) * emo[m]);
         v.cm[m * P + c] = cm[m];
       }
       cc = smax(cc, cm[m]);
@@ -1911,7 +1911,7 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     double uc = quarter(spd[0]);
   #pragma unroll
     for (int k = 1; k < 4; ++k) uc = addz(uc, quarter(spd[k]));
-    const double d = cflsq / addz(uc, cc);
+    const double d = div_ip(cflsq, addz(uc, cc));
     if (!is_nan(d)) dtb = ord_bits(d) < dtb ? ord_bits(d) : dtb;
   }
   if (!is_nan(p)) pb = ord_bits(p) > pb ? ord_bits(p) : pb;
@@ -1988,9 +1988,9 @@ struct LagCellsLagrangeOnly {
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const double a = v.u[nd[k]], b = v.u[NP + nd[k]];
-        uc += sqrt(a * a + b * b) * 0.25;
+        uc += sqrt_ip(a * a + b * b) * 0.25;
       }
-      const double d = 0.1 * sqrt(v.vL[c]) / (0. * uc + v.c[c]);
+      const double d = div_ip(0.1 * sqrt_ip(v.vL[c]), 0. * uc + v.c[c]);
       if (v.sans_lagrange == 0 && !is_nan(d)) dtb = ord_bits(d);
       const double p = v.p[c];
       if (!is_nan(p)) pb = ord_bits(p);

@@ -129,10 +129,18 @@ def test_invalid_request_fails_alone(M):
     from mahyco_gb300.workloads import Instance
     good = Instance("sod", 32, 32, 1, "minmod", 10, "Y").spec(M)
     bad = good.copy()
-    bad.projection = 0  # the GPU path needs the remap: rejected at preparation
+    bad.nx = 1  # an invalid mesh: rejected at preparation, on the worker
     a = srv.submit(good)
     b = srv.submit(bad)
     done = drain(srv, 2)
     assert done[a][0] == 0
     assert done[b][0] == -1
+    # a run without the remap is refused at submission (the serving loop
+    # advances runs with the remap), and the loop goes on
+    lag = good.copy()
+    lag.projection = 0
+    with pytest.raises(RuntimeError, match="remap"):
+        srv.submit(lag)
+    c = srv.submit(good)
+    assert drain(srv, 1)[c][0] == 0
     srv.stop()
