@@ -25,15 +25,18 @@
 //    zeros after cancellation, as in the classic guard / round / sticky
 //    adder (e.g. Goldberg, "What every computer scientist should know about
 //    floating-point arithmetic", 1991);
-//  - quotient: a 24-bit FP32 reciprocal estimate, two Newton-Raphson steps
-//    z <- z + z (1 - d z) in 64-bit fixed point, the quotient estimate from
-//    the reciprocal, then the exact remainder n - q d (integer, exact modulo
-//    2^64) corrects the estimate and decides the rounding (no midpoint can
-//    occur for a quotient of two 53-bit significands);
-//  - square root: a 24-bit FP32 reciprocal square root estimate, Newton
-//    steps y <- y (3 - x y^2) / 2 in fixed point, s = x y, and the exact
-//    remainder x - s^2 corrects s and decides the rounding (no midpoint:
-//    (s + 1/2)^2 is never an integer).
+//  - quotient: a 24-bit FP32 reciprocal estimate (rcp.approx), one
+//    Newton-Raphson step z <- z + z (1 - d z) on 32-bit halves and one in
+//    64-bit fixed point, arranged so that the reciprocal never exceeds
+//    1/d (a Newton step on 1/d ends below it from either side); the
+//    quotient estimate from it is the floor or one below, and the exact
+//    remainder n - q d (integer arithmetic modulo 2^64) corrects it and
+//    decides the rounding (no midpoint can occur for a quotient of two
+//    53-bit significands);
+//  - square root: the same with a reciprocal square root estimate
+//    (rsqrt.approx) and steps y <- y + y (1 - x y^2) / 2, s = x y, and the
+//    exact remainder x - s^2 (no midpoint: (s + 1/2)^2 is never an
+//    integer).
 #ifndef MAHYCO_GB300_SOFTFP_CUH
 #define MAHYCO_GB300_SOFTFP_CUH
 
@@ -143,39 +146,44 @@ HD bool add_fast(u64 ab, u64 bb, u64& out) {
 }
 
 // --------------------------------------------------------------- quotient
-// 2^127 / D for D in (2^63, 2^64) (the significand of the divisor shifted
-// left by 11), to within a few units: Z in [2^63, 2^64).
+HD u32 hi32(u64 x) { return (u32)(x >> 32); }
+HD u64 wide(u32 a, u32 b) { return (u64)a * b; }  // one 32 x 32 -> 64 product
+
+// One Newton-Raphson correction in 64-bit fixed point: x + sign(e) *
+// floor(hi32(x) (|e| >> sh) / 2^k) for a signed residual e.
+HD u64 newton_step(u64 x, i64 e, int sh, int k) {
+  const u64 mag = e < 0 ? (u64)(-e) : (u64)e;
+  const u64 corr = wide(hi32(x), (u32)(mag >> sh)) >> k;
+  return e < 0 ? x - corr : x + corr;
+}
+
+// Z ~ 2^127 / D for D in (2^63, 2^64) (the divisor's significand shifted
+// left by 11), never above it and at most ~2^-57 below.
+//  - FP32 estimate of 1 / (t + 1) (t: D's top 24 bits) scaled by
+//    2^87 (1 - 2^-17): below, relative error < 2^-16.8;
+//  - step 1 on the top halves, with the divisor's top word rounded up:
+//    e = 2^63 - (D32 + 1) Z32 > 0, z e / 2^63 ~ Z32 (e >> 16) / 2^15; its
+//    truncations leave |relative error| < 2^-29.8, on either side;
+//  - step 2: e / 2^64 = 2^63 - floor(D Z1 / 2^64) - 1 (signed,
+//    |e| < 2^34), correction z e / 2^63 ~ Z1hi (|e| >> 3) / 2^28.  A step
+//    z <- z (2 - d z) ends below 1/d from either side (1/d - z' =
+//    d (1/d - z)^2); a margin of 32 units covers its truncations.
 HD u64 recip127(u64 D) {
-  // FP32 estimate of 2^87 / (t + 1) with t = D >> 40 (24 bits), an
-  // underestimate of 2^127 / D by at most about 2^-22 relative
   const u32 t = (u32)(D >> 40);
 #ifdef __CUDA_ARCH__
   const float y = __uint_as_float(0x4b000000u | (t & 0x7fffffu)) + 1.0f;  // t + 1, exact
   float rf;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(y));
-  u64 Z = __float2ull_rz(rf * 0x1p87f);  // saturates at 2^64 - 1
+  const u64 Z0 = __float2ull_rz(rf * 0x1.ffffp86f);
 #else
-  const float y = (float)t + 1.0f;
-  const float rf = 1.0f / y;
-  const double zs = (double)rf * 0x1p87;
-  u64 Z = zs >= 0x1p64 ? ~0ull : (u64)zs;
+  const float rf = 1.0f / ((float)t + 1.0f);
+  const u64 Z0 = (u64)(rf * 0x1.ffffp86f);
 #endif
-  if (Z < (1ull << 63)) Z = 1ull << 63;
-  // Newton-Raphson: z <- z + z e / 2^127 with e = 2^127 - D z (signed)
-#pragma unroll
-  for (int it = 0; it < 2; ++it) {
-    const u64 ph = mulhi(D, Z), pl = D * Z;  // D Z = ph 2^64 + pl, near 2^127
-    // e / 2^63, truncated toward minus infinity: (2^127 - D Z) >> 63
-    // = 2^64 - (ph << 1 | pl >> 63) - (low bits != 0 ? 1 : 0), as a signed
-    // 64-bit value (|e| < 2^106 after the FP32 estimate)
-    const u64 p63 = (ph << 1) | (pl >> 63);
-    const u64 lowz = (pl << 1) != 0;
-    const i64 e63 = (i64)(0ull - p63 - lowz);
-    const u64 mag = e63 < 0 ? (u64)(-e63) : (u64)e63;
-    const u64 corr = mulhi(Z, mag);  // Z |e| / 2^127 = Z |e63| / 2^64
-    Z = e63 < 0 ? Z - corr : Z + corr;
-  }
-  return Z;
+  const u32 D32 = hi32(D), Z32 = hi32(Z0);
+  const u64 e1 = (1ull << 63) - (wide(D32, Z32) + Z32);
+  const u64 Z1 = Z0 + (wide(Z32, (u32)(e1 >> 16)) >> 15);
+  const i64 e2 = (i64)((1ull << 63) - mulhi(D, Z1) - 1);
+  return newton_step(Z1, e2, 3, 28) - 32;
 }
 
 // The quotient's significand from N in [mb, 2 mb) (the dividend's
@@ -183,27 +191,17 @@ HD u64 recip127(u64 D) {
 // significand mb in (2^52, 2^53) and Z = recip127(mb << 11):
 // Q = floor(N 2^52 / mb) in [2^52, 2^53), rounded to nearest.
 HD u64 div_significand(u64 N, u64 mb, u64 Z) {
-  // N 2^52 / mb = N 2^63 / D ~ N Z / 2^64
+  // N 2^52 / mb = N 2^63 / D ~ N Z / 2^64, never above: Q is the floor or
+  // one below it (N Z / 2^64 is within 2^54 2^-58 of N 2^63 / D)
   u64 Q = mulhi(N, Z);
-  // exact remainder N 2^52 - Q mb (|R| < 2^63: the arithmetic modulo 2^64
-  // gives it exactly), then at most two correction steps each way
-  i64 R = (i64)((N << 52) - Q * mb);
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    if (R < 0) {
-      --Q;
-      R += (i64)mb;
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    if (R >= (i64)mb) {
-      ++Q;
-      R -= (i64)mb;
-    }
+  // exact remainder N 2^52 - Q mb in [0, 2 mb) (arithmetic modulo 2^64)
+  u64 R = (N << 52) - Q * mb;
+  if (R >= mb) {
+    ++Q;
+    R -= mb;
   }
   // round to nearest: 2R > mb (2R = mb cannot occur)
-  return Q + (u64)((u64)R << 1 > mb);
+  return Q + (u64)((R << 1) > mb);
 }
 
 // A divisor prepared once for several quotients: its bits, significand and
@@ -262,6 +260,39 @@ HD bool div_fast(u64 ab, u64 bb, u64& out) {
 }
 
 // ------------------------------------------------------------ square root
+// Y ~ 2^94 / sqrt(W) for W in [2^62, 2^64): in (2^62, 2^63], never above
+// and at most ~2^-56 below.
+HD u64 rsqrt94(u64 W) {
+  // Y ~ 2^94 / sqrt(W) in (2^62, 2^63], never above and at most ~2^-56
+  // below, as recip127 forms 1 / D, with y <- y + y (1 - W y^2) / 2 (which
+  // also ends below 1 / sqrt(W) from either side: with y = (1 + d) /
+  // sqrt(W), y' = (1 - 3d^2/2 - d^3/2) / sqrt(W)):
+  //  - FP32 estimate from the top 24 bits of W rounded up, scaled by
+  //    2^74 (1 - 2^-17);
+  //  - step 1 on the top halves: Y32^2 / 2^30 ~ 2^94 / W, e = 2^62 -
+  //    (W32 + 1) y2 > 0, y e / 2^63 ~ Y32 (e >> 16) / 2^15 (|relative
+  //    error| < 2^-29 after it);
+  //  - step 2: e / 2^64 = 2^60 - floor(W floor(Y1^2 / 2^64) / 2^64) - 1
+  //    (signed, |e| < 2^32), correction y e / 2^61 ~ Y1hi (|e| >> 2) / 2^27,
+  //    then a margin of 16 units.
+  const u32 t = (u32)(W >> 40);      // [2^22, 2^24)
+  const float wf = (float)(t + 1u);  // exact
+#ifdef __CUDA_ARCH__
+  float rf;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(wf));
+  const u64 Y0 = __float2ull_rz(rf * 0x1.ffffp73f);
+#else
+  const float rf = 1.0f / __builtin_sqrtf(wf);
+  const u64 Y0 = (u64)(rf * 0x1.ffffp73f);
+#endif
+  const u32 W32 = hi32(W), Y32 = hi32(Y0);
+  const u32 y2 = (u32)(wide(Y32, Y32) >> 30);
+  const u64 e1 = (1ull << 62) - (wide(W32, y2) + y2);
+  const u64 Y1 = Y0 + (wide(Y32, (u32)(e1 >> 16)) >> 15);
+  const i64 e2 = (i64)((1ull << 60) - mulhi(W, mulhi(Y1, Y1)) - 1);
+  return newton_step(Y1, e2, 2, 27) - 16;
+}
+
 HD bool sqrt_fast(u64 ab, u64& out) {
   if ((ab << 1) == 0) {  // sqrt(+-0) = +-0
     out = ab;
@@ -278,52 +309,18 @@ HD bool sqrt_fast(u64 ab, u64& out) {
   const u32 E = (ea + 1023u - odd) >> 1;
   // W = M 2^10 in [2^62, 2^64): M 2^52 = W 2^42, sqrt(M 2^52) = sqrt(W) 2^21
   const u64 W = M << 10;
-  // Y ~ 2^94 / sqrt(W) in (2^62, 2^63]: FP32 estimate from the top 24 bits
-  // of W (rounded up, an underestimate by about 2^-22 at most)
-  const u32 t = (u32)(W >> 40);  // [2^22, 2^24)
-  const float wf = (float)(t + 1u);  // exact
-#ifdef __CUDA_ARCH__
-  float rf;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(wf));
-  u64 Y = __float2ull_rz(rf * 0x1p74f);
-#else
-  const float rf = 1.0f / __builtin_sqrtf(wf);
-  u64 Y = (u64)((double)rf * 0x1p74);
-#endif
-  if (Y < (1ull << 62)) Y = 1ull << 62;
-  // Newton-Raphson on 1 / sqrt: y <- y + y e / 2 with e = 1 - W y^2 / 2^188
-#pragma unroll
-  for (int it = 0; it < 2; ++it) {
-    const u64 y2 = mulhi(Y, Y);                // ~ 2^124 / W
-    const u64 ph = mulhi(W, y2), pl = W * y2;  // W y2 ~ 2^124
-    // (2^124 - W y2) >> 60, signed (|.| < 2^45 after the FP32 estimate)
-    const u64 p60 = (ph << 4) | (pl >> 60);
-    const u64 lowz = (pl << 4) != 0;
-    const i64 e60 = (i64)(0ull - p60 - lowz);
-    const u64 mag = e60 < 0 ? (u64)(-e60) : (u64)e60;
-    const u64 corr = mulhi(Y, mag) >> 1;  // Y |e| / 2 = Y |e60| / 2^65
-    Y = e60 < 0 ? Y - corr : Y + corr;
-  }
-  // S ~ sqrt(W) 2^21 = W Y / 2^73, then the exact remainder M 2^52 - S^2
-  // (|.| < 2^63: exact modulo 2^64) corrects S to floor(sqrt(M 2^52))
+  const u64 Y = rsqrt94(W);
+  // S = floor(W Y / 2^73) ~ sqrt(W) 2^21 = sqrt(M 2^52), never above and
+  // at most one below; the exact remainder M 2^52 - S^2 (modulo 2^64)
+  // corrects it
   u64 S = mulhi(W, Y) >> 9;
-  i64 R = (i64)((M << 52) - S * S);
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    if (R < 0) {  // (S - 1)^2 = S^2 - 2S + 1
-      R += (i64)(2 * S - 1);
-      --S;
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    if (R > (i64)(2 * S)) {  // (S + 1)^2 = S^2 + 2S + 1
-      R -= (i64)(2 * S + 1);
-      ++S;
-    }
+  u64 R = (M << 52) - S * S;
+  if (R > 2 * S) {  // (S + 1)^2 = S^2 + 2S + 1
+    R -= 2 * S + 1;
+    ++S;
   }
   // round to nearest: sqrt > S + 1/2  <=>  R > S (R = S + 1/4 is impossible)
-  S += (u64)(R > (i64)S);
+  S += (u64)(R > S);
   out = pack(0, E, S);
   return true;
 }

@@ -67,6 +67,80 @@ static void check(const char* name, int op, u64 a, u64 b, long& fast, long& bad)
   }
 }
 
+// floor(sqrt(x)) of a 128-bit integer, exactly
+static unsigned __int128 isqrt128(unsigned __int128 x) {
+  unsigned __int128 r = (unsigned __int128)std::sqrt((long double)x);
+  while (r * r > x) --r;
+  while ((r + 1) * (r + 1) <= x) ++r;
+  return r;
+}
+
+// The estimates behind the quotient and the square root: for a divisor
+// significand mb, Q = mulhi(N, recip127(mb << 11)) must be floor(N 2^52 /
+// mb) or one below (never above); for M in [2^52, 2^54),
+// S = mulhi(W, rsqrt94(W)) >> 9 with W = M 2^10 must be floor(sqrt(M 2^52))
+// or one below.  Divisors and radicands at the ends of their ranges and of
+// the 24-bit estimate's steps, then random ones.
+static long check_estimates() {
+  long bad = 0, n = 0;
+  auto qcheck = [&](u64 mb, u64 N) {
+    const u64 Q = mulhi(N, recip127(mb << 11));
+    const u64 Qt = (u64)(((unsigned __int128)N << 52) / mb);
+    ++n;
+    if (Q > Qt || Qt - Q > 1) {
+      if (bad++ < 5) std::printf("quotient estimate: mb %llx N %llx Q %llx floor %llx\n", mb, N, Q, Qt);
+    }
+  };
+  auto scheck = [&](u64 M) {
+    const u64 W = M << 10;
+    const u64 S = mulhi(W, rsqrt94(W)) >> 9;
+    const u64 St = (u64)isqrt128((unsigned __int128)M << 52);
+    ++n;
+    if (S > St || St - S > 1) {
+      if (bad++ < 5) std::printf("root estimate: M %llx S %llx floor %llx\n", M, S, St);
+    }
+  };
+  std::vector<u64> mbs;
+  for (u64 k = 1; k < 3000; ++k) {
+    mbs.push_back(kHidden + k);
+    mbs.push_back((kHidden << 1) - k);
+  }
+  for (int k = 0; k < 20000; ++k) {  // the 24-bit steps of the FP32 estimate
+    const u64 top = (rng() & ((1ull << 23) - 1)) | (1ull << 23);
+    const u64 low = (rng() & 1) ? 0 : ((1ull << 29) - 1);
+    mbs.push_back((top << 29) | (low ^ (rng() & 7)));
+  }
+  for (int k = 0; k < 300000; ++k) mbs.push_back(kHidden | (rng() & kFracMask));
+  for (u64 mb : mbs) {
+    if (mb <= kHidden) continue;
+    qcheck(mb, mb);
+    qcheck(mb, 2 * mb - 1);
+    qcheck(mb, kHidden | (rng() & kFracMask) | ((u64)(rng() & 1) << 52));
+    const u64 Nr = mb + rng() % mb;
+    qcheck(mb, Nr);
+  }
+  std::vector<u64> ms;
+  for (u64 k = 0; k < 3000; ++k) {
+    ms.push_back(kHidden + k);
+    ms.push_back((kHidden << 2) - 1 - k);
+    ms.push_back((kHidden << 1) + k);
+    ms.push_back((kHidden << 1) - 1 - k);
+  }
+  for (int k = 0; k < 400000; ++k)
+    ms.push_back(kHidden + rng() % (3 * kHidden));
+  for (int k = 0; k < 20000; ++k) {  // perfect squares and their neighbours
+    const u64 r = (1ull << 52) + rng() % (1ull << 52);
+    const unsigned __int128 sq = (unsigned __int128)r * r;
+    if ((sq & ((1ull << 52) - 1)) == 0) ms.push_back((u64)(sq >> 52));
+    ms.push_back((u64)(sq >> 52));
+    ms.push_back((u64)(sq >> 52) + 1);
+  }
+  for (u64 M : ms)
+    if (M >= kHidden && M < (kHidden << 2)) scheck(M);
+  std::printf("estimates: %ld checked, %ld outside [floor - 1, floor]\n", n, bad);
+  return bad;
+}
+
 int main() {
   const char* names[5] = {"mul", "add", "div", "sqrt", "div_by"};
   // structured edge values
@@ -101,6 +175,7 @@ int main() {
     std::printf("%s: %ld of %ld on the fast path, %ld mismatches\n", names[op], fast, tot, bad);
     bad_total += bad;
   }
+  bad_total += check_estimates();
   std::printf("softfp: %ld mismatches\n", bad_total);
   return bad_total ? 1 : 0;
 }
