@@ -106,6 +106,13 @@ HD double div_ip(double n, double d) {
   unsigned long long r;
   return sfp::div_fast(ubits(n), ubits(d), r) ? from_bits(r) : ddiv_native(n, d);
 }
+// div_ip behind a call, for a division on a path that most threads skip
+// (the ~90 instructions are then not inlined at each use)
+#ifdef __CUDA_ARCH__
+static __device__ __noinline__ double div_ip_call(double n, double d) { return div_ip(n, d); }
+#else
+static inline double div_ip_call(double n, double d) { return div_ip(n, d); }
+#endif
 
 // n / d with the exact shortcuts decided on the integer pipe:
 //   n = +-0, d finite non-zero   -> zero with sign(n) xor sign(d)

@@ -193,7 +193,7 @@ struct LagNodes {
       auto step = [&](double r) {
         if (s_easy && iszero(r)) return r;
         if (!s_have) {
-          s_val = div_ip(dt, m);
+          s_val = div_ip_call(dt, m);
           s_have = true;
         }
         return s_val * r;

@@ -93,6 +93,12 @@ def summarize(capture: dict[str, list[dict]], mesh: int) -> dict:
             "warp_inst_per_unit": round(tot("sm__inst_executed.sum") / n / units, 2),
             "units": units,
         }
+        # pipe and issue utilisation, when the capture has them
+        for key, metric in (("alu_pipe_pct", "sm__pipe_alu_cycles_active.avg.pct_of_peak_sustained_active"),
+                            ("fma_pipe_pct", "sm__pipe_fma_cycles_active.avg.pct_of_peak_sustained_active"),
+                            ("issue_pct", "sm__inst_issued.avg.pct_of_peak_sustained_active")):
+            if any(metric in l for l in ls):
+                res[k][key] = round(tot(metric) / n, 1)
     return res
 
 
@@ -114,7 +120,8 @@ def main() -> None:
         "command_developed": a.command_developed,
         "note": "per launch, divided by the launch's units (cells, or nodes for node "
                 "kernels); FP64 flops = dadd + dmul + 2*dfma thread instructions; "
-                "FP64-pipe inst = 32 x sm__inst_executed_pipe_fp64; times are ncu's "
+                "FP64-pipe inst = 32 x sm__inst_executed_pipe_fp64; alu / fma / issue: "
+                "percent of peak sustained (active cycles); times are ncu's "
                 "serialized cold-cache launches",
         "kernels": summarize(read_capture(a.early), a.mesh),
         "developed": summarize(read_capture(a.developed), a.mesh),
