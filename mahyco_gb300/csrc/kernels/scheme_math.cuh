@@ -106,13 +106,6 @@ HD double div_ip(double n, double d) {
   unsigned long long r;
   return sfp::div_fast(ubits(n), ubits(d), r) ? from_bits(r) : ddiv_native(n, d);
 }
-// div_ip behind a call, for a division on a path that most threads skip
-// (the ~90 instructions are then not inlined at each use)
-#ifdef __CUDA_ARCH__
-static __device__ __noinline__ double div_ip_call(double n, double d) { return div_ip(n, d); }
-#else
-static inline double div_ip_call(double n, double d) { return div_ip(n, d); }
-#endif
 
 // n / d with the exact shortcuts decided on the integer pipe:
 //   n = +-0, d finite non-zero   -> zero with sign(n) xor sign(d)
@@ -499,7 +492,7 @@ HD CellGeom euc_cell_geometry(const double X[4][2], bool widths) {
 HD double mul_pm1(double x, double n) {
   const unsigned long long b = ubits(n);
   if (b == 0x3ff0000000000000ull) return x;
-  if (b == 0xbff0000000000000ull) return -x;
+  if (b == 0xbff0000000000000ull) return from_bits(ubits(x) ^ 0x8000000000000000ull);
   return x * n;
 }
 

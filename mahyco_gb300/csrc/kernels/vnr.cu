@@ -193,7 +193,7 @@ struct LagNodes {
       auto step = [&](double r) {
         if (s_easy && iszero(r)) return r;
         if (!s_have) {
-          s_val = div_ip_call(dt, m);
+          s_val = div_ip(dt, m);
           s_have = true;
         }
         return s_val * r;
@@ -1358,10 +1358,41 @@ struct SweepUpdateT {
     const bool dual_share = v.scheme != HYDRO_SCHEME_EUCCLHYD && v.dual_method != 2;
     const double rl = (dual_share && v.dual_method == 1) ? v.rL[c] : 0.;
     const double vl = (sweep == 1 && v.pb != 1) ? v.vL[c] : 0.;
+    // Both faces with integral planes flagged all +0.0 (PenteBorne face
+    // values formed here, each +0 - +0 = +0), finite coefficients, normals
+    // and rL, no boundary flux, no NaN input: every flux is the zero of
+    // sign(coef), each component keeps its value and each mass-flux share
+    // is a signed zero.  The whole cell takes one branch without FP64
+    // instructions (the cell at rest); decided per value, the branches are
+    // if-converted into FP64 instructions that run anyway.
+    // (the still paths form the mass-flux shares' signed zeros from the sign
+    // bits: they need finite coefficients, normals and rL)
+    const bool still_ok = cfin && is_finite(rl) && is_finite(nrm[0]) && is_finite(nrm[1]);
+    bool zface = form && still_ok && bcf == 0 && (!has[0] || (lf[0].zv && lf[0].zr)) &&
+                 (!has[1] || (lf[1].zv && lf[1].zr));
+    if (zface) {
+  #pragma unroll
+      for (int k = 0; k < kMaxComp; ++k) {
+        if (k >= ncomp) break;
+        U[k] = Uin[k * P + c];
+        zface = zface && !is_nan(U[k]);
+      }
+    }
+    if (zface && dual_share) {
+      // F = coef * (+0): the zero of sign(coef) (+0 for a missing face);
+      // times the normal: its sign xor the normal's; the two summed: -0
+      // only when both are -0
+      constexpr unsigned long long kS = 0x8000000000000000ull;
+      const unsigned long long s0 = ((has[0] ? ubits(coef[0]) : 0ull) ^ ubits(nrm[0])) & kS;
+      const unsigned long long s1 = ((has[1] ? ubits(coef[1]) : 0ull) ^ ubits(nrm[1])) & kS;
+      unsigned long long w = s0 & s1;
+      if (v.dual_method == 1) w ^= ubits(rl) & kS;
+      for (int m = 0; m < nb; ++m) v.FFd[m * P + c] = from_bits(w);
+    }
     // components four at a time: the loads of a group are issued together,
     // ahead of the group's stores (which would otherwise order each
     // component's loads behind the previous component's stores)
-    for (int k0 = 0; k0 < ncomp; k0 += 4) {
+    for (int k0 = 0; k0 < (zface ? 0 : ncomp); k0 += 4) {
       double qa[4], qb[4], ui[4];
   #pragma unroll
       for (int t = 0; t < 4; ++t) {
@@ -1379,7 +1410,7 @@ struct SweepUpdateT {
       // with a zero coefficient): each component keeps its value (see
       // below), decided once so that the arithmetic is branched over rather
       // than issued under a predicate
-      bool group_still = cfin;
+      bool group_still = still_ok;
   #pragma unroll
       for (int t = 0; t < 4; ++t)
         if (k0 + t < ncomp)
@@ -1392,13 +1423,17 @@ struct SweepUpdateT {
           if (k >= ncomp) break;
           U[k] = ui[t];
           if (dual_share && k >= doff && k < doff + nb) {
-            // the signed-zero fluxes times the normals, summed: -0 only when
-            // both terms are -0
-            const double F0 = has[0] ? from_bits((ubits(coef[0]) ^ ubits(qa[t])) & ~kMag) : 0.;
-            const double F1 = has[1] ? from_bits((ubits(coef[1]) ^ ubits(qb[t])) & ~kMag) : 0.;
-            double w = from_bits(ubits(mul_pm1(F0, nrm[0])) & ubits(mul_pm1(F1, nrm[1])));
-            if (v.dual_method == 1) w = rl * w;
-            v.FFd[(k - doff) * P + c] = w;
+            // the signed-zero fluxes (+0 for a missing face) times the
+            // finite normals: sign xor sign; summed: -0 only when both terms
+            // are -0; times the finite rL: sign xor sign again
+            constexpr unsigned long long kS = 0x8000000000000000ull;
+            const unsigned long long s0 =
+                ((has[0] ? ubits(coef[0]) ^ ubits(qa[t]) : 0ull) ^ ubits(nrm[0])) & kS;
+            const unsigned long long s1 =
+                ((has[1] ? ubits(coef[1]) ^ ubits(qb[t]) : 0ull) ^ ubits(nrm[1])) & kS;
+            unsigned long long w = s0 & s1;
+            if (v.dual_method == 1) w ^= ubits(rl) & kS;
+            v.FFd[(k - doff) * P + c] = from_bits(w);
           }
         }
         continue;
@@ -1749,6 +1784,94 @@ struct DualUpdate {
 // index stay in registers instead of local memory); iterations m >= nbmat do
 // nothing
 #define MAT_LOOP(m, first) _Pragma("unroll") for (int m = (first); m < 3; ++m) if (m < nb)
+
+// final_cell for a cell that holds one material p: the other materials'
+// volume, mass and energy are +0.0 (bits), p's volume and mass are positive,
+// every material is a perfect gas, the threshold lies in [0, 1), and (for
+// the time step) the four node speeds are +0.0.  The general path then
+// reduces exactly to: volt = vn_p, masset = Um_p (x + +0 = x), rv = vol /
+// vn_p, vn_p' = vn_p * rv and the others +0 * rv = +0 (rv > 0), f = 1 and +0
+// (x / x = 1, +0 / x = +0, neither moved by the threshold), mf likewise,
+// rho = 0.0 + Um_p / vn_p', e = 0.0 + Ue_p / Um_p, p = 0.0 + pm_p with pm_p
+// = (g_p - 1) rho_p e_p, the others' pm = ((g_m - 1) * +0) * +0 (the zero
+// of sign(g_m - 1)), cmassm = cmass and the zero of sign(cmass), and the
+// time-step denominator 0.0 + c.  The few products and quotients that
+// remain are the reference's; a value that leaves these ranges (a negative
+// density or energy, a NaN, a non-finite product) returns false before any
+// store, and the general path runs.  One branch for the whole cell: decided
+// per value inside the general path, the shortcuts are if-converted into
+// FP64 instructions that run anyway.
+__device__ __forceinline__ bool final_single(const RunView& v, Ctrl& C, long long c, int nb,
+                                             double thr, double vol, const double* vn,
+                                             const double* Um, const double* Ue, double Uq,
+                                             double c_in, double sarg_in, const double* spd,
+                                             double cflsq, unsigned long long& dtb,
+                                             unsigned long long& pb) {
+  constexpr unsigned long long kS = 0x8000000000000000ull;
+  int p = -1, nonzero = 0;
+  bool ok = nonneg(thr) && dlt(thr, 1.0);
+  MAT_LOOP(m, 0) {
+    const bool z = (ubits(vn[m]) | ubits(Um[m]) | ubits(Ue[m])) == 0ull;
+    if (!z) {
+      p = m;
+      ++nonzero;
+    }
+    ok = ok && eos_of(v, m) == HYDRO_EOS_PERFECT_GAS && is_finite(gm1_of(v, m));
+  }
+  if (v.sans_lagrange == 0)
+    ok = ok && (ubits(spd[0]) | ubits(spd[1]) | ubits(spd[2]) | ubits(spd[3])) == 0ull;
+  if (!ok || nonzero != 1) return false;
+  // p's values by select over the unrolled materials (an index held in a
+  // register would put the arrays in local memory)
+  double vnp0 = 0., ump = 0., uep = 0.;
+  MAT_LOOP(m, 0) {
+    if (m == p) {
+      vnp0 = vn[m];
+      ump = Um[m];
+      uep = Ue[m];
+    }
+  }
+  if (!(pos(vnp0) && is_finite(vnp0) && pos(ump) && is_finite(ump))) return false;
+  const double rv = qdiv(vol, vnp0);
+  if (!(pos(rv) && is_finite(rv))) return false;
+  const double vnp = mul1z(vnp0, rv);
+  if (!(pos(vnp) && is_finite(vnp))) return false;
+  const double dmp = qdiv(ump, vnp), emp = qdiv(uep, ump);
+  if (neg(dmp) || neg(emp) || is_nan(dmp) || is_nan(emp)) return false;
+  const double rho = plus_zero(dmp), e = plus_zero(emp);
+  if (!pos(rho)) return false;
+  const double cmass = v.euler_volume * rho;
+  if (!is_finite(cmass)) return false;
+  const double pmp = (gm1_of(v, p) * dmp) * emp;
+  const double pres = plus_zero(pmp);
+  // the state, as the general path stores it
+  const long long P = v.pitch;
+  v.mixte[c] = 0;
+  v.pure[c] = p;
+  v.cell_mass[c] = cmass;
+  v.q[c] = qdiv(Uq, vol);
+  const double cc = (ubits(e) == ubits(sarg_in)) ? c_in : sqrt_ip(v.g0gm1 * e);
+  v.rho[c] = rho;
+  v.e[c] = e;
+  v.p[c] = pres;
+  v.c[c] = cc;
+  v.sarg[c] = e;
+  MAT_LOOP(m, 0) {
+    const bool here = m == p;
+    v.cmassm[m * P + c] = here ? cmass : from_bits(ubits(cmass) & kS);
+    v.fm[m * P + c] = here ? 1.0 : 0.0;
+    v.mfm[m * P + c] = here ? 1.0 : 0.0;
+    v.rhom[m * P + c] = here ? dmp : 0.0;
+    v.em[m * P + c] = here ? emp : 0.0;
+    v.pm[m * P + c] = here ? pmp : from_bits(ubits(gm1_of(v, m)) & kS);
+  }
+  if (v.sans_lagrange == 0) {
+    const double d = div_ip(cflsq, plus_zero(cc));
+    if (!is_nan(d)) dtb = ord_bits(d) < dtb ? ord_bits(d) : dtb;
+  }
+  if (!is_nan(pres)) pb = ord_bits(pres) > pb ? ord_bits(pres) : pb;
+  return true;
+}
 __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
                                            int j, unsigned long long& dtb,
                                            unsigned long long& pb) {
@@ -1781,6 +1904,8 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
     spd[3] = ld(v.speed, n0 + v.nx + 1);
     cflsq = ld(v.cflsq, c);
   }
+  if (final_single(v, C, c, nb, thr, vol, vn, Um, Ue, Uq, c_in, sarg_in, spd, cflsq, dtb, pb))
+    return;
   // every sum below starts from 0.0 in the reference: its first addition
   // 0.0 + x is plus_zero(x), on the integer pipe (materials 0 .. nb-1, nb >= 1)
   double volt = plus_zero(vn[0]), masset = plus_zero(Um[0]);
@@ -2034,11 +2159,11 @@ __global__ void __launch_bounds__(kBX* kBY, 8) k_sweep_grad_pb(RunView v, int sw
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFaceT<2>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdateT<0>{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY) k_sweep_update_f(RunView v, int sweep) { plain_items(v, SweepUpdateT<1>{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY, 7) k_sweep_update_f(RunView v, int sweep) { plain_items(v, SweepUpdateT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
 // ten resident blocks: where nodes are quiet the kernel waits on memory
 __global__ void __launch_bounds__(kBX* kBY, 10) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY, 8) k_final(RunView v) { plain_items(v, Final{}); }
+__global__ void __launch_bounds__(kBX* kBY, 7) k_final(RunView v) { plain_items(v, Final{}); }
 
 // Batched launches: a persistent grid walks the tile table; every thread of
 // a block works on the same tile (the final phase's block reduction relies
