@@ -544,8 +544,9 @@ struct LagCells {
           em_new[m] = v.em[m * P + c];
         }
       }
-      for (int m = 0; m < nb; ++m)
-        if (eos_of(v, m) == HYDRO_EOS_VOID) e_new = 0.;
+  #pragma unroll
+      for (int m = 0; m < 3; ++m)
+        if (m < nb && eos_of(v, m) == HYDRO_EOS_VOID) e_new = 0.;
       // computePressionMoyenne: max of the in-place c and the materials'
       // sound speeds, replaced by the mixture's when rho > 0 (then the
       // materials' values are not needed)
@@ -558,7 +559,9 @@ struct LagCells {
                                                                  : sqrt_ip(v.g0gm1 * e_new);
         sarg_new = e_new;
       } else {
-        for (int m = 0; m < nb; ++m) {
+  #pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          if (m >= nb) break;
           if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
             const double g = gamma_of(v, m);
             cm_new[m] = sqrt_ip(g * (g - 1.0) * em_new[m]);
@@ -566,8 +569,9 @@ struct LagCells {
           cc = smax(cc, cm_new[m]);
         }
       }
-      for (int m = 0; m < nb; ++m)
-        if (eos_of(v, m) == HYDRO_EOS_VOID) e_new += mf[m] * em_new[m];
+  #pragma unroll
+      for (int m = 0; m < 3; ++m)
+        if (m < nb && eos_of(v, m) == HYDRO_EOS_VOID) e_new += mf[m] * em_new[m];
       v.c[c] = cc;
       v.sarg[c] = sarg_new;
       if (v.projection == 0) {
@@ -577,7 +581,9 @@ struct LagCells {
         // keeps its pressure) and computePressionMoyenne (the sum from 0.0
         // of f p) are stored here (PhaseLagrange.cc:392-485)
         double pmean = 0.;
-        for (int m = 0; m < nb; ++m) {
+  #pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          if (m >= nb) break;
           const double pmm = (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS)
                                  ? gm1_of(v, m) * rhom_new[m] * em_new[m]
                                  : pm_o[m];
@@ -600,31 +606,50 @@ struct LagCells {
       // initial density of the row's first cell
       if (v.periodic_x && (j == v.nx - 1 || j == 0)) rho_new = ld(v.rho0_left, i);
     }
-    // ---- PrepareRemap (cell part)
-    const int ncomp = v.ncomp;
-    double U[kMaxComp];
+    // ---- PrepareRemap (cell part): the conserved values per material
+    // (volume, mass, energy; indexes known at compile time, so they stay in
+    // registers) and the pseudo-viscosity slot 3 nbmat
+    double uv[3], um[3], ue[3];
   #pragma unroll
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
-      U[m] = mul_frac(f[m], vol);
+      uv[m] = mul_frac(f[m], vol);
       const double mv = mul_frac(mf[m], vol);  // (mf * vol) * rho_new ...
-      U[nb + m] = mulz(mv, rho_new);
-      U[2 * nb + m] = mulz(mulz(mv, rho_new), e_new);
+      um[m] = mulz(mv, rho_new);
+      ue[m] = mulz(mulz(mv, rho_new), e_new);
     }
-    U[3 * nb] = mulz(q_new, vol);  // reference slot 3*nbmat+3
-    for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
+    const double uq = mulz(q_new, vol);  // reference slot 3*nbmat+3
+  #pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nb) break;
+      v.UL[m * P + c] = uv[m];
+      v.UL[(nb + m) * P + c] = um[m];
+      v.UL[(2 * nb + m) * P + c] = ue[m];
+    }
+    v.UL[3 * nb * P + c] = uq;
     if (v.pb == 1) {
-      double sv = plus_zero(U[0]);
-      for (int m = 1; m < nb; ++m) sv = addz(sv, U[m]);
-      for (int m = 0; m < nb; ++m) {
-        v.Phi[m * P + c] = qdiv(U[m], sv);
-        v.Phi[(nb + m) * P + c] = nz(U[m]) ? qdiv(U[nb + m], U[m]) : 0.;
-        v.Phi[(2 * nb + m) * P + c] = nz(U[nb + m]) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
+      double sv = plus_zero(uv[0]);
+  #pragma unroll
+      for (int m = 1; m < 3; ++m)
+        if (m < nb) sv = addz(sv, uv[m]);
+  #pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        v.Phi[m * P + c] = qdiv(uv[m], sv);
+        v.Phi[(nb + m) * P + c] = nz(uv[m]) ? qdiv(um[m], uv[m]) : 0.;
+        v.Phi[(2 * nb + m) * P + c] = nz(um[m]) ? qdiv(ue[m], um[m]) : 0.;
       }
       v.Phi[3 * nb * P + c] = q_new;
     } else {
-      const SharedDiv Sv = shared_div(vol);  // one denominator, ncomp quotients
-      for (int k = 0; k < ncomp; ++k) v.Phi[k * P + c] = qdiv_shared(Sv, U[k]);
+      const SharedDiv Sv = shared_div(vol);  // one denominator, 3 nbmat + 1 quotients
+  #pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        if (m >= nb) break;
+        v.Phi[m * P + c] = qdiv_shared(Sv, uv[m]);
+        v.Phi[(nb + m) * P + c] = qdiv_shared(Sv, um[m]);
+        v.Phi[(2 * nb + m) * P + c] = qdiv_shared(Sv, ue[m]);
+      }
+      v.Phi[3 * nb * P + c] = qdiv_shared(Sv, uq);
     }
     v.vL[c] = vol;
     v.rL[c] = rho_new;
@@ -2146,7 +2171,7 @@ __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
 }
 
 __global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
-__global__ void __launch_bounds__(kBX* kBY, 6) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
+__global__ void __launch_bounds__(kBX* kBY, 7) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_lag_cells_lo(RunView v) { plain_items(v, LagCellsLagrangeOnly{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_next_positions(RunView v) { plain_items(v, NextPositions{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { plain_items(v, FaceGrad{sweep}); }
