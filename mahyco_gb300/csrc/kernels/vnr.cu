@@ -2171,7 +2171,7 @@ __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
 }
 
 __global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
-__global__ void __launch_bounds__(kBX* kBY, 7) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
+__global__ void __launch_bounds__(kBX* kBY, 8) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_lag_cells_lo(RunView v) { plain_items(v, LagCellsLagrangeOnly{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_next_positions(RunView v) { plain_items(v, NextPositions{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_face_grad(RunView v, int sweep) { plain_items(v, FaceGrad{sweep}); }
