@@ -2170,7 +2170,7 @@ __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
   f(v, blockIdx.y * kBY + threadIdx.y, blockIdx.x * kBX + threadIdx.x);
 }
 
-__global__ void __launch_bounds__(kBX* kBY) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
+__global__ void __launch_bounds__(kBX* kBY, 10) k_lag_nodes(RunView v) { plain_items(v, LagNodes{}); }
 __global__ void __launch_bounds__(kBX* kBY, 8) k_lag_cells(RunView v) { plain_items(v, LagCells{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_lag_cells_lo(RunView v) { plain_items(v, LagCellsLagrangeOnly{}); }
 __global__ void __launch_bounds__(kBX* kBY) k_next_positions(RunView v) { plain_items(v, NextPositions{}); }
@@ -2184,11 +2184,11 @@ __global__ void __launch_bounds__(kBX* kBY, 8) k_sweep_grad_pb(RunView v, int sw
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFaceT<2>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdateT<0>{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY, 7) k_sweep_update_f(RunView v, int sweep) { plain_items(v, SweepUpdateT<1>{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY, 9) k_sweep_update_f(RunView v, int sweep) { plain_items(v, SweepUpdateT<1>{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY, 10) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
 // ten resident blocks: where nodes are quiet the kernel waits on memory
-__global__ void __launch_bounds__(kBX* kBY, 10) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY, 7) k_final(RunView v) { plain_items(v, Final{}); }
+__global__ void __launch_bounds__(kBX* kBY, 12) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY, 8) k_final(RunView v) { plain_items(v, Final{}); }
 
 // Batched launches: a persistent grid walks the tile table; every thread of
 // a block works on the same tile (the final phase's block reduction relies
@@ -2217,16 +2217,16 @@ __device__ __forceinline__ void batch_items(const BatchArgs& b, const F& f) {
   }
 }
 
-__global__ void __launch_bounds__(kBatchThreads) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 10) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads) kb_final(BatchArgs b) { batch_items(b, Final{}); }
+__global__ void __launch_bounds__(kBatchThreads, 9) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 10) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 12) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_final(BatchArgs b) { batch_items(b, Final{}); }
 
 // One thread per run: cycle start (begin + reduction reset) and cycle end.
 __global__ void kb_begin(const RunView* views, const int* ninst) {
