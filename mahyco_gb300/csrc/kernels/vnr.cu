@@ -2219,7 +2219,7 @@ __device__ __forceinline__ void batch_items(const BatchArgs& b, const F& f) {
 
 __global__ void __launch_bounds__(kBatchThreads, 10) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
 __global__ void __launch_bounds__(kBatchThreads, 8) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
-__global__ void __launch_bounds__(kBatchThreads, 8) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
