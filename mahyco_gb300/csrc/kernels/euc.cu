@@ -786,10 +786,10 @@ __device__ __forceinline__ void plain_items(const RunView& v, const F& f) {
   f(v, blockIdx.y * kBY + threadIdx.y, blockIdx.x * kBX + threadIdx.x);
 }
 
-__global__ void __launch_bounds__(kBX* kBY) ke_cell_pre(RunView v) { plain_items(v, EucCellPre{}); }
-__global__ void __launch_bounds__(kBX* kBY) ke_nodes(RunView v) { plain_items(v, EucNodes{}); }
-__global__ void __launch_bounds__(kBX* kBY) ke_cells(RunView v) { plain_items(v, EucCells{}); }
-__global__ void __launch_bounds__(kBX* kBY) ke_final(RunView v) { plain_items(v, EucFinal{}); }
+__global__ void __launch_bounds__(kBX* kBY, 12) ke_cell_pre(RunView v) { plain_items(v, EucCellPre{}); }
+__global__ void __launch_bounds__(kBX* kBY, 8) ke_nodes(RunView v) { plain_items(v, EucNodes{}); }
+__global__ void __launch_bounds__(kBX* kBY, 8) ke_cells(RunView v) { plain_items(v, EucCells{}); }
+__global__ void __launch_bounds__(kBX* kBY, 10) ke_final(RunView v) { plain_items(v, EucFinal{}); }
 
 }  // namespace
 

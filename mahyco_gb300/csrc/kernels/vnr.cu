@@ -2182,7 +2182,7 @@ __global__ void __launch_bounds__(kBX* kBY) k_sweep_grad(RunView v, int sweep) {
 // at rest; measured faster than the register-limited four to six
 __global__ void __launch_bounds__(kBX* kBY, 8) k_sweep_grad_pb(RunView v, int sweep) { plain_items(v, SweepGradT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) { plain_items(v, SweepFaceT<2>{sweep}); }
-__global__ void __launch_bounds__(kBX* kBY) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
+__global__ void __launch_bounds__(kBX* kBY, 4) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdateT<0>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY, 9) k_sweep_update_f(RunView v, int sweep) { plain_items(v, SweepUpdateT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY, 10) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
