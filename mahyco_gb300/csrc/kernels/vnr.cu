@@ -353,6 +353,20 @@ struct LagNodes {
 // then computeVariablesForRemap / computeCellQuantitesForRemap
 // (vnr_remap/PrepareRemap.cc:65-176) and the Lagrangian face lengths that
 // give HvLagrange (remap/PhaseRemap1.cc:57-71, 104-119).
+// e + sum over the Void materials of mf * em (computePressionMoyenne's
+// last loop, vnr_remap/PhaseLagrange.cc:480-483), behind a call:
+// the runs without a Void material skip it whole (inline, the products and
+// sums of the unrolled material loop would be if-converted into FP64
+// instructions that run for every cell)
+static __device__ __noinline__ double void_energy(unsigned mask, double e, double mf0,
+                                                  double mf1, double mf2, double em0,
+                                                  double em1, double em2) {
+  if (mask & 1u) e += mf0 * em0;
+  if (mask & 2u) e += mf1 * em1;
+  if (mask & 4u) e += mf2 * em2;
+  return e;
+}
+
 struct LagCells {
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
     Ctrl& C = *v.ctrl;
@@ -399,7 +413,7 @@ struct LagCells {
     const double vol = G.vol;
     const int nb = v.nbmat;
     const double thr = v.threshold;
-    double f[3], mf[3], rhom_new[3], rho_o[3], em_o[3], pm_o[3], qm_o[3];
+    double f[3], mf[3] = {0., 0., 0.}, rhom_new[3], rho_o[3], em_o[3], pm_o[3], qm_o[3];
     double rho_new = 0.;
     // every value read before the first store (the stores would otherwise
     // order the later loads behind them)
@@ -473,7 +487,7 @@ struct LagCells {
       // energies (updateEnergy) and EOS
       e_new = 0.;
       bool e_first = true;  // 0.0 + x is plus_zero(x)
-      double cm_new[3], em_new[3];
+      double cm_new[3], em_new[3] = {0., 0., 0.};
       bool bad = false;
   #pragma unroll
       for (int m = 0; m < 3; ++m) {
@@ -544,9 +558,11 @@ struct LagCells {
           em_new[m] = v.em[m * P + c];
         }
       }
+      unsigned void_mask = 0;  // the run's Void materials
   #pragma unroll
       for (int m = 0; m < 3; ++m)
-        if (m < nb && eos_of(v, m) == HYDRO_EOS_VOID) e_new = 0.;
+        if (m < nb && eos_of(v, m) == HYDRO_EOS_VOID) void_mask |= 1u << m;
+      if (void_mask) e_new = 0.;
       // computePressionMoyenne: max of the in-place c and the materials'
       // sound speeds, replaced by the mixture's when rho > 0 (then the
       // materials' values are not needed)
@@ -569,9 +585,8 @@ struct LagCells {
           cc = smax(cc, cm_new[m]);
         }
       }
-  #pragma unroll
-      for (int m = 0; m < 3; ++m)
-        if (m < nb && eos_of(v, m) == HYDRO_EOS_VOID) e_new += mf[m] * em_new[m];
+      if (void_mask) e_new = void_energy(void_mask, e_new, mf[0], mf[1], mf[2], em_new[0],
+                                         em_new[1], em_new[2]);
       v.c[c] = cc;
       v.sarg[c] = sarg_new;
       if (v.projection == 0) {
