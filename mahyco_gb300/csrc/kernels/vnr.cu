@@ -423,22 +423,59 @@ struct LagCells {
     // volume): the Euler cell's with the remap, the Lagrangian volume of the
     // previous cycle (vL) without it
     const double vol_start = (v.projection == 0) ? v.vL[c] : 0.0;
+    // A cell holding one material p (f = mf = 1 for it, +0 for the others,
+    // whose densities are finite and at most the threshold), with the
+    // remap, perfect gases only, a threshold in [0, 1), a positive finite
+    // volume and a sound speed not negative: the material loops below run
+    // over p alone (slot 0, plane mat(0) = p), every sum over the materials
+    // keeping its value (the others add zeros: x + -0 = x, 0.0 + x as
+    // plus_zero), and the others' stores are the signed zeros the loops
+    // would form (below).  One branch for the whole cell; decided per value,
+    // the loops' shortcuts are if-converted into FP64 instructions that run
+    // for every material.
+    int p = -1;
+    bool single = v.projection == 1 && v.sans_lagrange == 0 && nonneg(thr) && dlt(thr, 1.0) &&
+                  pos(vol) && is_finite(vol) && !neg(c_old);
+    double fa[3] = {0., 0., 0.}, mfa[3] = {0., 0., 0.}, rma[3] = {0., 0., 0.};
   #pragma unroll
     for (int m = 0; m < 3; ++m) {
       if (m >= nb) break;
-      em_o[m] = v.em[m * P + c];
-      pm_o[m] = v.pm[m * P + c];
-      qm_o[m] = v.qm[m * P + c];
+      fa[m] = v.fm[m * P + c];
+      mfa[m] = v.mfm[m * P + c];
+      rma[m] = v.rhom[m * P + c];
+      constexpr unsigned long long kOne = 0x3ff0000000000000ull;
+      single = single && eos_of(v, m) == HYDRO_EOS_PERFECT_GAS;
+      if (ubits(fa[m]) == kOne && ubits(mfa[m]) == kOne) {
+        single = single && p < 0;
+        p = m;
+      } else {
+        single = single && (ubits(fa[m]) | ubits(mfa[m])) == 0ull && is_finite(rma[m]) &&
+                 !dgt(rma[m], thr);
+      }
+    }
+    single = single && p >= 0;
+    const int nbl = single ? 1 : nb;              // material slots of the loops
+    auto mat = [&](int m) { return single ? p : m; };  // a slot's planes
+    auto pick = [&](const double* a, int m) {     // a slot's value, by select
+      const int q = mat(m);
+      return q == 0 ? a[0] : (q == 1 ? a[1] : a[2]);
+    };
+  #pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (m >= nbl) break;
+      em_o[m] = v.em[mat(m) * P + c];
+      pm_o[m] = v.pm[mat(m) * P + c];
+      qm_o[m] = v.qm[mat(m) * P + c];
     }
   #pragma unroll
     for (int m = 0; m < 3; ++m) {
-      if (m >= nb) break;
-      f[m] = v.fm[m * P + c];
-      mf[m] = v.mfm[m * P + c];
-      const double rm = v.rhom[m * P + c];
+      if (m >= nbl) break;
+      f[m] = pick(fa, m);
+      mf[m] = pick(mfa, m);
+      const double rm = pick(rma, m);
       rho_o[m] = rm;
       rhom_new[m] = rm;
-      if (dgt(f[m], thr)) rhom_new[m] = qdiv(v.cmassm[m * P + c], mul_frac(f[m], vol));
+      if (dgt(f[m], thr)) rhom_new[m] = qdiv(v.cmassm[mat(m) * P + c], mul_frac(f[m], vol));
       const double fr = mul_frac(f[m], rhom_new[m]);
       rho_new = (m == 0) ? plus_zero(fr) : addz(rho_new, fr);
     }
@@ -491,10 +528,10 @@ struct LagCells {
       bool bad = false;
   #pragma unroll
       for (int m = 0; m < 3; ++m) {
-        if (m >= nb) break;
+        if (m >= nbl) break;
         const double qm_old = qm_o[m];
         const double qm_new = mul_frac(f[m], q_new);
-        v.qm[m * P + c] = qm_new;
+        v.qm[mat(m) * P + c] = qm_new;
         const double rn = rhom_new[m], ro = rho_o[m];
         em_new[m] = 0.;
         if (dgt(rn, thr) && dgt(ro, thr)) {
@@ -518,7 +555,7 @@ struct LagCells {
           const double em_old = em_o[m], pm_old = pm_o[m];
           constexpr unsigned long long kBig = 0x7fd0000000000000ull;   // 2^1022
           constexpr unsigned long long kSafe = 0x5fe0000000000000ull;  // 2^511
-          const double hg = hgm1_of(v, m);
+          const double hg = hgm1_of(v, mat(m));
           if (eq_inv && nz(em_old) && !is_nan(em_old) &&
               (ubits(pm_old) & kMag) < kBig &&
               (v.pseudo_centree != 0 || (ubits(qm_new) & kMag) < kBig) &&
@@ -552,10 +589,10 @@ struct LagCells {
       // matter here (the pressures are recomputed after the remap)
   #pragma unroll
       for (int m = 0; m < 3; ++m) {
-        if (m >= nb) break;
-        if (eos_of(v, m) != HYDRO_EOS_PERFECT_GAS) {  // Void: state kept
-          cm_new[m] = v.cm[m * P + c];
-          em_new[m] = v.em[m * P + c];
+        if (m >= nbl) break;
+        if (eos_of(v, mat(m)) != HYDRO_EOS_PERFECT_GAS) {  // Void: state kept
+          cm_new[m] = v.cm[mat(m) * P + c];
+          em_new[m] = v.em[mat(m) * P + c];
         }
       }
       unsigned void_mask = 0;  // the run's Void materials
@@ -577,9 +614,9 @@ struct LagCells {
       } else {
   #pragma unroll
         for (int m = 0; m < 3; ++m) {
-          if (m >= nb) break;
-          if (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) {
-            const double g = gamma_of(v, m);
+          if (m >= nbl) break;
+          if (eos_of(v, mat(m)) == HYDRO_EOS_PERFECT_GAS) {
+            const double g = gamma_of(v, mat(m));
             cm_new[m] = sqrt_ip(g * (g - 1.0) * em_new[m]);
           }
           cc = smax(cc, cm_new[m]);
@@ -598,15 +635,16 @@ struct LagCells {
         double pmean = 0.;
   #pragma unroll
         for (int m = 0; m < 3; ++m) {
-          if (m >= nb) break;
-          const double pmm = (eos_of(v, m) == HYDRO_EOS_PERFECT_GAS)
-                                 ? gm1_of(v, m) * rhom_new[m] * em_new[m]
+          if (m >= nbl) break;
+          const double pmm = (eos_of(v, mat(m)) == HYDRO_EOS_PERFECT_GAS)
+                                 ? gm1_of(v, mat(m)) * rhom_new[m] * em_new[m]
                                  : pm_o[m];
           pmean += f[m] * pmm;
-          v.pm[m * P + c] = pmm;
-          v.rhom[m * P + c] = rhom_new[m];
-          v.em[m * P + c] = em_new[m];
-          if (!pos(rho_new) && eos_of(v, m) == HYDRO_EOS_PERFECT_GAS) v.cm[m * P + c] = cm_new[m];
+          v.pm[mat(m) * P + c] = pmm;
+          v.rhom[mat(m) * P + c] = rhom_new[m];
+          v.em[mat(m) * P + c] = em_new[m];
+          if (!pos(rho_new) && eos_of(v, mat(m)) == HYDRO_EOS_PERFECT_GAS)
+            v.cm[mat(m) * P + c] = cm_new[m];
         }
         v.p[c] = pmean;
         v.rho[c] = rho_new;
@@ -627,7 +665,7 @@ struct LagCells {
     double uv[3], um[3], ue[3];
   #pragma unroll
     for (int m = 0; m < 3; ++m) {
-      if (m >= nb) break;
+      if (m >= nbl) break;
       uv[m] = mul_frac(f[m], vol);
       const double mv = mul_frac(mf[m], vol);  // (mf * vol) * rho_new ...
       um[m] = mulz(mv, rho_new);
@@ -636,35 +674,76 @@ struct LagCells {
     const double uq = mulz(q_new, vol);  // reference slot 3*nbmat+3
   #pragma unroll
     for (int m = 0; m < 3; ++m) {
-      if (m >= nb) break;
-      v.UL[m * P + c] = uv[m];
-      v.UL[(nb + m) * P + c] = um[m];
-      v.UL[(2 * nb + m) * P + c] = ue[m];
+      if (m >= nbl) break;
+      v.UL[mat(m) * P + c] = uv[m];
+      v.UL[(nb + mat(m)) * P + c] = um[m];
+      v.UL[(2 * nb + mat(m)) * P + c] = ue[m];
     }
     v.UL[3 * nb * P + c] = uq;
     if (v.pb == 1) {
       double sv = plus_zero(uv[0]);
   #pragma unroll
       for (int m = 1; m < 3; ++m)
-        if (m < nb) sv = addz(sv, uv[m]);
+        if (m < nbl) sv = addz(sv, uv[m]);
   #pragma unroll
       for (int m = 0; m < 3; ++m) {
-        if (m >= nb) break;
-        v.Phi[m * P + c] = qdiv(uv[m], sv);
-        v.Phi[(nb + m) * P + c] = nz(uv[m]) ? qdiv(um[m], uv[m]) : 0.;
-        v.Phi[(2 * nb + m) * P + c] = nz(um[m]) ? qdiv(ue[m], um[m]) : 0.;
+        if (m >= nbl) break;
+        v.Phi[mat(m) * P + c] = qdiv(uv[m], sv);
+        v.Phi[(nb + mat(m)) * P + c] = nz(uv[m]) ? qdiv(um[m], uv[m]) : 0.;
+        v.Phi[(2 * nb + mat(m)) * P + c] = nz(um[m]) ? qdiv(ue[m], um[m]) : 0.;
       }
       v.Phi[3 * nb * P + c] = q_new;
     } else {
       const SharedDiv Sv = shared_div(vol);  // one denominator, 3 nbmat + 1 quotients
   #pragma unroll
       for (int m = 0; m < 3; ++m) {
-        if (m >= nb) break;
-        v.Phi[m * P + c] = qdiv_shared(Sv, uv[m]);
-        v.Phi[(nb + m) * P + c] = qdiv_shared(Sv, um[m]);
-        v.Phi[(2 * nb + m) * P + c] = qdiv_shared(Sv, ue[m]);
+        if (m >= nbl) break;
+        v.Phi[mat(m) * P + c] = qdiv_shared(Sv, uv[m]);
+        v.Phi[(nb + mat(m)) * P + c] = qdiv_shared(Sv, um[m]);
+        v.Phi[(2 * nb + mat(m)) * P + c] = qdiv_shared(Sv, ue[m]);
       }
       v.Phi[3 * nb * P + c] = qdiv_shared(Sv, uq);
+    }
+    if (single && nb > 1) {
+      // the other materials, as the loops form them for f = mf = +0 and a
+      // density at most the threshold: q_m = +0 * q; U = (+0 * vol, (+0 *
+      // vol) * rho, ((+0 * vol) * rho) * e); Phi = +0 / V or 0 (with
+      // PenteBorne), +0 / vol and the two zeros over vol (without): zeros
+      // whose signs follow from q, rho, e (vol > 0).  Non-finite q, rho or e
+      // take the products themselves.
+      constexpr unsigned long long kS = 0x8000000000000000ull;
+      if (is_finite(q_new) && is_finite(rho_new) && is_finite(e_new)) {
+        const double zq = from_bits(ubits(q_new) & kS);
+        const double zm = from_bits(ubits(rho_new) & kS);
+        const double ze = from_bits((ubits(rho_new) ^ ubits(e_new)) & kS);
+  #pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          if (m >= nb) break;
+          if (m == p) continue;
+          v.qm[m * P + c] = zq;
+          v.UL[m * P + c] = 0.0;
+          v.UL[(nb + m) * P + c] = zm;
+          v.UL[(2 * nb + m) * P + c] = ze;
+          v.Phi[m * P + c] = 0.0;
+          v.Phi[(nb + m) * P + c] = (v.pb == 1) ? 0.0 : zm;
+          v.Phi[(2 * nb + m) * P + c] = (v.pb == 1) ? 0.0 : ze;
+        }
+      } else {
+        const double zm = mulz(0.0, rho_new), ze = mulz(mulz(0.0, rho_new), e_new);
+  #pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          if (m >= nb) break;
+          if (m == p) continue;
+          v.qm[m * P + c] = mul_frac(0.0, q_new);
+          v.UL[m * P + c] = 0.0;
+          v.UL[(nb + m) * P + c] = zm;
+          v.UL[(2 * nb + m) * P + c] = ze;
+          v.Phi[m * P + c] = 0.0;
+          v.Phi[(nb + m) * P + c] = (v.pb == 1) ? 0.0 : qdiv(zm, vol);
+          v.Phi[(2 * nb + m) * P + c] =
+              (v.pb == 1) ? (nz(zm) ? qdiv(ze, zm) : 0.0) : qdiv(ze, vol);
+        }
+      }
     }
     v.vL[c] = vol;
     v.rL[c] = rho_new;
