@@ -2317,10 +2317,10 @@ __global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { bat
 __global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 9) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads, 10) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads, 12) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 8) kb_final(BatchArgs b) { batch_items(b, Final{}); }
+__global__ void __launch_bounds__(kBatchThreads, 7) kb_final(BatchArgs b) { batch_items(b, Final{}); }
 
 // One thread per run: cycle start (begin + reduction reset) and cycle end.
 __global__ void kb_begin(const RunView* views, const int* ninst) {
