@@ -92,6 +92,9 @@ size_t layout(RunView& v, char* base) {
   // planes, which those runs never use (2 nc cell planes hold nc face
   // planes: FP <= 2 P for nx, ny >= 2)
   v.phiG = v.dPAv;
+  // the fused sweeps keep the integrals on chip: dPAv holds the first
+  // sweep's Phi of the cells it changes
+  v.Phi2 = fused_sweeps_ok(v) ? v.dPAv : nullptr;
   v.phiF = a.take<double>(nc * FP);
   v.FFd = a.take<double>(nb * P);
   if (v.order == 3) {

@@ -100,6 +100,9 @@ struct RunView {
   double *vL, *rL, *XcL /*2 planes*/, *Hx, *Hy;
   double* UL;         // ncomp planes (also receives the second sweep)
   double* Phi;        // ncomp planes
+  double* Phi2;       // fused sweeps: the first sweep's Phi of the cells it
+                      // changed (aliases dPAv, which those runs do not
+                      // use); null otherwise
   double* U1;         // ncomp planes
   unsigned char* u1s; // per cell (orders 1-2): the first sweep left every
                       // component unchanged and did not store U1
@@ -157,6 +160,16 @@ struct RunView {
   struct Ctrl* ctrl;
 };
 
+// The fused remap sweep (k_sweep_fused: slopes, plateau-slope integrals and
+// update in one kernel per sweep) applies to VNR runs with the remap,
+// PenteBorne without the mixed limiter or the "complet" variant, order 2,
+// the A1 / A2 dual mass flux (not PenteBorne's) and no boundary flux.
+inline bool fused_sweeps_ok(const RunView& v) {
+  return v.scheme == HYDRO_SCHEME_VNR && v.projection == 1 && v.pb == 1 && v.pb_mixte == 0 &&
+         v.pb_complet == 0 && v.order == 2 && v.dual_method != 2 && v.flux_bc == 0 &&
+         v.ncomp <= 10;
+}
+
 // Per-run device control block.
 struct Ctrl {
   double t_n, dt_n, t_np1, dt_np1;
@@ -202,7 +215,7 @@ __device__ __forceinline__ bool output_pause_here(Ctrl& C) {
 
 // Per-kernel timing hook for launch_cycle.
 using LaunchHook = std::function<void(int)>;
-constexpr int kNumKernelKinds = 19;
+constexpr int kNumKernelKinds = 20;
 extern const char* const kKernelNames[kNumKernelKinds];
 
 // ---- batched execution: many independent runs advance in one launch per

@@ -833,6 +833,21 @@ __device__ __noinline__ PPFluxes pp_fluxes_call(int plim, double thr, double y0,
 template <int PB>
 struct SweepGradT {
   int sweep;
+  // Fused sweeps (PenteBorne): the cell's flag and integrals go to a tile in
+  // shared memory (tz[ti]; tr / tv[k * ts + ti]) instead of pbz / dPAr /
+  // dPAv, and (phi2) the second sweep reads the Phi of a cell the first
+  // sweep changed from Phi2, where that sweep wrote it.
+  unsigned char* tz = nullptr;
+  double *tr = nullptr, *tv = nullptr;
+  int ti = 0, ts = 0;
+  bool phi2 = false;
+  DV const double* phi_of(const RunView& v, long long x) const {
+    return (phi2 && v.u1s[x] == 0) ? v.Phi2 + x : v.Phi + x;
+  }
+  DV void put_z(const RunView& v, long long c, unsigned char z) const {
+    if (tz) tz[ti] = z;
+    else v.pbz[c] = z;
+  }
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
     const int pb = (PB == 2) ? v.pb : PB;
     // no slopes at order 1, nor at order 3 without PenteBorne (batched
@@ -887,7 +902,7 @@ struct SweepGradT {
         const unsigned long long z = ubits(v.u[o + n0]) | ubits(v.u[o + n0 + 1]) |
                                      ubits(v.u[o + n0 + v.nx + 1]) | ubits(v.u[o + n0 + v.nx + 2]);
         if ((z & kMag) == 0 && is_finite(C.dt_n)) {
-          v.pbz[c] = 3;  // both integral planes all +0.0, not stored
+          put_z(v, c, 3);  // both integral planes all +0.0, not stored
           if (cfd) {
             const double fl = dirx ? half(ld(v.flv, i) + ld(v.flv, i)) : half(ld(v.flh, j) + ld(v.flh, j));
             const double zf = 0.0 * fl;
@@ -919,7 +934,7 @@ struct SweepGradT {
       // half-faces: every flux stored below is then exactly 0 (0 * flen for
       // the dual one) whatever the slopes, so they are not formed
       if (iszero(ppa) && iszero(ppb) && (!cfd || iszero(ppd))) {
-        v.pbz[c] = 3;
+        put_z(v, c, 3);
         if (cfd) {
           const double z = 0.0 * flen;
           for (int m = 0; m < nb; ++m) v.DPF[m * P + c] = z;
@@ -989,14 +1004,20 @@ struct SweepGradT {
       sp = plus_zero(xf_p - xc);
       sm = plus_zero(xf_m - xc);
     }
+    // Phi of the cell and of its front / back neighbours
+    const double* Pc = phi_of(v, c);
+    const double* Pf = phi_of(v, cf);
+    const double* Pb = phi_of(v, cb);
+    const double* Pp = dirx ? Pf : Pb;  // plus / minus neighbours
+    const double* Pm = dirx ? Pb : Pf;
     double grad[kMaxComp];
     for (int k = 0; k < ngrad; ++k) {
-      const double y0 = v.Phi[k * P + c];
-      const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
+      const double y0 = Pc[k * P];
+      const double yp = Pp[k * P], ym = Pm[k * P];
       double gp = 0., gm = 0.;
       if (pb == 1) {
-        if (has_gp) gp = qdiv_shared(Sp, v.Phi[k * P + cf] - y0);
-        if (has_gm) gm = qdiv_shared(Sm, y0 - v.Phi[k * P + cb]);
+        if (has_gp) gp = qdiv_shared(Sp, Pf[k * P] - y0);
+        if (has_gm) gm = qdiv_shared(Sm, y0 - Pb[k * P]);
       } else {
         if (has_gp) gp = v.phiG[k * FP + fp];
         if (has_gm) gm = v.phiG[k * FP + fm];
@@ -1013,8 +1034,8 @@ struct SweepGradT {
       double Fr[kMaxComp], Fv[kMaxComp];
       const double hh = h0;
       for (int k = 0; k < nuse; ++k) {
-        const double y0 = v.Phi[k * P + c];
-        const double yp = v.Phi[k * P + cp], ym = v.Phi[k * P + cm];
+        const double y0 = Pc[k * P];
+        const double yp = Pp[k * P], ym = Pm[k * P];
         const bool dual_k = cfd && k >= nb && k < 2 * nb;
         double fa_, fb_, fd_;
         if (nonneg((yp - y0) * (ym - y0))) {
@@ -1043,7 +1064,7 @@ struct SweepGradT {
         }
       }
       // derived fluxes
-      auto finish = [&](double* F, double ppv, double* out) {
+      auto finish = [&](double* F, double* out, long long stride) {
         if (v.pb_complet == 1) {
           double sfm = 0., sfv = plus_zero(F[0]);
           for (int m = 1; m < nb; m++) sfv += F[m];
@@ -1056,7 +1077,7 @@ struct SweepGradT {
             if (euc)
               for (int k = 3 * nb; k < ncomp; ++k) F[k] = div_ip(F[k], sfv) * sfm;
             else
-              F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
+              F[3 * nb] = Pc[3 * nb * P] * sfv;
           } else {
             for (int k = 0; k < ncomp; ++k) F[k] = 0.0;
           }
@@ -1064,23 +1085,29 @@ struct SweepGradT {
           double sfv = 0., sfm = 0.;
           for (int m = 0; m < nb; m++) {
             // an absent material's volume flux is exactly 0 (mul_frac)
-            if (!vp) F[nb + m] = mul_frac(F[m], v.Phi[(nb + m) * P + c]);
-            F[2 * nb + m] = mul_frac(F[nb + m], v.Phi[(2 * nb + m) * P + c]);
+            if (!vp) F[nb + m] = mul_frac(F[m], Pc[(nb + m) * P]);
+            F[2 * nb + m] = mul_frac(F[nb + m], Pc[(2 * nb + m) * P]);
             sfm = (m == 0) ? plus_zero(F[nb + m]) : sfm + F[nb + m];
             sfv = (m == 0) ? plus_zero(F[m]) : sfv + F[m];
           }
           if (euc)
-            for (int k = 3 * nb; k < ncomp; ++k) F[k] = v.Phi[k * P + c] * sfm;
+            for (int k = 3 * nb; k < ncomp; ++k) F[k] = Pc[k * P] * sfm;
           else
-            F[3 * nb] = v.Phi[3 * nb * P + c] * sfv;
+            F[3 * nb] = Pc[3 * nb * P] * sfv;
         }
-        for (int k = 0; k < ncomp; ++k) out[k * P] = F[k];
+        for (int k = 0; k < ncomp; ++k) out[k * stride] = F[k];
       };
       // a zero swept length makes every integral of that side exactly +0.0:
       // recorded in pbz instead of stored (bit 0: dPAr, bit 1: dPAv)
-      v.pbz[c] = (iszero(ppa) ? 1 : 0) | (iszero(ppb) ? 2 : 0);
-      if (!iszero(ppa)) finish(Fr, ppa, v.dPAr + c);
-      if (!iszero(ppb)) finish(Fv, ppb, v.dPAv + c);
+      put_z(v, c, (iszero(ppa) ? 1 : 0) | (iszero(ppb) ? 2 : 0));
+      if (!iszero(ppa)) {
+        if (tz) finish(Fr, tr + ti, ts);
+        else finish(Fr, v.dPAr + c, P);
+      }
+      if (!iszero(ppb)) {
+        if (tz) finish(Fv, tv + ti, ts);
+        else finish(Fv, v.dPAv + c, P);
+      }
     }
   }
 };
@@ -1345,6 +1372,22 @@ DV LowFace low_face(const RunView& v, bool dirx, long long cb, long long cf) {
   F.zr = (v.pbz[F.ar] & 1) != 0;
   return F;
 }
+// the same from a fused sweep's tile: tz[] flags, tv / tr[k * ts + x]
+// integrals, x the tile index of the face's back / front cell
+DV LowFace low_face_tile(const unsigned char* tz, bool dirx, int cb, int cf) {
+  LowFace F;
+  F.av = dirx ? cb : cf;
+  F.ar = dirx ? cf : cb;
+  F.zv = (tz[F.av] & 2) != 0;
+  F.zr = (tz[F.ar] & 1) != 0;
+  return F;
+}
+DV double low_face_value_tile(const double* tv, const double* tr, int ts, const LowFace& F,
+                              int k) {
+  const double a = F.zv ? 0.0 : tv[k * ts + F.av];
+  const double b = F.zr ? 0.0 : tr[k * ts + F.ar];
+  return subz(a, b);
+}
 DV double low_face_value(const RunView& v, const LowFace& F, int k) {
   const long long P = v.pitch;
   // an integral plane flagged in pbz holds +0.0 for every component (the
@@ -1367,6 +1410,14 @@ DV double low_face_value(const RunView& v, const LowFace& F, int k) {
 template <int FACES>
 struct SweepUpdateT {
   int sweep;
+  // Fused sweeps (PenteBorne, orders 1-2): the faces' flags and integrals
+  // come from the tile (lc: the cell's tile index, lm / lp: its neighbours'
+  // at -1 / +1 along the sweep axis), and (phi2) the first sweep writes the
+  // Phi of the cells it changes to Phi2 instead of Phi.
+  const unsigned char* tz = nullptr;
+  const double *tr = nullptr, *tv = nullptr;
+  int lc = 0, lm = 0, lp = 0, ts = 0;
+  bool phi2 = false;
   __device__ __forceinline__ void operator()(const RunView& v, int i, int j) const {
     const Ctrl& C = *v.ctrl;
     if (i >= v.ny || j >= v.nx) return;
@@ -1437,7 +1488,15 @@ struct SweepUpdateT {
     // SweepFace names them
     const bool form = (FACES == 1) || (FACES == 2 && v.order <= 2 && v.pb == 1);
     LowFace lf[2];
-    if (form) {
+    if (form && tz) {
+      if (dirx) {
+        if (has[0]) lf[0] = low_face_tile(tz, true, lm, lc);
+        if (has[1]) lf[1] = low_face_tile(tz, true, lc, lp);
+      } else {
+        if (has[0]) lf[0] = low_face_tile(tz, false, lc, lm);
+        if (has[1]) lf[1] = low_face_tile(tz, false, lp, lc);
+      }
+    } else if (form) {
       if (dirx) {
         if (has[0]) lf[0] = low_face(v, true, c - 1, c);
         if (has[1]) lf[1] = low_face(v, true, c, c + 1);
@@ -1516,7 +1575,10 @@ struct SweepUpdateT {
   #pragma unroll
       for (int t = 0; t < 4; ++t) {
         const int k = k0 + t;
-        if (form) {
+        if (form && tz) {
+          qa[t] = (k < ncomp && has[0]) ? low_face_value_tile(tv, tr, ts, lf[0], k) : 0.;
+          qb[t] = (k < ncomp && has[1]) ? low_face_value_tile(tv, tr, ts, lf[1], k) : 0.;
+        } else if (form) {
           qa[t] = (k < ncomp && has[0]) ? low_face_value(v, lf[0], k) : 0.;
           qb[t] = (k < ncomp && has[1]) ? low_face_value(v, lf[1], k) : 0.;
         } else {
@@ -1607,7 +1669,10 @@ struct SweepUpdateT {
       for (int k = 0; k < ncomp; ++k) v.UL[k * P + c] = U[k];
     }
     if (sweep == 1) {
-      double* Phi = v.Phi;
+      // (fused sweeps: to Phi2, which the second sweep reads for the cells
+      // changed here; Phi itself stays as the Lagrange kernel left it, since
+      // neighbouring tiles still read it)
+      double* Phi = phi2 ? v.Phi2 : v.Phi;
       // a VNR cell whose conserved values came through the sweep unchanged
       // keeps the Phi the Lagrange kernel formed from exactly these values
       // with the same formulas (the pseudo-viscosity slot is not updated
@@ -1634,9 +1699,10 @@ struct SweepUpdateT {
         const SharedDiv Sv = shared_div(vl);  // one denominator, ncomp quotients
         for (int k = 0; k < ncomp; ++k) Phi[k * P + c] = qdiv_shared(Sv, U[k]);
       }
+      const double* Pr = keep ? v.Phi : Phi;  // the cell's Phi after the sweep
       int matcell = 0, imatpure = -1;
       for (int m = 0; m < nb; m++)
-        if (pos(Phi[m * P + c])) {
+        if (pos(Pr[m * P + c])) {
           matcell++;
           imatpure = m;
         }
@@ -2279,6 +2345,103 @@ __global__ void __launch_bounds__(kBX* kBY) k_sweep_face(RunView v, int sweep) {
 __global__ void __launch_bounds__(kBX* kBY, 4) k_sweep_face3(RunView v, int sweep) { plain_items(v, SweepFaceT<1>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY) k_sweep_update(RunView v, int sweep) { plain_items(v, SweepUpdateT<0>{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY, 9) k_sweep_update_f(RunView v, int sweep) { plain_items(v, SweepUpdateT<1>{sweep}); }
+
+// ------------------------------------------------------- fused remap sweep
+// One launch per sweep for VNR runs with PenteBorne pure at order 2 (the
+// benchmark's options; fused_sweeps_ok): the slopes and plateau-slope
+// integrals of SweepGradT and the update of SweepUpdateT, with the
+// integrals and their zero flags kept in shared memory instead of the
+// dPAr / dPAv / pbz planes.  A cell's face values need the integrals of
+// its neighbours along the sweep, so a tile computes them for one cell more
+// on each side (the same arithmetic as the neighbouring tile, the same
+// bits).  The first sweep writes the new Phi of the cells it changes to
+// Phi2 (a neighbouring tile may still read their Phi for its halo); the
+// second reads Phi2 for those cells.  The blocks take the sweep direction
+// from the control block:
+//  - along x: 8 rows of 126 cells, each row's 128 slope cells computed,
+//    then its 126 cells updated;
+//  - along y: a strip of 32 columns by 60 rows, walked down 4 rows at a time
+//    with the slope rows in a ring of 8 (the rows above and below the strip,
+//    and two beyond, are its only extra slope work).
+constexpr int kFxCells = 128, kFxRows = 8;   // x: slope cells per row, rows per block
+constexpr int kFyW = 32, kFyH = 60, kFyRing = 8;  // y: strip width, height, ring rows
+constexpr int kFusedCells = kFyRing * kFyW;       // tile cells held (>= kFxCells)
+
+// shared memory of a tile of `cells` slope cells: their flags, then the
+// dPAr-side and dPAv-side integrals (ncomp planes of `cells` each)
+size_t fused_smem_bytes(int ncomp, int cells) {
+  return (size_t)cells + (size_t)2 * ncomp * cells * sizeof(double);
+}
+dim3 fused_grid_x(const RunView& v) {
+  return dim3((unsigned)((long long)((v.nx + kFxCells - 3) / (kFxCells - 2)) *
+                         ((v.ny + kFxRows - 1) / kFxRows)));
+}
+dim3 fused_grid_y(const RunView& v) {
+  return dim3((unsigned)((long long)((v.nx + kFyW - 1) / kFyW) * ((v.ny + kFyH - 1) / kFyH)));
+}
+
+// DIRX: the kernel of the sweeps along x (the other returns at once)
+template <bool DIRX>
+__device__ __forceinline__ void sweep_fused(const RunView& v, int sweep) {
+  const Ctrl& C = *v.ctrl;
+  if (!C.active) return;
+  const bool dirx = (sweep == 1) ? C.x_then_y : !C.x_then_y;
+  if (dirx != DIRX) return;
+  constexpr int cells = DIRX ? kFxCells : kFusedCells;  // tile slope cells
+  extern __shared__ double fused_smem[];
+  unsigned char* sz = reinterpret_cast<unsigned char*>(fused_smem);
+  double* sr = fused_smem + cells / 8;
+  double* sv = sr + (size_t)v.ncomp * cells;
+  const int tid = threadIdx.x;
+  if (DIRX) {
+    const int ntx = (v.nx + kFxCells - 3) / (kFxCells - 2);
+    const int bx = blockIdx.x % ntx, by = blockIdx.x / ntx;
+    if (by * kFxRows >= v.ny) return;
+    const int j = bx * (kFxCells - 2) - 1 + tid;
+    for (int r = 0; r < kFxRows; ++r) {
+      const int i = by * kFxRows + r;
+      if (i >= v.ny) break;  // uniform over the block
+      if (j >= 0 && j < v.nx)
+        SweepGradT<1>{sweep, sz, sr, sv, tid, cells, sweep == 2}(v, i, j);
+      __syncthreads();
+      if (tid >= 1 && tid <= kFxCells - 2 && j < v.nx)
+        SweepUpdateT<1>{sweep, sz, sr, sv, tid, tid - 1, tid + 1, cells, sweep == 1}(v, i, j);
+      __syncthreads();
+    }
+  } else {
+    const int nty = (v.nx + kFyW - 1) / kFyW;
+    const int bx = blockIdx.x % nty, by = blockIdx.x / nty;
+    const int i0 = by * kFyH;
+    if (i0 >= v.ny) return;
+    const int tx = tid & (kFyW - 1), ty = tid / kFyW;  // 4 rows of 32
+    const int j = bx * kFyW + tx;
+    const int i1 = (i0 + kFyH < v.ny) ? i0 + kFyH : v.ny;  // rows i0 .. i1 - 1
+    auto slot = [&](int row) { return (row & (kFyRing - 1)) * kFyW + tx; };
+    // step s: the slope rows i0 - 1 + 4s .. + 3 (one per warp), then the rows
+    // i0 + 4(s - 1) .. + 3, whose slope rows (one above, one below) are all
+    // in the ring of 8 now; the next step's slope rows overwrite those of
+    // rows 4 older, which no update reads any more
+    for (int s = 0;; ++s) {
+      const int g = i0 - 1 + 4 * s + ty;
+      if (g >= 0 && g <= i1 && g < v.ny && j < v.nx)
+        SweepGradT<1>{sweep, sz, sr, sv, slot(g), cells, sweep == 2}(v, g, j);
+      __syncthreads();
+      const int r = i0 + 4 * (s - 1);
+      const int row = r + ty;
+      if (s >= 1 && row < i1 && j < v.nx)
+        SweepUpdateT<1>{sweep, sz, sr, sv, slot(row), slot(row - 1), slot(row + 1), cells,
+                        sweep == 1}(v, row, j);
+      if (s >= 1 && r + 4 >= i1) break;  // uniform over the block
+      __syncthreads();
+    }
+  }
+}
+__global__ void __launch_bounds__(128, 7) k_sweep_fused_x(RunView v, int sweep) {
+  sweep_fused<true>(v, sweep);
+}
+__global__ void __launch_bounds__(128, 7) k_sweep_fused_y(RunView v, int sweep) {
+  sweep_fused<false>(v, sweep);
+}
 __global__ void __launch_bounds__(kBX* kBY, 10) k_dual_grad(RunView v, int sweep) { plain_items(v, DualGrad{sweep}); }
 // ten resident blocks: where nodes are quiet the kernel waits on memory
 __global__ void __launch_bounds__(kBX* kBY, 12) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
@@ -2365,7 +2528,7 @@ const char* const kKernelNames[kNumKernelKinds] = {
     "k_sweep_grad", "k_sweep_face",       "k_sweep_update", "k_dual_grad",
     "k_dual_update", "k_final",           "k_end",         "k_face_grad",
     "ke_cell_pre",  "ke_nodes",           "ke_cells",      "ke_final",
-    "k_o3_grad",    "k_o3_ystar",        "k_next_positions"};
+    "k_o3_grad",    "k_o3_ystar",        "k_next_positions", "k_sweep_fused"};
 
 // Enqueues one full cycle on stream s; hook(kind) is called before each
 // launch (and with kind = -1 after the last) when given.  Returns the number
@@ -2380,6 +2543,15 @@ int launch_sweep(const RunView& v, int sweep, cudaStream_t s, const LaunchHook* 
   auto H = [&](int kind) {
     if (hook) (*hook)(kind);
   };
+  if (v.Phi2) {
+    // one kernel per direction; the one whose direction this sweep is not
+    // returns at once (the direction is decided on the device)
+    H(19);
+    k_sweep_fused_x<<<fused_grid_x(v), kFxCells, fused_smem_bytes(v.ncomp, kFxCells), s>>>(v, sweep);
+    k_sweep_fused_y<<<fused_grid_y(v), kFxCells, fused_smem_bytes(v.ncomp, kFusedCells), s>>>(v,
+                                                                                       sweep);
+    return 2;
+  }
   // limited slopes (with their face gradients) feed the order-2 face values
   // and PenteBorne only
   if (v.order == 2 || (v.order == 3 && v.pb == 1)) {
