@@ -1691,9 +1691,12 @@ struct SweepUpdateT {
         for (int m = 0; m < nb; m++)
           Phi[(2 * nb + m) * P + c] = nz(U[nb + m]) ? qdiv(U[2 * nb + m], U[nb + m]) : 0.;
         // Eucclhyd momentum / kinetic energy per unit mass (the VNR
-        // pseudo-viscosity slot is not updated here in the reference)
+        // pseudo-viscosity slot is not updated here in the reference: in
+        // Phi2 it is the Lagrange kernel's value, copied)
         if (v.scheme == HYDRO_SCHEME_EUCCLHYD)
           for (int k = 3 * nb; k < ncomp; ++k) Phi[k * P + c] = qdiv(U[k], sm);
+        else if (phi2)
+          Phi[3 * nb * P + c] = v.Phi[3 * nb * P + c];
       } else {
         // vl: the Lagrangian volume, read with the inputs
         const SharedDiv Sv = shared_div(vl);  // one denominator, ncomp quotients
