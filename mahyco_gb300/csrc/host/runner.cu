@@ -7,6 +7,7 @@
 #include <climits>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -44,6 +45,14 @@ struct Carve {
     return base ? reinterpret_cast<T*>(base + at) : nullptr;
   }
 };
+
+// The fused remap sweeps measured slower than the separate slope and update
+// kernels on GB300 (the kernels are latency-bound; a tile's barrier between
+// its slope and update phases idles warps), so they run only on request.
+bool fused_sweeps_requested() {
+  const char* e = std::getenv("MAHYCO_GB300_FUSED_SWEEPS");
+  return e && e[0] == '1';
+}
 
 // Lays out every device array of a run; with base == nullptr it only sizes.
 size_t layout(RunView& v, char* base) {
@@ -92,9 +101,10 @@ size_t layout(RunView& v, char* base) {
   // planes, which those runs never use (2 nc cell planes hold nc face
   // planes: FP <= 2 P for nx, ny >= 2)
   v.phiG = v.dPAv;
-  // the fused sweeps keep the integrals on chip: dPAv holds the first
-  // sweep's Phi of the cells it changes
-  v.Phi2 = fused_sweeps_ok(v) ? v.dPAv : nullptr;
+  // the fused sweeps (opt-in: MAHYCO_GB300_FUSED_SWEEPS=1 when the run is
+  // created) keep the integrals on chip: dPAv holds the first sweep's Phi of
+  // the cells it changes
+  v.Phi2 = (fused_sweeps_ok(v) && fused_sweeps_requested()) ? v.dPAv : nullptr;
   v.phiF = a.take<double>(nc * FP);
   v.FFd = a.take<double>(nb * P);
   if (v.order == 3) {
