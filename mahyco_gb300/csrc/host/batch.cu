@@ -45,6 +45,10 @@ int phase_of_kind(int kind) {
     case 7: return kPhDualGrad;
     case 8: return kPhDualUpdate;
     case 9: return kPhFinal;
+    case 12: return kPhEucCellPre;
+    case 13: return kPhEucNodes;
+    case 14: return kPhEucCells;
+    case 15: return kPhEucFinal;
     default: return -1;
   }
 }
@@ -126,7 +130,11 @@ void fill_launch(BatchPlan* p) {
   L.any_face = 0;
   L.any_face_grad = 0;
   L.variant = kBatchNoOrder3 | kBatchNoPB;
+  L.any_vnr = 0;
+  L.any_euc = 0;
   for (auto* r : p->runs) {
+    if (r->v.scheme == HYDRO_SCHEME_EUCCLHYD) L.any_euc = 1;
+    else L.any_vnr = 1;
     if (r->v.order > 1) L.any_order2 = 1;
     // the face phase serves order-3 runs and order-1 runs without PenteBorne
     if (r->v.order == 3 || (r->v.order == 1 && r->v.pb == 0)) L.any_face = 1;
@@ -231,7 +239,9 @@ int set_members(BatchPlan* p, hydro_run* const* runs, int n) {
                                  sizeof(Tile) * tiles[on][w].size(),
                                  cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaStreamSynchronize(s));
-  const int old_order2 = p->L.any_order2, old_variant = p->L.variant;
+  // the flags that decide which kernels a cycle launches
+  const int old_flags[6] = {p->L.any_order2, p->L.variant, p->L.any_face,
+                            p->L.any_face_grad, p->L.any_vnr, p->L.any_euc};
   p->runs = rv;
   p->cells = cells;
   p->h_done.assign(n, 0);
@@ -240,8 +250,10 @@ int set_members(BatchPlan* p, hydro_run* const* runs, int n) {
   fill_launch(p);
   // the persistent grids do not depend on the membership; one-block-per-tile
   // grids and the slope phases do
-  if (memcmp(old_grid, p->L.grid, sizeof(old_grid)) || old_order2 != p->L.any_order2 ||
-      old_variant != p->L.variant)
+  const int new_flags[6] = {p->L.any_order2, p->L.variant, p->L.any_face,
+                            p->L.any_face_grad, p->L.any_vnr, p->L.any_euc};
+  if (memcmp(old_grid, p->L.grid, sizeof(old_grid)) ||
+      memcmp(old_flags, new_flags, sizeof(old_flags)))
     drop_graph(p);
   return 0;
 }
@@ -251,8 +263,8 @@ int get_plan(hydro_ctx* ctx, hydro_run* const* runs, int n, BatchPlan** out) {
   for (int r = 0; r < n; ++r) {
     if (!runs[r]) return fail(-1, "batch: null run");
     if (runs[r]->ctx != ctx) return fail(-2, "batch: run belongs to another context");
-    if (runs[r]->v.scheme != HYDRO_SCHEME_VNR)
-      return fail(-4, "batch: the batched form advances VNR runs");
+    if (runs[r]->v.scheme != HYDRO_SCHEME_VNR && runs[r]->v.scheme != HYDRO_SCHEME_EUCCLHYD)
+      return fail(-4, "batch: unknown scheme");
     if (runs[r]->v.projection != 1)
       return fail(-5, "batch: the batched form advances runs with the remap");
   }

@@ -345,8 +345,8 @@ int hydro_serve_config(hydro_ctx* ctx, size_t budget_bytes, int max_resident,
 int hydro_serve_submit(hydro_ctx* ctx, const hydro_spec* spec, int keep,
                        long* req_id) {
   if (!ctx || !spec) return fail(-1, "hydro_serve_submit: null argument");
-  if (spec->scheme != HYDRO_SCHEME_VNR)
-    return fail(-4, "hydro_serve_submit: the serving loop advances VNR runs");
+  if (spec->scheme != HYDRO_SCHEME_VNR && spec->scheme != HYDRO_SCHEME_EUCCLHYD)
+    return fail(-4, "hydro_serve_submit: unknown scheme");
   if (spec->projection != 1)
     return fail(-5, "hydro_serve_submit: the serving loop advances runs with the remap");
   ServeState* S = get_serve(ctx);

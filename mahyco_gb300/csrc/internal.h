@@ -239,13 +239,16 @@ struct BatchArgs {
 };
 // Item phases of a cycle, in launch order; the two domains are cells
 // (nx x ny) and nodes ((nx+1) x (ny+1), which also index the faces).
+// The Eucclhyd phases (kPhEuc*) run on the batch's Eucclhyd runs, the VNR
+// Lagrange, dual and final phases on its VNR runs, the sweep phases on all.
 enum BatchPhase {
   kPhLagNodes, kPhLagCells, kPhFaceGrad, kPhSweepGrad, kPhSweepFace,
-  kPhSweepUpdate, kPhDualGrad, kPhDualUpdate, kPhFinal, kNumPhases
+  kPhSweepUpdate, kPhDualGrad, kPhDualUpdate, kPhFinal,
+  kPhEucCellPre, kPhEucNodes, kPhEucCells, kPhEucFinal, kNumPhases
 };
 constexpr bool phase_on_nodes(int ph) {
   return ph == kPhLagNodes || ph == kPhFaceGrad || ph == kPhSweepFace ||
-         ph == kPhDualGrad || ph == kPhDualUpdate;
+         ph == kPhDualGrad || ph == kPhDualUpdate || ph == kPhEucNodes;
 }
 // Tile shapes: 2^tw_log2 items wide; each of the block's
 // kBatchThreads >> tw_log2 thread rows covers `rows` item rows, so one tile
@@ -273,6 +276,7 @@ struct BatchLaunch {
                           // without PenteBorne)
   int variant;            // kBatch* bits: lighter kernels when no run needs
                           // the order-3 faces / the PenteBorne slopes
+  int any_vnr, any_euc;   // the batch holds runs of that scheme
 };
 constexpr int kBatchNoOrder3 = 1;
 constexpr int kBatchNoPB = 2;

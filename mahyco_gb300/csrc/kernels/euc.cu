@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include "../internal.h"
+#include "items.cuh"
 #include "scheme_math.cuh"
 
 namespace hydro {
@@ -86,7 +87,7 @@ DV void block_min(unsigned long long dtv, Ctrl* C) {
 }
 
 // ------------------------------------------------------------- control
-__global__ void ke_begin(RunView v) {
+DV void euc_begin_at(const RunView& v) {
   Ctrl& C = *v.ctrl;
   if (C.done || (C.err & ~HYDRO_ERR_NEGATIVE)) {
     C.active = 0;
@@ -101,11 +102,12 @@ __global__ void ke_begin(RunView v) {
   C.n += 1;
   C.dt_min_bits = ord_bits(1.7976931348623157e308);
 }
+__global__ void ke_begin(RunView v) { euc_begin_at(v); }
 
 // computedeltat (EucclhydRemap.cc:203-221): the cycle's cell dt minimum
 // gives dt_{n+1}; updateTime; the loop condition and the swap of t, dt.
 // The Lagrange positions and the remap of this cycle used dt_n.
-__global__ void ke_end(RunView v) {
+DV void euc_end_at(const RunView& v) {
   Ctrl& C = *v.ctrl;
   if (!C.active) return;
   const double red = from_ord(C.dt_min_bits);
@@ -121,6 +123,7 @@ __global__ void ke_end(RunView v) {
     C.done = 1;
   if (C.err & ~HYDRO_ERR_NEGATIVE) C.done = 1;
 }
+__global__ void ke_end(RunView v) { euc_end_at(v); }
 
 // computeEOSGP / computeEOSVoid for material m of cell c (PhaseLagrange.cc
 // :70-109); the other EOS ids keep the stored values (their reference
@@ -791,12 +794,66 @@ __global__ void __launch_bounds__(kBX* kBY, 8) ke_nodes(RunView v) { plain_items
 __global__ void __launch_bounds__(kBX* kBY, 8) ke_cells(RunView v) { plain_items(v, EucCells{}); }
 __global__ void __launch_bounds__(kBX* kBY, 10) ke_final(RunView v) { plain_items(v, EucFinal{}); }
 
+// Batched launches of the Eucclhyd phases (the batch's VNR runs are skipped;
+// the remap sweeps are the shared batched kernels of vnr.cu).
+constexpr int kE = HYDRO_SCHEME_EUCCLHYD;
+__global__ void __launch_bounds__(kBatchThreads, 12) kbe_cell_pre(BatchArgs b) { batch_items(b, EucCellPre{}, kE); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kbe_nodes(BatchArgs b) { batch_items(b, EucNodes{}, kE); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kbe_cells(BatchArgs b) { batch_items(b, EucCells{}, kE); }
+__global__ void __launch_bounds__(kBatchThreads, 10) kbe_final(BatchArgs b) { batch_items(b, EucFinal{}, kE); }
+// one thread per Eucclhyd run: cycle start and end
+__global__ void kbe_begin(const RunView* views, const int* ninst) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= *ninst) return;
+  const RunView v = views[r];
+  if (v.scheme == kE) euc_begin_at(v);
+}
+__global__ void kbe_end(const RunView* views, const int* ninst, int* done) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= *ninst) return;
+  const RunView v = views[r];
+  if (v.scheme != kE) return;
+  euc_end_at(v);
+  done[r] = v.ctrl->done;
+}
+
 }  // namespace
 
 int launch_euc_out_pressure(const RunView& v, double* out, cudaStream_t s) {
   const dim3 cg((v.nx + kBX - 1) / kBX, (v.ny + kBY - 1) / kBY);
   ke_out_pressure<<<cg, dim3(kBX, kBY), 0, s>>>(v, out);
   return 1;
+}
+
+// One Eucclhyd phase of a batched cycle: kPhEucCellPre, kPhEucNodes,
+// kPhEucCells, kPhEucFinal on the tile arguments a, or (ph < 0) the
+// per-run cycle start (-1) / end (-2).
+void launch_batch_euc(int ph, const BatchLaunch& L, const BatchArgs& a, int grid,
+                      cudaStream_t s) {
+  const int T = kBatchThreads, rg = (L.max_inst + T - 1) / T;
+  switch (ph) {
+    case -1: kbe_begin<<<rg, T, 0, s>>>(L.views, L.ninst); break;
+    case -2: kbe_end<<<rg, T, 0, s>>>(L.views, L.ninst, L.done); break;
+    case kPhEucCellPre: kbe_cell_pre<<<grid, T, 0, s>>>(a); break;
+    case kPhEucNodes: kbe_nodes<<<grid, T, 0, s>>>(a); break;
+    case kPhEucCells: kbe_cells<<<grid, T, 0, s>>>(a); break;
+    case kPhEucFinal: kbe_final<<<grid, T, 0, s>>>(a); break;
+    default: break;
+  }
+}
+// resident blocks per SM of the Eucclhyd phase kernels
+int batch_occupancy_euc(int* blocks_per_sm) {
+  const int ph[4] = {kPhEucCellPre, kPhEucNodes, kPhEucCells, kPhEucFinal};
+  const void* fns[4] = {(const void*)kbe_cell_pre, (const void*)kbe_nodes,
+                        (const void*)kbe_cells, (const void*)kbe_final};
+  for (int k = 0; k < 4; ++k) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fns[k], kBatchThreads, 0) !=
+        cudaSuccess)
+      return -1;
+    blocks_per_sm[ph[k]] = n;
+  }
+  return 0;
 }
 
 // One Eucclhyd cycle on stream s (kind ids: 0 begin, 12 cell_pre, 13 nodes,

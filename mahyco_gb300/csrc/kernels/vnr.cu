@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include "../internal.h"
+#include "items.cuh"
 #include "scheme_math.cuh"
 
 namespace hydro {
@@ -2450,49 +2451,24 @@ __global__ void __launch_bounds__(kBX* kBY, 10) k_dual_grad(RunView v, int sweep
 __global__ void __launch_bounds__(kBX* kBY, 12) k_dual_update(RunView v, int sweep) { plain_items(v, DualUpdate{sweep}); }
 __global__ void __launch_bounds__(kBX* kBY, 8) k_final(RunView v) { plain_items(v, Final{}); }
 
-// Batched launches: a persistent grid walks the tile table; every thread of
-// a block works on the same tile (the final phase's block reduction relies
-// on it).  The tile's run view is staged in shared memory by the whole block,
-// so its fields are read where they are used instead of being held in
-// registers for the whole tile.
-template <class F>
-__device__ __forceinline__ void batch_items(const BatchArgs& b, const F& f) {
-  __shared__ RunView sv;
-  constexpr int kWords = sizeof(RunView) / sizeof(unsigned long long);
-  static_assert(sizeof(RunView) % sizeof(unsigned long long) == 0, "RunView size");
-  const int n = *b.ntiles;
-  const int tx = threadIdx.x & ((1 << b.tw_log2) - 1);
-  const int ty = threadIdx.x >> b.tw_log2;
-  const int th = kBatchThreads >> b.tw_log2;
-  for (int t = blockIdx.x; t < n; t += gridDim.x) {
-    const Tile T = b.tiles[t];
-    const unsigned long long* src =
-        reinterpret_cast<const unsigned long long*>(b.views + T.inst);
-    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sv);
-    for (int k = threadIdx.x; k < kWords; k += blockDim.x) dst[k] = src[k];
-    __syncthreads();
-    if (sv.ctrl->active)
-      for (int r = 0; r < b.rows; ++r) f(sv, T.i0 + ty + r * th, T.j0 + tx);
-    __syncthreads();
-  }
-}
-
-__global__ void __launch_bounds__(kBatchThreads, 10) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}); }
-__global__ void __launch_bounds__(kBatchThreads, 8) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}); }
+__global__ void __launch_bounds__(kBatchThreads, 10) kb_lag_nodes(BatchArgs b) { batch_items(b, LagNodes{}, HYDRO_SCHEME_VNR); }
+__global__ void __launch_bounds__(kBatchThreads, 8) kb_lag_cells(BatchArgs b) { batch_items(b, LagCells{}, HYDRO_SCHEME_VNR); }
 __global__ void __launch_bounds__(kBatchThreads) kb_face_grad(BatchArgs b) { batch_items(b, FaceGrad{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_grad(BatchArgs b) { batch_items(b, SweepGradT<2>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_grad_nopb(BatchArgs b) { batch_items(b, SweepGradT<0>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads) kb_sweep_face(BatchArgs b) { batch_items(b, SweepFaceT<3>{b.sweep}); }
 __global__ void __launch_bounds__(kBatchThreads, 8) kb_sweep_update(BatchArgs b) { batch_items(b, SweepUpdateT<2>{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 10) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 12) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}); }
-__global__ void __launch_bounds__(kBatchThreads, 7) kb_final(BatchArgs b) { batch_items(b, Final{}); }
+__global__ void __launch_bounds__(kBatchThreads, 10) kb_dual_grad(BatchArgs b) { batch_items(b, DualGrad{b.sweep}, HYDRO_SCHEME_VNR); }
+__global__ void __launch_bounds__(kBatchThreads, 12) kb_dual_update(BatchArgs b) { batch_items(b, DualUpdate{b.sweep}, HYDRO_SCHEME_VNR); }
+__global__ void __launch_bounds__(kBatchThreads, 7) kb_final(BatchArgs b) { batch_items(b, Final{}, HYDRO_SCHEME_VNR); }
 
-// One thread per run: cycle start (begin + reduction reset) and cycle end.
+// One thread per VNR run: cycle start (begin + reduction reset) and cycle
+// end (Eucclhyd runs of the batch: kbe_begin / kbe_end).
 __global__ void kb_begin(const RunView* views, const int* ninst) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= *ninst) return;
   const RunView v = views[r];
+  if (v.scheme != HYDRO_SCHEME_VNR) return;
   begin_at(v);
   reset_at(v);
 }
@@ -2501,6 +2477,7 @@ __global__ void kb_end(const RunView* views, const int* ninst, int* done) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= *ninst) return;
   const RunView v = views[r];
+  if (v.scheme != HYDRO_SCHEME_VNR) return;
   end_at(v);
   done[r] = v.ctrl->done;
 }
@@ -2622,6 +2599,14 @@ int launch_cycle(const RunView& v, cudaStream_t s, const LaunchHook* hook) {
 
 // Kernels of the batched cycle in launch order (same kind ids as above; the
 // batched cycle start covers kinds 0 and 1).
+void launch_batch_euc(int ph, const BatchLaunch& L, const BatchArgs& a, int grid,
+                      cudaStream_t s);
+int batch_occupancy_euc(int* blocks_per_sm);
+
+// One cycle of every run of a batch: each scheme's Lagrange and final phases
+// over its own runs (their phase kernels skip the other scheme's tiles,
+// and are launched only when the batch holds runs of that scheme), the
+// remap sweeps over all.
 int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
                        const LaunchHook* hook) {
   int nk = 0;
@@ -2633,11 +2618,28 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
     return BatchArgs{L.views, L.tiles[on][w], L.ntiles[on][w],
                      kTileShapes[w].tw_log2, kTileShapes[w].rows, sweep};
   };
+  auto euc = [&](int kind, int ph) {
+    H(kind);
+    launch_batch_euc(ph, L, ph >= 0 ? args(ph, 0) : BatchArgs{}, ph >= 0 ? L.grid[ph] : 0, s);
+    ++nk;
+  };
   const int T = kBatchThreads;
   const int rg = (L.max_inst + T - 1) / T;
-  H(0); kb_begin<<<rg, T, 0, s>>>(L.views, L.ninst); ++nk;
-  H(2); kb_lag_nodes<<<L.grid[kPhLagNodes], T, 0, s>>>(args(kPhLagNodes, 0)); ++nk;
-  H(3); kb_lag_cells<<<L.grid[kPhLagCells], T, 0, s>>>(args(kPhLagCells, 0)); ++nk;
+  if (L.any_vnr) {
+    H(0); kb_begin<<<rg, T, 0, s>>>(L.views, L.ninst); ++nk;
+  }
+  if (L.any_euc) {
+    euc(0, -1);
+    euc(12, kPhEucCellPre);
+  }
+  if (L.any_vnr) {
+    H(2); kb_lag_nodes<<<L.grid[kPhLagNodes], T, 0, s>>>(args(kPhLagNodes, 0)); ++nk;
+  }
+  if (L.any_euc) euc(13, kPhEucNodes);
+  if (L.any_vnr) {
+    H(3); kb_lag_cells<<<L.grid[kPhLagCells], T, 0, s>>>(args(kPhLagCells, 0)); ++nk;
+  }
+  if (L.any_euc) euc(14, kPhEucCells);
   for (int sweep = 1; sweep <= 2; ++sweep) {
     if (L.any_order2) {
       if (L.any_face_grad) {
@@ -2657,11 +2659,19 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
       H(5); kb_sweep_face<<<L.grid[kPhSweepFace], T, 0, s>>>(args(kPhSweepFace, sweep)); ++nk;
     }
     H(6); kb_sweep_update<<<L.grid[kPhSweepUpdate], T, 0, s>>>(args(kPhSweepUpdate, sweep)); ++nk;
-    H(7); kb_dual_grad<<<L.grid[kPhDualGrad], T, 0, s>>>(args(kPhDualGrad, sweep)); ++nk;
-    H(8); kb_dual_update<<<L.grid[kPhDualUpdate], T, 0, s>>>(args(kPhDualUpdate, sweep)); ++nk;
+    if (L.any_vnr) {
+      H(7); kb_dual_grad<<<L.grid[kPhDualGrad], T, 0, s>>>(args(kPhDualGrad, sweep)); ++nk;
+      H(8); kb_dual_update<<<L.grid[kPhDualUpdate], T, 0, s>>>(args(kPhDualUpdate, sweep)); ++nk;
+    }
   }
-  H(9); kb_final<<<L.grid[kPhFinal], T, 0, s>>>(args(kPhFinal, 0)); ++nk;
-  H(10); kb_end<<<rg, T, 0, s>>>(L.views, L.ninst, L.done); ++nk;
+  if (L.any_vnr) {
+    H(9); kb_final<<<L.grid[kPhFinal], T, 0, s>>>(args(kPhFinal, 0)); ++nk;
+  }
+  if (L.any_euc) euc(15, kPhEucFinal);
+  if (L.any_vnr) {
+    H(10); kb_end<<<rg, T, 0, s>>>(L.views, L.ninst, L.done); ++nk;
+  }
+  if (L.any_euc) euc(10, -2);
   H(-1);
   return nk;
 }
@@ -2669,7 +2679,7 @@ int launch_batch_cycle(const BatchLaunch& L, cudaStream_t s,
 // Resident blocks per SM of each batched phase kernel at kBatchThreads
 // threads (for the persistent grid sizes).
 int batch_occupancy(int* blocks_per_sm, int variant) {
-  const void* fns[kNumPhases] = {
+  const void* fns[kPhFinal + 1] = {
       (const void*)kb_lag_nodes,   (const void*)kb_lag_cells,
       (const void*)kb_face_grad,
       (variant & kBatchNoPB) ? (const void*)kb_sweep_grad_nopb : (const void*)kb_sweep_grad,
@@ -2677,14 +2687,14 @@ int batch_occupancy(int* blocks_per_sm, int variant) {
       (const void*)kb_sweep_update,
       (const void*)kb_dual_grad,   (const void*)kb_dual_update,
       (const void*)kb_final};
-  for (int ph = 0; ph < kNumPhases; ++ph) {
+  for (int ph = 0; ph <= kPhFinal; ++ph) {
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fns[ph], kBatchThreads, 0) !=
         cudaSuccess)
       return -1;
     blocks_per_sm[ph] = n;
   }
-  return 0;
+  return batch_occupancy_euc(blocks_per_sm);
 }
 
 }  // namespace hydro

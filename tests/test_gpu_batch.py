@@ -99,6 +99,55 @@ def test_batch_of_reference_decks(M):
             assert_bitwise(f"{c}:{f}", get_field(r, f, spec.nbmat), want[f])
 
 
+def test_batch_of_eucclhyd_reference_decks(M):
+    """Every Eucclhyd golden deck with the remap (orders 1-3, one to three
+    materials, PenteBorne variants, the conservative projection, the flux
+    boundary, Noh, shock bubble, unit tests) in one batch: the Eucclhyd
+    phases run on their own kernels, the sweeps on the shared ones, and each
+    run matches the reference's final state (or stops where it stops)."""
+    ctx = M.Context(0)
+    cases = [c for c in golden_cases()
+             if load_golden(GOLDEN / f"{c}.npz")[0].scheme == M.SCHEME_EUCCLHYD
+             and load_golden(GOLDEN / f"{c}.npz")[0].projection == 1]
+    assert len(cases) > 10
+    loaded = [load_golden(GOLDEN / f"{c}.npz") for c in cases]
+    runs = [M.Run(spec, ctx) for spec, _, _ in loaded]
+    batch = M.Batch(runs)
+    while batch.step(256):
+        pass
+    for c, (spec, meta, want), r in zip(cases, loaded, runs):
+        t, dt, n = r.time()
+        if init_only(meta):
+            code, cell = r.error()
+            assert n <= 1 and (code & STOP_BITS[meta["reference_stop"]]), c
+            continue
+        assert n == int(meta["cycles"]), c
+        assert t == float(meta["t"]), c
+        for f in fields_of(spec):
+            assert_bitwise(f"{c}:{f}", get_field(r, f, spec.nbmat), want[f])
+
+
+def test_batch_mixed_schemes_matches_plain(M):
+    """VNR runs of the seeded mix and Eucclhyd reference decks in one batch,
+    30 cycles: each run equals the same run advanced alone, bit for bit."""
+    ctx = M.Context(0)
+    vnr = [inst.spec(M) for inst in small_mix(6, seed=23)]
+    euc = [load_golden(GOLDEN / f"{c}.npz")[0] for c in golden_cases()
+           if load_golden(GOLDEN / f"{c}.npz")[0].scheme == M.SCHEME_EUCCLHYD
+           and load_golden(GOLDEN / f"{c}.npz")[0].projection == 1
+           and not init_only(load_golden(GOLDEN / f"{c}.npz")[1])][:6]
+    specs = [x for pair in zip(vnr, euc) for x in pair]
+    runs = [M.Run(s, ctx) for s in specs]
+    M.Batch(runs).step(30)
+    for s, rb in zip(specs, runs):
+        alone = M.Run(s, ctx)
+        alone.step(30)
+        for f in fields_of(s):
+            assert_bitwise(f"{s.scheme}:{s.nx}x{s.ny}:{f}", get_field(rb, f, s.nbmat),
+                           get_field(alone, f, s.nbmat))
+        assert rb.time() == alone.time() and rb.error() == alone.error()
+
+
 def test_batch_membership_change(M):
     """The same context batches different run lists one after another; a
     run can leave a batch and continue alone."""

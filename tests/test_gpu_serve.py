@@ -144,3 +144,32 @@ def test_invalid_request_fails_alone(M):
     c = srv.submit(good)
     assert drain(srv, 1)[c][0] == 0
     srv.stop()
+
+
+def test_served_eucclhyd_equals_alone(M):
+    """Eucclhyd requests are served beside VNR ones (the batch's phase
+    kernels of each scheme skip the other's tiles): each result equals the
+    same run alone."""
+    from conftest import GOLDEN, fields_of, golden_cases, init_only, load_golden
+    ctx = M.Context(0)
+    srv = M.Server(ctx, tick_cycles=4)
+    euc = [c for c in golden_cases()
+           if load_golden(GOLDEN / f"{c}.npz")[0].scheme == M.SCHEME_EUCCLHYD
+           and load_golden(GOLDEN / f"{c}.npz")[0].projection == 1
+           and not init_only(load_golden(GOLDEN / f"{c}.npz")[1])][:4]
+    specs = [load_golden(GOLDEN / f"{c}.npz")[0] for c in euc]
+    for r in small_stream(4, 1000.0, seed=5):
+        specs.append(r.inst.spec(M))
+    ids = [srv.submit(s, keep=True) for s in specs]
+    done = drain(srv, len(ids), timeout=600.0)
+    for rid, s in zip(ids, specs):
+        assert done[rid][0] & ~M.ERR_NEGATIVE == 0
+        served = srv.result(rid)
+        alone = M.Run(s, M.Context(0))
+        alone.simulate()
+        for f in fields_of(s):
+            assert_bitwise(f"req{rid}:{f}", get_field(served, f, s.nbmat),
+                           get_field(alone, f, s.nbmat))
+        assert served.time() == alone.time()
+        srv.release(rid)
+    srv.stop()
