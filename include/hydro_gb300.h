@@ -192,8 +192,11 @@ int hydro_batch_timed(hydro_ctx* ctx, hydro_run* const* runs, int nruns,
 int hydro_batch_profile(hydro_ctx* ctx, hydro_run* const* runs, int nruns,
                         int ncycles, double* ms, long long* launches,
                         int nkinds);
-/* Tile width and height (items) and grid (blocks) chosen per batched phase;
- * returns 1 once a timed tuning pass has chosen them. */
+/* Tile width and height (items) and grid (blocks) chosen per batched phase
+ * (nphases >= 13: VNR Lagrange nodes, cells, face gradients, slopes, faces,
+ * update, dual slopes, dual update, final, then Eucclhyd cell pre-pass,
+ * nodes, cells, final); returns 1 once a timed tuning pass has chosen
+ * them. */
 int hydro_batch_config(hydro_ctx* ctx, int* width, int* height, int* grid,
                        int nphases);
 int hydro_batch_set_tuning(hydro_ctx* ctx, int enable);

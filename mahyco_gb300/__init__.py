@@ -402,7 +402,7 @@ class Run:
 
 BATCH_PHASES = ("lag_nodes", "lag_cells", "face_grad", "sweep_grad",
                 "sweep_face", "sweep_update", "dual_grad", "dual_update",
-                "final")
+                "final", "euc_cell_pre", "euc_nodes", "euc_cells", "euc_final")
 
 
 class Batch:
