@@ -177,7 +177,9 @@ struct Ctrl {
   int done;             // reference loop condition failed
   int active;           // this cycle runs
   int x_then_y;         // direction of the first sweep of this cycle
-  int pad;
+  int nout_general;     // set up: some outer normal of the Euler mesh is not
+                        // the Cartesian -1 / +1 (L.x, R.x, B.y, T.y), so the
+                        // kernels load them (nout_at)
   unsigned long long dt_min_bits;  // ordered encoding of the dt partial min
   unsigned long long pmax_bits;    // ordered encoding of max pressure
   double pmax_prev;                // max pressure of the state at cycle start

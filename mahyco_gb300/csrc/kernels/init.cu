@@ -260,7 +260,9 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_cells_vnr(RunView v, int t, 
       const double* b = X[ends[q][1]];
       const double d0 = 0.5 * (a[0] + b[0]) - Xc[0], d1 = 0.5 * (a[1] + b[1]) - Xc[1];
       const double nr = norm2(d0, d1);
-      const_cast<double*>(v.nout)[q * P + c] = (q < 2 ? d0 : d1) / nr;
+      const double n = (q < 2 ? d0 : d1) / nr;
+      const_cast<double*>(v.nout)[q * P + c] = n;
+      if (ubits(n) != ubits((q & 1) ? 1.0 : -1.0)) atomicOr(&v.ctrl->nout_general, 1);
     }
     // the Lagrangian geometry of the cell at rest, by the Lagrange kernel's
     // own function from the Euler coordinates its nodes keep then
@@ -611,7 +613,9 @@ __global__ void __launch_bounds__(kBX* kBY) kd_init_cells_euc(RunView v, int t, 
     const double* a = X[ends[q][0]];
     const double* b = X[ends[q][1]];
     const double d[2] = {0.5 * (a[0] + b[0]) - x0, 0.5 * (a[1] + b[1]) - x1};
-    const_cast<double*>(v.nout)[q * P + c] = (q < 2 ? d[0] : d[1]) / nrm(d);
+    const double n = (q < 2 ? d[0] : d[1]) / nrm(d);
+    const_cast<double*>(v.nout)[q * P + c] = n;
+    if (ubits(n) != ubits((q & 1) ? 1.0 : -1.0)) atomicOr(&v.ctrl->nout_general, 1);
   }
   v.rho[c] = rho;
   v.e[c] = e;

@@ -38,6 +38,13 @@ constexpr int kBX = 32, kBY = 4;  // 2D cell / node tiles
 #define DV __device__ __forceinline__
 
 DV double ld(const double* p, long long i) { return __ldg(p + i); }
+
+// Outer normal q (L.x, R.x, B.y, T.y) of cell c: the Cartesian -1 / +1 the
+// set-up found in every cell, or the stored plane where it did not
+DV double nout_at(const RunView& v, int q, long long c) {
+  if (v.ctrl->nout_general) return __ldg(v.nout + q * v.pitch + c);
+  return (q & 1) ? 1.0 : -1.0;
+}
 DV unsigned ld_u8(const unsigned char* p, long long i) { return __ldg(p + i); }
 
 // Per-material options read by select rather than by a dynamic index, so a
@@ -916,14 +923,14 @@ struct SweepGradT {
       if (dirx) {
         fa_v = fnv_vertical(v, n0, n0 + v.nx + 1);          // left face
         fb_v = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);      // right face
-        Fa = mul_pm1(fa_v, ld(v.nout, 0 * P + c));
-        Fb = mul_pm1(fb_v, ld(v.nout, 1 * P + c));
+        Fa = mul_pm1(fa_v, nout_at(v, 0, c));
+        Fb = mul_pm1(fb_v, nout_at(v, 1, c));
         flen = half(ld(v.flv, i) + ld(v.flv, i));
       } else {
         fa_v = fnv_horizontal(v, n0, n0 + 1);               // bottom face
         fb_v = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);  // top face
-        Fa = mul_pm1(fa_v, ld(v.nout, 2 * P + c));
-        Fb = mul_pm1(fb_v, ld(v.nout, 3 * P + c));
+        Fa = mul_pm1(fa_v, nout_at(v, 2, c));
+        Fb = mul_pm1(fb_v, nout_at(v, 3, c));
         flen = half(ld(v.flh, j) + ld(v.flh, j));
       }
       const double fdual = half(fa_v + fb_v);
@@ -1452,7 +1459,7 @@ struct SweepUpdateT {
       const double fl = ld(v.flv, i);
       const double va = fnv_vertical(v, n0, n0 + v.nx + 1);
       const double vb = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);
-      const double na = ld(v.nout, 0 * P + c), nb_ = ld(v.nout, 1 * P + c);
+      const double na = nout_at(v, 0, c), nb_ = nout_at(v, 1, c);
       nrm[0] = na;
       nrm[1] = nb_;
       if (v.pb == 0) {
@@ -1472,7 +1479,7 @@ struct SweepUpdateT {
       const double fl = ld(v.flh, j);
       const double va = fnv_horizontal(v, n0, n0 + 1);
       const double vb = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);
-      const double na = ld(v.nout, 2 * P + c), nb_ = ld(v.nout, 3 * P + c);
+      const double na = nout_at(v, 2, c), nb_ = nout_at(v, 3, c);
       nrm[0] = na;
       nrm[1] = nb_;
       if (v.pb == 0) {
