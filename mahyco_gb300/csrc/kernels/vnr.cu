@@ -1443,6 +1443,8 @@ struct SweepUpdateT {
     const bool from_ul = (sweep == 2) && lowo && v.u1s[c] != 0;
     const double* Uin = (sweep == 1 || from_ul) ? v.UL : v.U1;
     const double dt = C.dt_n;
+    // PenteBorne, known at compile time for the kernel that forms its faces
+    const int pbv = (FACES == 1) ? 1 : v.pb;
     // the two faces perpendicular to the sweep, in getNeighbourCells order
     // (below before above, left before right); faces parallel to the sweep
     // contribute 0 * phiFace and are skipped.
@@ -1462,7 +1464,7 @@ struct SweepUpdateT {
       const double na = nout_at(v, 0, c), nb_ = nout_at(v, 1, c);
       nrm[0] = na;
       nrm[1] = nb_;
-      if (v.pb == 0) {
+      if (pbv == 0) {
         // ((n * u_f) * L) * dt exactly; a face at rest gives a zero on the
         // integer pipe
         coef[0] = mulz(mulz(mulz(na, va), fl), dt);
@@ -1482,7 +1484,7 @@ struct SweepUpdateT {
       const double na = nout_at(v, 2, c), nb_ = nout_at(v, 3, c);
       nrm[0] = na;
       nrm[1] = nb_;
-      if (v.pb == 0) {
+      if (pbv == 0) {
         // ((n * u_f) * L) * dt exactly; a face at rest gives a zero on the
         // integer pipe
         coef[0] = mulz(mulz(mulz(na, va), fl), dt);
@@ -1543,7 +1545,7 @@ struct SweepUpdateT {
     const bool cfin = is_finite(coef[0]) && is_finite(coef[1]);
     const bool dual_share = v.scheme != HYDRO_SCHEME_EUCCLHYD && v.dual_method != 2;
     const double rl = (dual_share && v.dual_method == 1) ? v.rL[c] : 0.;
-    const double vl = (sweep == 1 && v.pb != 1) ? v.vL[c] : 0.;
+    const double vl = (sweep == 1 && pbv != 1) ? v.vL[c] : 0.;
     // Both faces with integral planes flagged all +0.0 (PenteBorne face
     // values formed here, each +0 - +0 = +0), finite coefficients, normals
     // and rL, no boundary flux, no NaN input: every flux is the zero of
