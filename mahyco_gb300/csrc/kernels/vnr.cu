@@ -1558,7 +1558,15 @@ struct SweepUpdateT {
     const bool still_ok = cfin && is_finite(rl) && is_finite(nrm[0]) && is_finite(nrm[1]);
     bool zface = form && still_ok && bcf == 0 && (!has[0] || (lf[0].zv && lf[0].zr)) &&
                  (!has[1] || (lf[1].zv && lf[1].zr));
-    if (zface) {
+    // Such a VNR cell in the first sweep at orders 1-2, or in the second one
+    // where its components come from UL (the first left them unchanged),
+    // stores none of them (only the flag saying they are unchanged), and
+    // keeps its Phi: its components are not even read.  (A NaN component
+    // then keeps its bits, where the per-component path would give the
+    // subtraction's NaN; the final's NaN check stops the run either way.)
+    const bool zskip =
+        zface && v.scheme == HYDRO_SCHEME_VNR && ((sweep == 1 && lowo) || from_ul);
+    if (zface && !zskip) {
   #pragma unroll
       for (int k = 0; k < kMaxComp; ++k) {
         if (k >= ncomp) break;
