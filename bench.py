@@ -125,6 +125,11 @@ def algorithmic_bytes(kind: str, nb: int, pb: bool, rest: bool = False) -> int:
         "k_dual_update": (2 * nb + 2 + 8) + 5,
         "k_final": (nc + 2) + (6 + 7 * nb + 1),
     }
+    if rest:
+        # a pure cell at rest leaves out the stores of the values it read
+        # and found unchanged: divergence, sound speed, the root's argument
+        # and its material's pseudo-viscosity
+        table["k_lag_cells"] -= 4
     if rest and pb:
         # a cell at rest: the node velocity along the sweep in / its flag
         # byte out; U, 2 node velocities, 2 outer normals and the flag bytes

@@ -192,6 +192,7 @@ struct Ctrl {
   double t_out;
   int pause, pause_skip, paused, pad3;
   double rdt_np1;  // 1.0 / dt_np1, formed once per cycle (VNR divergence)
+  double dt_vel;   // 0.5 * (dt_np1 + dt_n), formed once per cycle (VNR velocity)
 };
 
 #ifdef __CUDACC__

@@ -348,6 +348,25 @@ HD double addz(double a, double b) {
   if ((ua ^ ub) == ~kMag && ma < kInfBits) return 0.0;  // a + (-a)
   return a + b;
 }
+// The bits of a + b when one of addz's shortcuts gives them; false when the
+// sum needs the FP64 addition (which this form never issues).
+HD bool addz_bits(double a, double b, unsigned long long& r) {
+  const unsigned long long ua = ubits(a), ub = ubits(b);
+  const unsigned long long ma = ua & kMag, mb = ub & kMag;
+  if (mb == 0 && ma <= kInfBits) {
+    r = (ma == 0) ? (ua & ub) : ua;
+    return true;
+  }
+  if (ma == 0 && mb <= kInfBits) {
+    r = ub;
+    return true;
+  }
+  if ((ua ^ ub) == ~kMag && ma < kInfBits) {
+    r = 0ull;
+    return true;
+  }
+  return false;
+}
 // a - b = a + (-b) exactly; the sign of b is flipped on the integer pipe
 // (a negated double operand may otherwise cost an FP64 instruction)
 HD double subz(double a, double b) {

@@ -47,6 +47,16 @@ DV double nout_at(const RunView& v, int q, long long c) {
 }
 DV unsigned ld_u8(const unsigned char* p, long long i) { return __ldg(p + i); }
 
+// Store of a value this thread read from the same address earlier in the
+// kernel: left out when the bits are the ones already there, so the location
+// ends up holding the same bits either way.  At rest most Lagrange outputs
+// that are also inputs (velocity, divergence, sound speed, the root's
+// argument, the pseudo-viscosity) come back unchanged, and a sector none of
+// whose stores happen is not written back to HBM.
+DV void st_if_new(double* a, double old_v, double new_v) {
+  if (ubits(new_v) != ubits(old_v)) *a = new_v;
+}
+
 // Per-material options read by select rather than by a dynamic index, so a
 // RunView copied into registers (batched launches) is never spilled whole to
 // local memory.
@@ -88,6 +98,8 @@ __device__ __forceinline__ void begin_at(const RunView& v) {
   }
   C.t_np1 = C.t_n + C.dt_np1;
   C.rdt_np1 = 1.0 / C.dt_np1;
+  // updateVelocity's time step (PhaseLagrange.cc:167-197)
+  C.dt_vel = half(C.dt_np1 + C.dt_n);
 }
 
 __device__ __forceinline__ void reset_at(const RunView& v) {
@@ -190,8 +202,14 @@ struct LagNodes {
     const double m = div_pow2(msum, k);  // msum / k, k in {1, 2, 4}
 
     double ux = v.u[p], uy = v.u[v.npitch + p];
+    // updatePosition (PhaseLagrange.cc:203-208) starts from the cycle's start
+    // positions (the Euler mesh with the remap); read with the other inputs,
+    // before any store (a store would order the later loads behind it)
+    const double X0 = v.XN ? v.XN[p] : ld(v.xs, j);
+    const double X1 = v.XN ? v.XN[v.npitch + p] : ld(v.ys, i);
+    double xl0, xl1;
     if (v.sans_lagrange == 0) {
-      const double dt = half(C.dt_np1 + C.dt_n);
+      const double dt = C.dt_vel;  // 0.5 * (dt^{n+1} + dt^n), formed once per cycle
       // s = dt / m, formed only when a force is not exactly zero: with dt and
       // m positive and of moderate size, s * (+-0) is +-0 itself (the force
       // sums cancel exactly on a mesh at rest)
@@ -257,99 +275,121 @@ struct LagNodes {
         }
       };
       const double u0x = ux, u0y = uy;
-      double r0, r1;
-      if (i > 0 && i < v.ny && j > 0 && j < v.nx) {
-        // one pressure in the four cells around a node whose corner normals
-        // cancel exactly (nsym, set up with the derivation): the sum is +0
-        // without the products
-        bool zero = false;
-        if (!v.XN && ld_u8(v.nsym, p)) {  // a flag of the Euler mesh
-          const unsigned long long w0 = ubits(addz(v.p[cells[0]], v.q[cells[0]]));
-          constexpr unsigned long long kMod = 1523ull << 52;  // 2^500
-          zero = (w0 & kMag) < kMod;
-          for (int t = 1; t < 4 && zero; ++t)
-            zero = ubits(addz(v.p[cells[t]], v.q[cells[t]])) == w0;
-        }
-        if (zero) {
-          r0 = 0.0;
-          r1 = 0.0;
-        } else {
-          force(false, 0., 0., r0, r1);
-        }
-        ux = addz(u0x, step(r0));
-        uy = addz(u0y, step(r1));
+      const bool inner = i > 0 && i < v.ny && j > 0 && j < v.nx;
+      // one pressure in the four cells around an inner node whose corner
+      // normals cancel exactly (nsym, set up with the derivation): the force
+      // sum is +0 without the products.  The four p + q are compared where
+      // the sums are exact on the integer pipe (p or q a zero); elsewhere the
+      // products run, and give the same +0.
+      bool zero = false;
+      if (inner && !v.XN && ld_u8(v.nsym, p)) {  // a flag of the Euler mesh
+        constexpr unsigned long long kMod = 1523ull << 52;  // 2^500
+        unsigned long long w0 = 0ull, w = 0ull;
+        zero = addz_bits(v.p[cells[0]], v.q[cells[0]], w0) && (w0 & kMag) < kMod;
+  #pragma unroll
+        for (int t = 1; t < 4; ++t)
+          zero = zero && addz_bits(v.p[cells[t]], v.q[cells[t]], w) && w == w0;
+      }
+      // An inner node at rest: a zero force sum, so s = dt / m is not formed
+      // (s * (+0) = +0); a zero velocity, (+-0) + (+0) = +0; dt^{n+1}
+      // positive and finite, so X + dt^{n+1} * (+0) = X + (+0) is X (+0 for a
+      // zero X, X not NaN).  One branch for the whole node: the general
+      // path's FP64 operations, if-converted, would be issued for it too.
+      const bool rest = zero && s_easy && ((ubits(u0x) | ubits(u0y)) & kMag) == 0 &&
+                        pos(C.dt_np1) && is_finite(C.dt_np1) && !is_nan(X0) && !is_nan(X1);
+      if (rest) {
+        ux = 0.0;
+        uy = 0.0;
+        xl0 = iszero(X0) ? 0.0 : X0;
+        xl1 = iszero(X1) ? 0.0 : X1;
         if (v.vout) {  // m_x/y_velocity, inner nodes only (PhaseLagrange.cc:193)
           v.vout[p] = ux;
           v.vout[v.npitch + p] = uy;
         }
-      }
-      // sides in the reference's order: bottom, top, left, right
-      if (i == 0) {
-        if (v.bc_bottom == kBcSym) {
-          force(true, 1.0, 0.0, r0, r1);
+      } else {
+        double r0, r1;
+        if (inner) {
+          if (zero) {
+            r0 = 0.0;
+            r1 = 0.0;
+          } else {
+            force(false, 0., 0., r0, r1);
+          }
           ux = addz(u0x, step(r0));
           uy = addz(u0y, step(r1));
-        } else if (v.bc_bottom == kBcImposed) {
-          ux = v.v_bottom[0];
-          uy = v.v_bottom[1];
+          if (v.vout) {
+            v.vout[p] = ux;
+            v.vout[v.npitch + p] = uy;
+          }
         }
-      }
-      if (i == v.ny) {
-        if (v.bc_top == kBcSym) {
-          force(true, 1.0, 0.0, r0, r1);
-          ux = addz(u0x, step(r0));
-          uy = addz(u0y, step(r1));
-        } else if (v.bc_top == kBcImposed) {
-          ux = v.v_top[0];
-          uy = v.v_top[1];
+        // sides in the reference's order: bottom, top, left, right
+        if (i == 0) {
+          if (v.bc_bottom == kBcSym) {
+            force(true, 1.0, 0.0, r0, r1);
+            ux = addz(u0x, step(r0));
+            uy = addz(u0y, step(r1));
+          } else if (v.bc_bottom == kBcImposed) {
+            ux = v.v_bottom[0];
+            uy = v.v_bottom[1];
+          }
         }
-      }
-      if (j == 0) {
-        if (v.bc_left == kBcSym) {
-          force(true, 0.0, 1.0, r0, r1);
-          ux = addz(u0x, step(r0));
-          uy = addz(u0y, step(r1));
-        } else if (v.bc_left == kBcImposed) {
-          ux = v.v_left[0];
-          uy = v.v_left[1];
+        if (i == v.ny) {
+          if (v.bc_top == kBcSym) {
+            force(true, 1.0, 0.0, r0, r1);
+            ux = addz(u0x, step(r0));
+            uy = addz(u0y, step(r1));
+          } else if (v.bc_top == kBcImposed) {
+            ux = v.v_top[0];
+            uy = v.v_top[1];
+          }
         }
-      }
-      if (j == v.nx) {
-        if (v.bc_right == kBcSym) {
-          force(true, 0.0, 1.0, r0, r1);
-          ux = addz(u0x, step(r0));
-          uy = addz(u0y, step(r1));
-        } else if (v.bc_right == kBcImposed) {
-          ux = v.v_right[0];
-          uy = v.v_right[1];
+        if (j == 0) {
+          if (v.bc_left == kBcSym) {
+            force(true, 0.0, 1.0, r0, r1);
+            ux = addz(u0x, step(r0));
+            uy = addz(u0y, step(r1));
+          } else if (v.bc_left == kBcImposed) {
+            ux = v.v_left[0];
+            uy = v.v_left[1];
+          }
         }
-      }
-      // corners (ConditionsLimites.cc:133-184)
-      const bool top = (i == v.ny), bot = (i == 0), lft = (j == 0), rgt = (j == v.nx);
-      if ((top || bot) && (lft || rgt)) {
-        const int bv = top ? v.bc_top : v.bc_bottom;
-        const int bh = lft ? v.bc_left : v.bc_right;
-        const double vh0 = lft ? v.v_left[0] : v.v_right[0];
-      const double vh1 = lft ? v.v_left[1] : v.v_right[1];
-        if (bv == kBcSym && bh == kBcSym) {
-          ux = 0.0;
-          uy = 0.0;
-        } else if (bv == kBcImposed && bh == kBcImposed) {
-          ux = vh0;
-          uy = vh1;
+        if (j == v.nx) {
+          if (v.bc_right == kBcSym) {
+            force(true, 0.0, 1.0, r0, r1);
+            ux = addz(u0x, step(r0));
+            uy = addz(u0y, step(r1));
+          } else if (v.bc_right == kBcImposed) {
+            ux = v.v_right[0];
+            uy = v.v_right[1];
+          }
         }
+        // corners (ConditionsLimites.cc:133-184)
+        const bool top = (i == v.ny), bot = (i == 0), lft = (j == 0), rgt = (j == v.nx);
+        if ((top || bot) && (lft || rgt)) {
+          const int bv = top ? v.bc_top : v.bc_bottom;
+          const int bh = lft ? v.bc_left : v.bc_right;
+          const double vh0 = lft ? v.v_left[0] : v.v_right[0];
+          const double vh1 = lft ? v.v_left[1] : v.v_right[1];
+          if (bv == kBcSym && bh == kBcSym) {
+            ux = 0.0;
+            uy = 0.0;
+          } else if (bv == kBcImposed && bh == kBcImposed) {
+            ux = vh0;
+            uy = vh1;
+          }
+        }
+        xl0 = addz(X0, mulz(C.dt_np1, ux));
+        xl1 = addz(X1, mulz(C.dt_np1, uy));
       }
-      v.u[p] = ux;
-      v.u[v.npitch + p] = uy;
+      st_if_new(v.u + p, u0x, ux);
+      st_if_new(v.u + v.npitch + p, u0y, uy);
+    } else {
+      xl0 = addz(X0, mulz(C.dt_np1, ux));
+      xl1 = addz(X1, mulz(C.dt_np1, uy));
     }
-    // stored last: a store earlier would order the force loads behind it;
-    // updatePosition (PhaseLagrange.cc:203-208) from the cycle's start
-    // positions (the Euler mesh with the remap)
-    const double X0 = v.XN ? v.XN[p] : ld(v.xs, j);
-    const double X1 = v.XN ? v.XN[v.npitch + p] : ld(v.ys, i);
     v.node_mass[p] = m;
-    v.XL[p] = addz(X0, mulz(C.dt_np1, ux));
-    v.XL[v.npitch + p] = addz(X1, mulz(C.dt_np1, uy));
+    v.XL[p] = xl0;
+    v.XL[v.npitch + p] = xl1;
   }
 };
 
@@ -528,7 +568,7 @@ struct LagCells {
         }
       }
       if (dgt(q_new, C.pmax_prev)) q_new = C.pmax_prev;
-      v.divu[c] = divu_new;
+      st_if_new(v.divu + c, divu_old, divu_new);
       // energies (updateEnergy) and EOS
       e_new = 0.;
       bool e_first = true;  // 0.0 + x is plus_zero(x)
@@ -539,7 +579,7 @@ struct LagCells {
         if (m >= nbl) break;
         const double qm_old = qm_o[m];
         const double qm_new = mul_frac(f[m], q_new);
-        v.qm[mat(m) * P + c] = qm_new;
+        st_if_new(v.qm + mat(m) * P + c, qm_old, qm_new);
         const double rn = rhom_new[m], ro = rho_o[m];
         em_new[m] = 0.;
         if (dgt(rn, thr) && dgt(ro, thr)) {
@@ -632,8 +672,8 @@ struct LagCells {
       }
       if (void_mask) e_new = void_energy(void_mask, e_new, mf[0], mf[1], mf[2], em_new[0],
                                          em_new[1], em_new[2]);
-      v.c[c] = cc;
-      v.sarg[c] = sarg_new;
+      st_if_new(v.c + c, c_old, cc);
+      st_if_new(v.sarg + c, sarg_old, sarg_new);
       if (v.projection == 0) {
         // Without the remap no later kernel forms the state after this
         // phase: its densities, energies, pseudo-viscosity, and the
@@ -2060,8 +2100,8 @@ __device__ __forceinline__ bool final_single(const RunView& v, Ctrl& C, long lon
   v.rho[c] = rho;
   v.e[c] = e;
   v.p[c] = pres;
-  v.c[c] = cc;
-  v.sarg[c] = e;
+  st_if_new(v.c + c, c_in, cc);
+  st_if_new(v.sarg + c, sarg_in, e);
   MAT_LOOP(m, 0) {
     const bool here = m == p;
     v.cmassm[m * P + c] = here ? cmass : from_bits(ubits(cmass) & kS);
@@ -2226,8 +2266,8 @@ __device__ __forceinline__ void final_cell(const RunView& v, Ctrl& C, int i,
   v.rho[c] = rho;
   v.e[c] = e;
   v.p[c] = p;
-  v.c[c] = cc;
-  v.sarg[c] = sarg_out;
+  st_if_new(v.c + c, c_in, cc);
+  st_if_new(v.sarg + c, sarg_in, sarg_out);
   MAT_LOOP(m, 0) {
     v.fm[m * P + c] = f[m];
     v.mfm[m * P + c] = mf[m];
