@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "fetch.h"
 #include "init.h"
 #include "runtime.h"
 
@@ -201,6 +202,13 @@ int hydro_ctx_create(int device, size_t budget, hydro_ctx** out) {
     delete c;
     return fail(-3, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
   }
+  // the pinned staging and host copy threads of hydro_run_fetch, set up
+  // with the context rather than inside a run's first fetch
+  if (int rc = create_fetch_stage(c->num_sms, &c->fetch)) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return rc;
+  }
   *out = c;
   return 0;
 }
@@ -212,6 +220,9 @@ void hydro_ctx_destroy(hydro_ctx* c) {
   c->serve = nullptr;
   destroy_plan(c->plan);
   c->plan = nullptr;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  destroy_fetch_stage(c->fetch);
+  c->fetch = nullptr;
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -631,15 +642,14 @@ static int fetch_dump(hydro_run* r, const char* f, int k, double* dst, size_t n)
     for (size_t i = 0; i < n; ++i) dst[i] = 0.0;
     return 0;
   }
-  cudaError_t e = cudaMemcpyAsync(dst, plane, n * sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  const int rc = fetch_planes(r->ctx, FetchPlanes{{plane, nullptr, nullptr}, 1}, (long long)n,
+                              dst, &r->kernels_launched);
   if (scratch) {
-    const cudaError_t e2 = cudaFree(scratch);
-    if (e == cudaSuccess) e = e2;
+    const cudaError_t e = cudaFree(scratch);
+    if (!rc && e != cudaSuccess)
+      return fail(-100, std::string("fetch ") + f + ": " + cudaGetErrorString(e));
   }
-  if (e != cudaSuccess)
-    return fail(-100, std::string("fetch ") + f + ": " + cudaGetErrorString(e));
-  return 0;
+  return rc;
 }
 
 size_t hydro_run_field_size(hydro_run* r, const char* f) {
@@ -675,31 +685,22 @@ int hydro_run_fetch(hydro_run* r, const char* f, double* dst, size_t n) {
   CUDA_TRY(cudaSetDevice(r->ctx->device));
   cudaStream_t s = r->ctx->stream;
   const RunView& v = r->v;
-  const long long nc = v.nc, nn = v.nn;
-  auto get = [&](const double* src, long long cnt, std::vector<double>& out) {
-    out.resize(cnt);
-    return cudaMemcpyAsync(out.data(), src, cnt * sizeof(double),
-                           cudaMemcpyDeviceToHost, s);
-  };
+  const long long nn = v.nn;
   if (const int k = dump_plane(r, f); k >= 0) return fetch_dump(r, f, k, dst, n);
-  std::vector<double> tmp;
-  const double* one = nullptr;
-  if (!strcmp(f, "density")) one = v.rho;
-  else if (!strcmp(f, "pressure")) one = v.p;
-  else if (!strcmp(f, "energy")) one = v.e;
-  else if (!strcmp(f, "sound_speed")) one = v.c;
-  else if (!strcmp(f, "pseudo")) one = v.q;
-  else if (!strcmp(f, "divu")) one = v.divu;
-  else if (!strcmp(f, "cell_mass")) one = v.cell_mass;
+  FetchPlanes g{{nullptr, nullptr, nullptr}, 1};
+  if (!strcmp(f, "density")) g.p[0] = v.rho;
+  else if (!strcmp(f, "pressure")) g.p[0] = v.p;
+  else if (!strcmp(f, "energy")) g.p[0] = v.e;
+  else if (!strcmp(f, "sound_speed")) g.p[0] = v.c;
+  else if (!strcmp(f, "pseudo")) g.p[0] = v.q;
+  else if (!strcmp(f, "divu")) g.p[0] = v.divu;
+  else if (!strcmp(f, "cell_mass")) g.p[0] = v.cell_mass;
   else if (!strcmp(f, "node_mass")) {
     launch_node_mass(v, s);
-    one = v.node_mass;
+    g.p[0] = v.node_mass;
   }
-  if (one) {
-    CUDA_TRY(cudaMemcpyAsync(dst, one, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    return 0;
-  }
+  // per-material planes, three values per cell (zeros past the run's
+  // materials)
   const double* planes = nullptr;
   if (!strcmp(f, "density_env")) planes = v.rhom;
   else if (!strcmp(f, "energy_env")) planes = v.em;
@@ -707,12 +708,8 @@ int hydro_run_fetch(hydro_run* r, const char* f, double* dst, size_t n) {
   else if (!strcmp(f, "fracvol_env")) planes = v.fm;
   else if (!strcmp(f, "mass_fraction_env")) planes = v.mfm;
   if (planes) {
-    CUDA_TRY(get(planes, v.nbmat * v.pitch, tmp));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    for (long long c = 0; c < nc; ++c)
-      for (int m = 0; m < 3; ++m)
-        dst[3 * c + m] = m < v.nbmat ? tmp[m * v.pitch + c] : 0.0;
-    return 0;
+    g.k = 3;
+    for (int m = 0; m < v.nbmat && m < 3; ++m) g.p[m] = planes + m * v.pitch;
   }
   if (!strcmp(f, "node_coord")) {
     // the mesh the next output shows: the moving positions of a run without
@@ -725,33 +722,14 @@ int hydro_run_fetch(hydro_run* r, const char* f, double* dst, size_t n) {
       }
       return 0;
     }
-    CUDA_TRY(get(v.XN, 2 * v.npitch, tmp));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    for (long long p = 0; p < nn; ++p) {
-      dst[2 * p] = tmp[p];
-      dst[2 * p + 1] = tmp[v.npitch + p];
-    }
-    return 0;
+    g = FetchPlanes{{v.XN, v.XN + v.npitch, nullptr}, 2};
+  } else if (!strcmp(f, "node_velocity")) {
+    g = FetchPlanes{{v.u, v.u + v.npitch, nullptr}, 2};
+  } else if (!strcmp(f, "cell_velocity")) {
+    g = FetchPlanes{{v.uc, v.uc + v.pitch, nullptr}, 2};
   }
-  if (!strcmp(f, "node_velocity")) {
-    CUDA_TRY(get(v.u, 2 * v.npitch, tmp));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    for (long long p = 0; p < nn; ++p) {
-      dst[2 * p] = tmp[p];
-      dst[2 * p + 1] = tmp[v.npitch + p];
-    }
-    return 0;
-  }
-  if (!strcmp(f, "cell_velocity")) {
-    CUDA_TRY(get(v.uc, 2 * v.pitch, tmp));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    for (long long c = 0; c < nc; ++c) {
-      dst[2 * c] = tmp[c];
-      dst[2 * c + 1] = tmp[v.pitch + c];
-    }
-    return 0;
-  }
-  return fail(-2, std::string("unknown field ") + f);
+  if (!g.p[0] && !planes) return fail(-2, std::string("unknown field ") + f);
+  return fetch_planes(r->ctx, g, (long long)(n / g.k), dst, &r->kernels_launched);
 }
 
 // Times ncycles cycles (graph replays) between two CUDA events recorded on

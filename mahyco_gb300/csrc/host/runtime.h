@@ -49,6 +49,9 @@ size_t run_arena_bytes(const hydro_spec& spec);
 
 struct BatchPlan;
 struct ServeState;
+struct FetchStage;
+int create_fetch_stage(int num_sms, FetchStage** out);
+void destroy_fetch_stage(FetchStage* st);
 void destroy_plan(BatchPlan* p);
 void plan_forget_run(BatchPlan* p, const struct ::hydro_run* r);
 void destroy_serve(ServeState* s);
@@ -64,6 +67,7 @@ struct hydro_ctx {
   std::mutex mu;
   hydro::BatchPlan* plan = nullptr;   // batch engine (lazily created)
   hydro::ServeState* serve = nullptr; // serving loop (lazily created)
+  hydro::FetchStage* fetch = nullptr; // pinned staging of hydro_run_fetch
   int batch_tuning = 1;               // autotune the batched launches
 };
 

@@ -79,3 +79,20 @@ def test_initial_state_mixed_row_and_triple_point(M, port_lib):
     t.cfl, t.final_time, t.dt_min, t.space_order = 0.4, 100.0, 1e-12, 2
     t.projection_order, t.limiter, t.init_variant, t.max_cycles = 3, M.LIMITERS["superBee"], 3, 5
     compare_initial(M, t, "triple-point")
+
+
+def test_initial_state_fetched_in_several_chunks(M, port_lib):
+    """Fields larger than one pinned staging chunk (8 MiB), with sizes that
+    leave a ragged last chunk, come back in the caller's layout: one, two
+    and three planes per value, a material slot past the run's materials
+    read as zero."""
+    from mahyco_gb300.workloads import Instance
+    import bench
+    sod = Instance("sod", 1100, 1001, 2, "superBee", 5, "X").spec(M)
+    compare_initial(M, sod, "sod-1100x1001")
+    run = M.Run(sod)
+    for f in ("fracvol_env", "density_env", "energy_env"):
+        third = run.fetch(f).reshape(-1, 3)[:, 2]
+        assert not np.any(third.view(np.uint64)), f
+    tp = bench.triple_point_spec(M, 1030, 1010, cycles=5)
+    compare_initial(M, tp, "triple-point-1030x1010")
