@@ -317,11 +317,12 @@ HD double dbl(double x) {
   if ((b << 1) == 0ull) return x;  // 2 * +-0 = +-0
   return dbl_slow(x);
 }
-// x + 0.0 (turns -0 into +0; NaN through the FP64 addition)
+// x + 0.0 (turns -0 into +0; NaN through the FP64 addition, behind a call:
+// inline, the select would issue the addition for every value)
 HD double plus_zero(double x) {
   const unsigned long long b = ubits(x);
   if (b == 0x8000000000000000ull) return 0.0;
-  return is_nan(x) ? x + 0.0 : x;
+  return is_nan(x) ? dadd_call(x, 0.0) : x;
 }
 // f * x for a volume or mass fraction f: in single-material cells the
 // fractions are exactly 1 or +0, and the product is x or the IEEE product's
@@ -330,6 +331,8 @@ HD double mul_frac(double f, double x) {
   const unsigned long long b = ubits(f);
   if (b == 0x3ff0000000000000ull) return x;
   if (b == 0ull && is_finite(x)) return from_bits(ubits(x) & ~kMag);
+  // a mixed cell (inline: behind a call, the callers' register allocation
+  // around it costs the Lagrange cell kernel more than the product saves)
   return f * x;
 }
 
@@ -512,7 +515,7 @@ HD double mul_pm1(double x, double n) {
   const unsigned long long b = ubits(n);
   if (b == 0x3ff0000000000000ull) return x;
   if (b == 0xbff0000000000000ull) return from_bits(ubits(x) ^ 0x8000000000000000ull);
-  return x * n;
+  return dmul_call(x, n);
 }
 
 // k * x for a small integer k in {0, 1, 2} (k = 0: the IEEE product's signed
@@ -520,7 +523,7 @@ HD double mul_pm1(double x, double n) {
 HD double mul_012(int k, double x) {
   if (k == 1) return x;
   if (k == 2) return dbl(x);
-  return is_finite(x) ? from_bits(ubits(x) & ~kMag) : 0.0 * x;
+  return is_finite(x) ? from_bits(ubits(x) & ~kMag) : dmul_call(0.0, x);
 }
 
 // minmod / superBee limiter of a quotient that is not NaN, with the

@@ -817,6 +817,11 @@ DV double fnv_vertical(const RunView& v, long long na, long long nb) {
 DV double fnv_horizontal(const RunView& v, long long na, long long nb) {
   return plus_zero(half(addz(v.u[v.npitch + na], v.u[v.npitch + nb])));
 }
+// either of the two, by the sweep direction: the component along the sweep
+DV double face_mean(const RunView& v, bool dirx, long long na, long long nb) {
+  const double* u = v.u + (dirx ? 0 : v.npitch);
+  return plus_zero(half(addz(u[na], u[nb])));
+}
 
 // ----------------------------------------------------------- remap sweep
 // Face gradients of one sweep for runs without PenteBorne
@@ -952,27 +957,26 @@ struct SweepGradT {
         if ((z & kMag) == 0 && is_finite(C.dt_n)) {
           put_z(v, c, 3);  // both integral planes all +0.0, not stored
           if (cfd) {
-            const double fl = dirx ? half(ld(v.flv, i) + ld(v.flv, i)) : half(ld(v.flh, j) + ld(v.flh, j));
-            const double zf = 0.0 * fl;
+            const double l = dirx ? ld(v.flv, i) : ld(v.flh, j);
+            const double zf = 0.0 * half(l + l);
             for (int m = 0; m < nb; ++m) v.DPF[m * P + c] = zf;
           }
           return;
         }
       }
-      double Fa, Fb, fa_v, fb_v;
-      if (dirx) {
-        fa_v = fnv_vertical(v, n0, n0 + v.nx + 1);          // left face
-        fb_v = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);      // right face
-        Fa = mul_pm1(fa_v, nout_at(v, 0, c));
-        Fb = mul_pm1(fb_v, nout_at(v, 1, c));
-        flen = half(ld(v.flv, i) + ld(v.flv, i));
-      } else {
-        fa_v = fnv_horizontal(v, n0, n0 + 1);               // bottom face
-        fb_v = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);  // top face
-        Fa = mul_pm1(fa_v, nout_at(v, 2, c));
-        Fb = mul_pm1(fb_v, nout_at(v, 3, c));
-        flen = half(ld(v.flh, j) + ld(v.flh, j));
-      }
+      // the faces' nodes and normals selected by direction, then one set of
+      // operations (two branches, if-converted, would issue both sets): the
+      // left and right faces of an x sweep (fnv_vertical), the bottom and
+      // top faces of a y sweep (fnv_horizontal)
+      const long long W = v.nx + 1;
+      const long long a1 = dirx ? n0 + W : n0 + 1, b0 = dirx ? n0 + 1 : n0 + W;
+      const double fa_v = face_mean(v, dirx, n0, a1);
+      const double fb_v = face_mean(v, dirx, b0, n0 + W + 1);
+      const int qa = dirx ? 0 : 2;
+      const double Fa = mul_pm1(fa_v, nout_at(v, qa, c));
+      const double Fb = mul_pm1(fb_v, nout_at(v, qa + 1, c));
+      const double l = dirx ? ld(v.flv, i) : ld(v.flh, j);
+      flen = half(l + l);
       const double fdual = half(fa_v + fb_v);
       const double dt = C.dt_n;
       ppa = half(Fa + fabs(Fa)) * dt;
@@ -1035,18 +1039,14 @@ struct SweepGradT {
     }
     if (pb == 0) {
       const long long n0 = (long long)i * (v.nx + 1) + j;
-      double fnv_p, fnv_m, xf_p, xf_m;
-      if (dirx) {
-        fnv_m = fnv_vertical(v, n0, n0 + v.nx + 1);
-        fnv_p = fnv_vertical(v, n0 + 1, n0 + v.nx + 2);
-        xf_m = ld(v.xs, j);
-        xf_p = ld(v.xs, j + 1);
-      } else {
-        fnv_p = fnv_horizontal(v, n0, n0 + 1);
-        fnv_m = fnv_horizontal(v, n0 + v.nx + 1, n0 + v.nx + 2);
-        xf_p = ld(v.ys, i);
-        xf_m = ld(v.ys, i + 1);
-      }
+      // x sweep: minus = left face (n0, n0 + W), plus = right face;
+      // y sweep: plus = bottom face (n0, n0 + 1), minus = top face
+      const long long W = v.nx + 1;
+      const long long lo1 = dirx ? n0 + W : n0 + 1, hi0 = dirx ? n0 + 1 : n0 + W;
+      const double f_lo = face_mean(v, dirx, n0, lo1), f_hi = face_mean(v, dirx, hi0, n0 + W + 1);
+      const double fnv_m = dirx ? f_lo : f_hi, fnv_p = dirx ? f_hi : f_lo;
+      const double xf_m = dirx ? ld(v.xs, j) : ld(v.ys, i + 1);
+      const double xf_p = dirx ? ld(v.xs, j + 1) : ld(v.ys, i);
       up_p = has_gp && pos(fnv_p * dxp);   // c is the plus face's back cell
       up_m = has_gm && !pos(fnv_m * dxm);  // c is the minus face's front cell
       sp = plus_zero(xf_p - xc);
@@ -1284,22 +1284,21 @@ struct SweepFaceT {
     const long long P = v.pitch, FP = v.fpitch;
     const int ncomp = v.ncomp;
     long long cb, cf, fidx;
-    double fnv;
     if (dirx) {
       if (i >= v.ny || j < 1 || j >= v.nx) return;
       cb = (long long)i * v.nx + j - 1;  // back = left
       cf = cb + 1;                        // front = right
       fidx = (long long)i * (v.nx + 1) + j;
-      const long long n0 = (long long)i * (v.nx + 1) + j;
-      fnv = fnv_vertical(v, n0, n0 + v.nx + 1);
     } else {
       if (j >= v.nx || i < 1 || i >= v.ny) return;
       cb = (long long)i * v.nx + j;       // back = above
       cf = cb - v.nx;                     // front = below
       fidx = (long long)i * v.nx + j;
-      const long long n0 = (long long)i * (v.nx + 1) + j;
-      fnv = fnv_horizontal(v, n0, n0 + 1);
     }
+    // the face's two nodes: (n0, n0 + W) for an x sweep (fnv_vertical),
+    // (n0, n0 + 1) for a y sweep (fnv_horizontal); one set of operations
+    const long long n0 = (long long)i * (v.nx + 1) + j;
+    const double fnv = face_mean(v, dirx, n0, dirx ? n0 + v.nx + 1 : n0 + 1);
     double* out = v.phiF + fidx;
     const int ax = dirx ? 0 : 1;
     const bool low = (ORDERS == 2) || (ORDERS == 3 && v.order <= 2);
@@ -1976,14 +1975,16 @@ struct DualUpdate {
         const double u = half((ax == 0 ? dn0 : dn1) + (ax == 0 ? dp0 : dp1));
         const double dx = xp - xn;
         const double sdx = pos(u) ? dx : -dx;  // sign(u) * dx
-        if (pos(Fm)) {
-          const double g0 = hasL ? v.gD[L] : 0.0, g1 = hasL ? v.gD[NP + L] : 0.0;
-          um[0] = dn0 + mul_012(order2, half(g0) * (sdx - dt * u));
-          um[1] = dn1 + mul_012(order2, half(g1) * (sdx - dt * u));
-        } else {
-          um[0] = dp0 + mul_012(order2, half(gp0) * (sdx - dt * u));
-          um[1] = dp1 + mul_012(order2, half(gp1) * (sdx - dt * u));
-        }
+        // the upwind node's value and slope, selected before the one
+        // expression both cases share (as two branches, if-converted, both
+        // sets of FP64 operations would be issued)
+        const bool nbr = pos(Fm);
+        const double gn0 = hasL ? v.gD[L] : 0.0, gn1 = hasL ? v.gD[NP + L] : 0.0;
+        const double b0 = nbr ? dn0 : dp0, b1 = nbr ? dn1 : dp1;
+        const double g0 = nbr ? gn0 : gp0, g1 = nbr ? gn1 : gp1;
+        const double w = sdx - dt * u;
+        um[0] = b0 + mul_012(order2, half(g0) * w);
+        um[1] = b1 + mul_012(order2, half(g1) * w);
       }
       // plus side (right / top)
       {
@@ -1992,14 +1993,13 @@ struct DualUpdate {
         const double u = half((ax == 0 ? dp0 : dp1) + (ax == 0 ? dn0 : dn1));
         const double dx = xn - xp;
         const double sdx = pos(u) ? dx : -dx;  // sign(u) * dx
-        if (neg(Fp)) {
-          const double g0 = hasR ? v.gD[R] : 0.0, g1 = hasR ? v.gD[NP + R] : 0.0;
-          up[0] = dn0 + mul_012(order2, half(g0) * (sdx - dt * u));
-          up[1] = dn1 + mul_012(order2, half(g1) * (sdx - dt * u));
-        } else {
-          up[0] = dp0 + mul_012(order2, half(gp0) * (sdx - dt * u));
-          up[1] = dp1 + mul_012(order2, half(gp1) * (sdx - dt * u));
-        }
+        const bool nbr = neg(Fp);
+        const double gn0 = hasR ? v.gD[R] : 0.0, gn1 = hasR ? v.gD[NP + R] : 0.0;
+        const double b0 = nbr ? dn0 : dp0, b1 = nbr ? dn1 : dp1;
+        const double g0 = nbr ? gn0 : gp0, g1 = nbr ? gn1 : gp1;
+        const double w = sdx - dt * u;
+        up[0] = b0 + mul_012(order2, half(g0) * w);
+        up[1] = b1 + mul_012(order2, half(g1) * w);
       }
       Un0 = Ui0 + Fm * um[0] - Fp * up[0];
       Un1 = Ui1 + Fm * um[1] - Fp * up[1];
