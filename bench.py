@@ -127,9 +127,11 @@ def algorithmic_bytes(kind: str, nb: int, pb: bool, rest: bool = False) -> int:
     }
     if rest:
         # a pure cell at rest leaves out the stores of the values it read
-        # and found unchanged: divergence, sound speed, the root's argument
-        # and its material's pseudo-viscosity
-        table["k_lag_cells"] -= 4
+        # and found unchanged (divergence, sound speed, the root's argument,
+        # its material's pseudo-viscosity), and, its Lagrange geometry planes
+        # holding the rest geometry already (one flag byte in), the rest
+        # geometry's four loads past the volume and the five stores
+        table["k_lag_cells"] -= 4 + 4 + 5 - 0.125
     if rest and pb:
         # a cell at rest: the node velocity along the sweep in / its flag
         # byte out; U, 2 node velocities, 2 outer normals and the flag bytes

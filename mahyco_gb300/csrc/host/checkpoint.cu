@@ -30,7 +30,7 @@ namespace hydro {
 namespace {
 
 constexpr char kMagic[8] = {'H', 'G', 'B', '3', 'C', 'K', 'P', 'T'};
-constexpr uint32_t kVersion = 4;
+constexpr uint32_t kVersion = 5;
 constexpr size_t kChunk = 64u << 20;
 
 struct Header {

@@ -125,6 +125,7 @@ size_t layout(RunView& v, char* base) {
     v.cqs = v.cflsq = v.s0 = v.sqs0 = nullptr;
     v.sarg = nullptr;
     v.nsym = nullptr;
+    v.gL = nullptr;
     v.geo0 = a.take<double>(5 * P);
     v.uc = a.take<double>(2 * P);
     v.uco = a.take<double>(2 * P);
@@ -140,6 +141,7 @@ size_t layout(RunView& v, char* base) {
     v.evol = a.take<double>(P);
   } else {
     v.geo0 = a.take<double>(5 * P);
+    v.gL = a.take<unsigned char>(P);
     v.sarg = a.take<double>(P);
     v.nsym = a.take<unsigned char>(NP);
     v.cqs = a.take<double>(8 * P);

@@ -124,6 +124,8 @@ struct RunView {
                       // or kNoRoot where c came otherwise
   const double* geo0; // 5 cell planes, the Lagrangian geometry of the cell
                       // at rest (volume, centroid x / y, widths x / y)
+  unsigned char* gL;  // VNR: per cell, 1 where vL, XcL, Hx, Hy hold the
+                      // rest geometry (geo0) bit for bit; null otherwise
   double* o3g;        // order 3: ncomp cell planes, each cell's limited-free
                       // gradient along the sweep (eval_grad); null otherwise
                       // and in batched launches, which work per face

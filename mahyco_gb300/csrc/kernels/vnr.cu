@@ -437,9 +437,17 @@ struct LagCells {
     // comparison below, its latency does not)
     double g0v[5] = {0., 0., 0., 0., 0.};
     bool rest = v.geo0 != nullptr;
+    // gL: this cell's Lagrange geometry planes (vL, XcL, Hx, Hy) already
+    // hold the rest geometry, stored when the cell was last found at rest;
+    // a cell at rest again then needs only the volume from it, and stores
+    // none of them
+    const bool held = v.gL && v.projection == 1 && v.gL[c] != 0;
     if (rest) {
+      g0v[0] = ld(v.geo0, c);
+      if (!held) {
   #pragma unroll
-      for (int q = 0; q < 5; ++q) g0v[q] = ld(v.geo0, q * P + c);
+        for (int q = 1; q < 5; ++q) g0v[q] = ld(v.geo0, q * P + c);
+      }
     }
     if (rest) {
       const unsigned long long x0 = ubits(ld(v.xs, j)), x1 = ubits(ld(v.xs, j + 1));
@@ -793,16 +801,19 @@ struct LagCells {
         }
       }
     }
-    v.vL[c] = vol;
     v.rL[c] = rho_new;
-    // Lagrangian centroid (PrepareRemap.cc:65-90) and the widths behind
-    // HvLagrange for both sweep directions
-    v.XcL[c] = G.xc0;
-    v.XcL[P + c] = G.xc1;
-    if (v.order > 1) {
-      v.Hx[c] = G.hx;
-      v.Hy[c] = G.hy;
+    if (!(rest && held)) {
+      v.vL[c] = vol;
+      // Lagrangian centroid (PrepareRemap.cc:65-90) and the widths behind
+      // HvLagrange for both sweep directions
+      v.XcL[c] = G.xc0;
+      v.XcL[P + c] = G.xc1;
+      if (v.order > 1) {
+        v.Hx[c] = G.hx;
+        v.Hy[c] = G.hy;
+      }
     }
+    if (v.gL && v.projection == 1 && rest != held) v.gL[c] = rest ? 1 : 0;
   }
 };
 
