@@ -108,6 +108,8 @@ const char* hydro_last_error(void);
 int hydro_spec_default(hydro_spec* spec);
 int hydro_spec_parse_deck(const char* path, hydro_spec* spec);
 
+/* A context owns a stream on the device, the pinned staging (3 x 8 MiB) and
+ * the host copy threads through which hydro_run_fetch hands fields over. */
 int hydro_ctx_create(int device, size_t hbm_budget_bytes, hydro_ctx** out);
 void hydro_ctx_destroy(hydro_ctx* ctx);
 
@@ -121,7 +123,8 @@ int hydro_run_step(hydro_run* run, int ncycles, int* done);
  * cycle: "Pressure", "Density", "Energy", VNR "fracvol1", "fracvol2" (cell)
  * and "VitesseX", "VitesseY" (node), Eucclhyd "F1".."F3", "VelocityX",
  * "VelocityY" (vnr_remap/VnrRemap.cc:264-278, eucclhyd_remap/EucclhydRemap.cc
- * :43-50). */
+ * :43-50).  Returns once the values are in host_dst (any host memory); the
+ * fetches of one context run one at a time. */
 int hydro_run_fetch(hydro_run* run, const char* field, double* host_dst,
                     size_t n);
 size_t hydro_run_field_size(hydro_run* run, const char* field);
